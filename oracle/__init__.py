@@ -1,0 +1,261 @@
+"""ctypes binding of the CPU oracle (oracle/rsh_oracle.cpp). TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, by __graft_entry__.smoke() as the checker and by bench.py's cpu_baseline / reference
+legs; the product (ray-tracer_gb300/) never imports it. `build()` compiles liboracle.so with g++.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+SRC = HERE / "rsh_oracle.cpp"
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-shared"]
+
+KEY_NONE = 0xFFFFFFFF
+HIT_NONE = 0xFFFFFFFFFFFFFFFF
+OCCLUDED = 0xFFFFFFFF
+
+RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
+NODE_DTYPE = np.dtype([("c", "<f4", 3), ("radius", "<f4"), ("axis", "<f4", 3), ("cos_spread", "<f4"),
+                       ("sin_spread", "<f4"), ("reach", "<f4"), ("first", "<u4"), ("count", "<u4")])
+
+
+def build(force: bool = False) -> Path:
+    if LIB.exists() and not force and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = LIB.with_suffix(".so.tmp")
+    r = subprocess.run([cxx, *CXXFLAGS, "-o", str(tmp), str(SRC)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(LIB))
+        P, U32, U64, F, I = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
+        sig = {
+            "orc_num_threads": (C.c_int, []),
+            "orc_set_threads": (None, [C.c_int]),
+            "orc_hash_params": (None, [P, P, U32, P]),
+            "orc_hash": (None, [P, U32, P, P, U32, U32, U32, P]),
+            "orc_raygen_primary": (None, [P, U32, U32, P, P]),
+            "orc_raygen_shadow": (None, [P, P, U32, U32, P, U32, F, P, P, U32, U32, P, P]),
+            "orc_raygen_reflect": (None, [P, P, P, P, U32, U32, F, F, U32, U32, P, P, U32, U32, P, P]),
+            "orc_compress": (None, [P, U32, P, P, P, P, P]),
+            "orc_sort_pairs": (None, [P, P, U32, U32, P, P]),
+            "orc_decompress": (None, [P, P, P, P, U32, U32, P, P]),
+            "orc_hierarchy_offsets": (U32, [U32, U32, P]),
+            "orc_build_rsh": (None, [P, P, U32, U32, U32, P]),
+            "orc_objh_build": (P, [P, U32, U32, P, P]),
+            "orc_objh_free": (None, [P]),
+            "orc_objh_levels": (U32, [P]),
+            "orc_objh_level_size": (U32, [P, U32]),
+            "orc_objh_get": (None, [P, P, P, P]),
+            "orc_traverse": (U64, [P, P, U32, U32, U32, P, U64, P]),
+            "orc_intersect": (None, [P, P, P, U32, U32, P, U64, I, P, P]),
+            "orc_brute": (None, [P, U32, P, U32, I, P, P]),
+            "orc_brute_second": (None, [P, U32, P, U32, P, P]),
+            "orc_resolve": (None, [P, P, P, P, P, P, U32, P, P]),
+            "orc_trace_keyed": (U32, [P, P, P, U32, U32, U32, I, P, P, P, P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(_lib, name)
+            fn.restype = res
+            fn.argtypes = args
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, np.uint32)
+
+
+def threads() -> int:
+    return lib().orc_num_threads()
+
+
+def hash_scale(lo, hi, grid_bits: int) -> np.ndarray:
+    out = np.zeros(3, np.float32)
+    lib().orc_hash_params(_p(_f32(lo)), _p(_f32(hi)), grid_bits, _p(out))
+    return out
+
+
+def hash_rays(rays, lo, scale, g, b, tag=0):
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    keys = np.empty(len(rays), np.uint32)
+    lib().orc_hash(_p(rays), len(rays), _p(_f32(lo)), _p(_f32(scale)), g, b, tag, _p(keys))
+    return keys
+
+
+def raygen_primary(cam: np.ndarray, W: int, H: int):
+    n = ((W + 7) // 8) * ((H + 7) // 8) * 64
+    rays = np.zeros(n, RAY_DTYPE)
+    pix = np.zeros(n, np.uint32)
+    lib().orc_raygen_primary(_p(_f32(cam)), W, H, _p(rays), _p(pix))
+    return rays, pix
+
+
+def raygen_shadow(spos, snrm, W, H, light_pos, eps, lo, scale, g, b):
+    light_pos = _f32(np.asarray(light_pos).reshape(-1, 3))
+    L = light_pos.shape[0]
+    rays = np.zeros(W * H * L, RAY_DTYPE)
+    keys = np.empty(W * H * L, np.uint32)
+    lib().orc_raygen_shadow(_p(_f32(spos)), _p(_f32(snrm)), W, H, _p(light_pos), L, float(eps), _p(_f32(lo)),
+                            _p(_f32(scale)), g, b, _p(rays), _p(keys))
+    return rays, keys
+
+
+def raygen_reflect(spos, snrm, prev, eye, W, H, eps, jitter, seed, bounce, lo, scale, g, b):
+    rays = np.zeros(W * H, RAY_DTYPE)
+    keys = np.empty(W * H, np.uint32)
+    prev = None if prev is None else np.ascontiguousarray(prev, RAY_DTYPE)
+    lib().orc_raygen_reflect(_p(_f32(spos)), _p(_f32(snrm)), _p(prev), _p(_f32(eye)), W, H, float(eps), float(jitter),
+                             seed, bounce, _p(_f32(lo)), _p(_f32(scale)), g, b, _p(rays), _p(keys))
+    return rays, keys
+
+
+def compress(keys):
+    keys = _u32(keys)
+    n = len(keys)
+    trimmed = np.zeros(max(n, 1), np.uint32)
+    ck = np.zeros(n + 1, np.uint32)
+    cb = np.zeros(n + 1, np.uint32)
+    cs = np.zeros(n + 1, np.uint32)
+    counts = np.zeros(2, np.uint32)
+    lib().orc_compress(_p(keys), n, _p(trimmed), _p(ck), _p(cb), _p(cs), _p(counts))
+    R, Cc = int(counts[0]), int(counts[1])
+    return trimmed[:R], ck[:Cc], cb[:Cc + 1], cs[:Cc]
+
+
+def sort_pairs(keys, vals, key_bits):
+    keys = _u32(keys)
+    n = len(keys)
+    ko = np.empty(n, np.uint32)
+    vo = np.empty(n, np.uint32)
+    lib().orc_sort_pairs(_p(keys), _p(None if vals is None else _u32(vals)), n, key_bits, _p(ko), _p(vo))
+    return ko, vo
+
+
+def decompress(skeys, svals, cbases, trimmed):
+    R = len(trimmed)
+    Cc = len(svals)
+    sk = np.empty(R, np.uint32)
+    si = np.empty(R, np.uint32)
+    lib().orc_decompress(_p(_u32(skeys)), _p(_u32(svals)), _p(_u32(cbases)), _p(_u32(trimmed)), R, Cc, _p(sk), _p(si))
+    return sk, si
+
+
+def build_rsh(rays, ids, n, P, max_rays=None):
+    max_rays = n if max_rays is None else max_rays
+    off = np.zeros(4, np.uint32)
+    cap = lib().orc_hierarchy_offsets(max_rays, P, _p(off))
+    nodes = np.zeros(max(cap, 1), NODE_DTYPE)
+    lib().orc_build_rsh(_p(np.ascontiguousarray(rays, RAY_DTYPE)), _p(None if ids is None else _u32(ids)), n,
+                        max_rays, P, _p(nodes))
+    return nodes, off
+
+
+class ObjH:
+    def __init__(self, positions, cluster, lo, hi):
+        self.positions = _f32(positions).reshape(-1, 12)
+        self.T = self.positions.shape[0]
+        self.h = lib().orc_objh_build(_p(self.positions), self.T, cluster, _p(_f32(lo)), _p(_f32(hi)))
+        self.cluster = cluster
+
+    def levels(self):
+        return [lib().orc_objh_level_size(self.h, l) for l in range(lib().orc_objh_levels(self.h))]
+
+    def arrays(self):
+        total = sum(self.levels())
+        order = np.empty(self.T, np.uint32)
+        tris = np.empty((self.T, 12), np.float32)
+        sph = np.empty((max(total, 1), 4), np.float32)
+        lib().orc_objh_get(self.h, _p(order), _p(tris), _p(sph))
+        return order, tris, sph[:total]
+
+    def traverse(self, nodes, n, P, max_rays=None, cap=1 << 28):
+        max_rays = n if max_rays is None else max_rays
+        tests = np.zeros(1, np.uint64)
+        cnt = lib().orc_traverse(self.h, _p(nodes), n, max_rays, P, None, 0, _p(tests))
+        cand = np.empty(max(int(cnt), 1), np.uint64)
+        lib().orc_traverse(self.h, _p(nodes), n, max_rays, P, _p(cand), cnt, None)
+        return cand[:cnt], int(tests[0])
+
+    def intersect(self, rays, ids, n, P, cand, any_hit, n_slots):
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        flags = np.zeros(n_slots, np.uint32)
+        hits = np.full(n_slots, HIT_NONE, np.uint64)
+        cand = np.ascontiguousarray(cand, np.uint64)
+        lib().orc_intersect(self.h, _p(rays), _p(None if ids is None else _u32(ids)), n, P, _p(cand), len(cand),
+                            int(any_hit), _p(flags), _p(hits))
+        return flags if any_hit else hits
+
+    def trace_keyed(self, rays, keys, key_bits, P, any_hit):
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        keys = _u32(keys)
+        n = len(keys)
+        flags = np.zeros(n, np.uint32)
+        hits = np.full(n, HIT_NONE, np.uint64)
+        ms = np.zeros(8, np.float32)
+        ctr = np.zeros(2, np.uint64)
+        R = lib().orc_trace_keyed(self.h, _p(rays), _p(keys), n, key_bits, P, int(any_hit), _p(flags), _p(hits),
+                                  _p(ms), _p(ctr))
+        return (flags if any_hit else hits), int(R), ms, ctr
+
+    def __del__(self):
+        try:
+            lib().orc_objh_free(self.h)
+        except Exception:
+            pass
+
+
+def brute(positions, rays, any_hit):
+    pos = _f32(positions).reshape(-1, 12)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    n = len(rays)
+    flags = np.zeros(n, np.uint32)
+    hits = np.full(n, HIT_NONE, np.uint64)
+    lib().orc_brute(_p(pos), pos.shape[0], _p(rays), n, int(any_hit), _p(flags), _p(hits))
+    return flags if any_hit else hits
+
+
+def brute_two_nearest(positions, rays):
+    pos = _f32(positions).reshape(-1, 12)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    n = len(rays)
+    t1 = np.empty(n, np.float32)
+    t2 = np.empty(n, np.float32)
+    lib().orc_brute_second(_p(pos), pos.shape[0], _p(rays), n, _p(t1), _p(t2))
+    return t1, t2
+
+
+def resolve(positions, normals, mat, rays, hits, pix, npix):
+    spos = np.zeros((npix, 4), np.float32)
+    snrm = np.zeros((npix, 4), np.float32)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    lib().orc_resolve(_p(_f32(positions)), _p(_f32(normals)), _p(None if mat is None else _u32(mat)), _p(rays),
+                      _p(np.ascontiguousarray(hits, np.uint64)), _p(None if pix is None else _u32(pix)), len(rays),
+                      _p(spos), _p(snrm))
+    return spos, snrm

@@ -1,0 +1,981 @@
+/*
+ * rsh_oracle.cpp — CPU ORACLE for the ray-space-hierarchy secondary-ray path. TEST INFRASTRUCTURE ONLY:
+ * imported by tests/, by __graft_entry__.smoke() as the checker, and by bench.py's cpu_baseline /
+ * reference legs. The product library never links or calls it.
+ *
+ * Parity: the reference (nuno-tiago-reis/ray-tracer, projects/CUDA-Engine) cannot be built here (CUDA 6.5
+ * headers, texture references, Win32/GL) and ships no CPU path, no golden vectors and no known-answer
+ * tests for this path. This file restates the reference's algorithm stage by stage, citing the lines it
+ * follows, with the arithmetic the GPU port defines where the reference is replaced (hash, conservative
+ * nodes, watertight test, 64-bit hit key). The brute-force any/closest hit (as CUDA-Naive-Engine,
+ * RayTracer.cu:276-291 and :344-360) is the independent end-to-end check. Parity against the reference's
+ * own outputs is UNPINNED: only order-of-magnitude sanity ranges exist (output/tests/configuration-n8).
+ *
+ * Numerics: compile with -ffp-contract=off (no FMA contraction); every expression below uses the same
+ * operation order as the GPU kernels so that keys, run heads, permutations, nodes, candidates and hit
+ * records are reproduced bit for bit.
+ */
+#include <omp.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+
+namespace {
+
+const uint32_t KEY_NONE = 0xFFFFFFFFu;
+const uint64_t HIT_NONE = 0xFFFFFFFFFFFFFFFFull;
+const uint32_t OCCLUDED = 0xFFFFFFFFu;
+const float INF = std::numeric_limits<float>::infinity();
+
+struct V3 {
+    float x, y, z;
+};
+inline V3 sub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 mul(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
+inline float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) { return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float length(V3 a) { return std::sqrt(dot(a, a)); }
+inline V3 normalize(V3 a) {
+    const float l = length(a);
+    return V3{a.x / l, a.y / l, a.z / l};
+}
+
+struct Ray {  // same 32-byte layout as rsh_ray
+    float o[3];
+    float tmin;
+    float d[3];
+    float tmax;
+};
+struct Node {  // same 48-byte layout as rsh_node
+    float c[3];
+    float radius;
+    float axis[3];
+    float cos_spread;
+    float sin_spread;
+    float reach;
+    uint32_t first;
+    uint32_t count;
+};
+struct HashP {
+    float lo[3], scale[3];
+    uint32_t g, b;
+};
+
+inline uint32_t spread3(uint32_t v) {
+    uint32_t r = 0;
+    for (int i = 0; i < 10; ++i) r |= ((v >> i) & 1u) << (3 * i);
+    return r;
+}
+inline uint32_t spread2(uint32_t v) {
+    uint32_t r = 0;
+    for (int i = 0; i < 16; ++i) r |= ((v >> i) & 1u) << (2 * i);
+    return r;
+}
+
+// 32-bit ray hash: tag | morton3(origin cell) | morton2(octahedral direction bin). Replaces
+// CreateShadowRayIndex / CreateReflectionRayIndex (RayTracer.cu:147-198), whose atan2(x, x) is constant.
+uint32_t ray_hash(const float o[3], const float d[3], const HashP& hp, uint32_t tag) {
+    const float gmax = (float)((1u << hp.g) - 1u);
+    uint32_t c[3];
+    for (int i = 0; i < 3; ++i) {
+        float f = (o[i] - hp.lo[i]) * hp.scale[i];
+        f = std::fmin(std::fmax(f, 0.0f), gmax);
+        c[i] = (uint32_t)f;
+    }
+    const uint32_t cell = (spread3(c[0]) << 2) | (spread3(c[1]) << 1) | spread3(c[2]);
+    const float s = (std::fabs(d[0]) + std::fabs(d[1])) + std::fabs(d[2]);
+    float px = d[0] / s, py = d[1] / s;
+    if (d[2] < 0.0f) {
+        const float qx = 1.0f - std::fabs(py), qy = 1.0f - std::fabs(px);
+        px = (px >= 0.0f) ? qx : -qx;
+        py = (py >= 0.0f) ? qy : -qy;
+    }
+    const uint32_t B = 1u << hp.b;
+    const float half_b = 0.5f * (float)B, bmax = (float)(B - 1u);
+    float u = (px + 1.0f) * half_b, v = (py + 1.0f) * half_b;
+    u = std::fmin(std::fmax(u, 0.0f), bmax);
+    v = std::fmin(std::fmax(v, 0.0f), bmax);
+    const uint32_t dir = (spread2((uint32_t)u) << 1) | spread2((uint32_t)v);
+    const uint32_t dbits = 2u * hp.b, hbits = 3u * hp.g + dbits;
+    return (tag << hbits) | (cell << dbits) | dir;
+}
+
+HashP mkhp(const float* lo, const float* scale, uint32_t g, uint32_t b) {
+    HashP h;
+    for (int i = 0; i < 3; ++i) {
+        h.lo[i] = lo[i];
+        h.scale[i] = scale[i];
+    }
+    h.g = g;
+    h.b = b;
+    return h;
+}
+
+// ------------------------------------------------------------- watertight test (Woop et al. 2013)
+struct RayWT {
+    float o[3], s[3];
+    int kx, ky, kz;
+    float tmin, tmax;
+};
+inline RayWT wt_setup(const Ray& r) {
+    RayWT w;
+    const float ax = std::fabs(r.d[0]), ay = std::fabs(r.d[1]), az = std::fabs(r.d[2]);
+    int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    const float dz = r.d[kz];
+    if (dz < 0.0f) std::swap(kx, ky);
+    w.kx = kx;
+    w.ky = ky;
+    w.kz = kz;
+    w.s[0] = r.d[kx] / dz;
+    w.s[1] = r.d[ky] / dz;
+    w.s[2] = 1.0f / dz;
+    for (int i = 0; i < 3; ++i) w.o[i] = r.o[i];
+    w.tmin = r.tmin;
+    w.tmax = r.tmax;
+    return w;
+}
+inline bool wt_hit(const RayWT& r, const float* p0, const float* p1, const float* p2, float& t_out) {
+    const float A[3] = {p0[0] - r.o[0], p0[1] - r.o[1], p0[2] - r.o[2]};
+    const float B[3] = {p1[0] - r.o[0], p1[1] - r.o[1], p1[2] - r.o[2]};
+    const float C[3] = {p2[0] - r.o[0], p2[1] - r.o[1], p2[2] - r.o[2]};
+    const float Ax = A[r.kx] - r.s[0] * A[r.kz], Ay = A[r.ky] - r.s[1] * A[r.kz];
+    const float Bx = B[r.kx] - r.s[0] * B[r.kz], By = B[r.ky] - r.s[1] * B[r.kz];
+    const float Cx = C[r.kx] - r.s[0] * C[r.kz], Cy = C[r.ky] - r.s[1] * C[r.kz];
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = (U + V) + W;
+    if (det == 0.0f) return false;
+    const float Az = r.s[2] * A[r.kz], Bz = r.s[2] * B[r.kz], Cz = r.s[2] * C[r.kz];
+    const float T = (U * Az + V * Bz) + W * Cz;
+    const float t = T / det;
+    t_out = t;
+    return t > r.tmin && t < r.tmax;
+}
+inline uint64_t hit_key(float t, uint32_t tri) {
+    uint32_t b;
+    std::memcpy(&b, &t, 4);
+    return ((uint64_t)b << 32) | tri;
+}
+inline float u2f(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+inline uint32_t f2u(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+// ------------------------------------------------------------- node test (RayTracer.cu:283-298 + reach)
+inline bool node_hits_sphere(const Node& p, const float* s) {
+    const float vx = s[0] - p.c[0], vy = s[1] - p.c[1], vz = s[2] - p.c[2];
+    const float dd = (vx * vx + vy * vy) + vz * vz;
+    const float dist = std::sqrt(dd);
+    const float rr = p.radius + s[3];
+    const float slack = (dist + rr) * 1e-5f;
+    if (dist - s[3] > p.reach + slack) return false;
+    if (p.cos_spread > 0.0f) {
+        const float t = (vx * p.axis[0] + vy * p.axis[1]) + vz * p.axis[2];
+        const float wx = vy * p.axis[2] - vz * p.axis[1];
+        const float wy = vz * p.axis[0] - vx * p.axis[2];
+        const float wz = vx * p.axis[1] - vy * p.axis[0];
+        const float perp = std::sqrt((wx * wx + wy * wy) + wz * wz);
+        if (perp * p.cos_spread - t * p.sin_spread > rr + slack) return false;
+    }
+    return true;
+}
+
+const float kRadSlack = 1.0f + 1.0f / 1048576.0f;
+const float kCosMargin = 4e-6f;
+
+// pairwise tree sum in index order with zero padding to a power of two (= the GPU xor butterfly)
+float tree_sum(std::vector<float> v) {
+    size_t n = 1;
+    while (n < v.size()) n <<= 1;
+    v.resize(n, 0.0f);
+    for (size_t s = 1; s < n; s <<= 1)
+        for (size_t i = 0; i + s < n; i += 2 * s) v[i] = v[i] + v[i + s];
+    return v[0];
+}
+
+// Leaf of the ray hierarchy (CreateHierarchyLevel0, RayTracer.cu:1061-1108, made conservative).
+Node make_leaf(const Ray* rays, const uint32_t* ids, uint32_t n, uint32_t k0, uint32_t P) {
+    std::vector<Ray> r;
+    std::vector<char> act;
+    for (uint32_t j = 0; j < P; ++j) {
+        const uint32_t k = k0 + j;
+        Ray x{};
+        bool a = k < n;
+        if (a) {
+            x = rays[ids ? ids[k] : k];
+            a = x.tmax > x.tmin;
+        }
+        r.push_back(x);
+        act.push_back(a);
+    }
+    float mn[3] = {INF, INF, INF}, mx[3] = {-INF, -INF, -INF};
+    std::vector<float> sx(P), sy(P), sz(P);
+    uint32_t cnt = 0;
+    for (uint32_t j = 0; j < P; ++j) {
+        if (act[j]) {
+            ++cnt;
+            for (int i = 0; i < 3; ++i) {
+                mn[i] = std::fmin(mn[i], r[j].o[i]);
+                mx[i] = std::fmax(mx[i], r[j].o[i]);
+            }
+        }
+        sx[j] = act[j] ? r[j].d[0] : 0.0f;
+        sy[j] = act[j] ? r[j].d[1] : 0.0f;
+        sz[j] = act[j] ? r[j].d[2] : 0.0f;
+    }
+    const float Sx = tree_sum(sx), Sy = tree_sum(sy), Sz = tree_sum(sz);
+    const V3 c = V3{(mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f};
+    const float sl = std::sqrt((Sx * Sx + Sy * Sy) + Sz * Sz);
+    bool full = !(sl > 1e-20f);
+    const V3 a = full ? V3{0.f, 0.f, 1.f} : V3{Sx / sl, Sy / sl, Sz / sl};
+    float mr2 = 0.0f, dt = INF, rc = 0.0f;
+    for (uint32_t j = 0; j < P; ++j) {
+        if (!act[j]) continue;
+        const V3 oc = V3{r[j].o[0] - c.x, r[j].o[1] - c.y, r[j].o[2] - c.z};
+        const float r2 = dot(oc, oc);
+        mr2 = std::fmax(mr2, r2);
+        dt = std::fmin(dt, dot(a, V3{r[j].d[0], r[j].d[1], r[j].d[2]}));
+        rc = std::fmax(rc, std::sqrt(r2) + r[j].tmax);
+    }
+    const float cs = dt - kCosMargin;
+    if (!(cs > 0.0f)) full = true;
+    Node nd{};
+    nd.c[0] = c.x;
+    nd.c[1] = c.y;
+    nd.c[2] = c.z;
+    nd.radius = std::sqrt(mr2) * kRadSlack;
+    nd.axis[0] = a.x;
+    nd.axis[1] = a.y;
+    nd.axis[2] = a.z;
+    nd.cos_spread = full ? -1.0f : cs;
+    nd.sin_spread = full ? 0.0f : std::sqrt((1.0f - cs) * (1.0f + cs));
+    nd.reach = rc * kRadSlack;
+    nd.first = k0;
+    nd.count = cnt;
+    return nd;
+}
+
+// Upper level (CreateHierarchyLevelN, RayTracer.cu:1110-1150, made conservative).
+Node merge_nodes(const Node* ch, uint32_t m) {
+    float mn[3] = {INF, INF, INF}, mx[3] = {-INF, -INF, -INF};
+    uint32_t count = 0;
+    bool full = false;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (uint32_t i = 0; i < m; ++i) {
+        const Node& q = ch[i];
+        if (q.count == 0) continue;
+        count += q.count;
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = std::fmin(mn[k], q.c[k] - q.radius);
+            mx[k] = std::fmax(mx[k], q.c[k] + q.radius);
+        }
+        if (!(q.cos_spread > 0.f)) full = true;
+        const float w = (float)q.count;
+        sx = sx + q.axis[0] * w;
+        sy = sy + q.axis[1] * w;
+        sz = sz + q.axis[2] * w;
+    }
+    Node nd{};
+    nd.first = ch[0].first;
+    nd.count = count;
+    const V3 c = V3{(mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f};
+    const float sl = std::sqrt((sx * sx + sy * sy) + sz * sz);
+    if (!(sl > 1e-20f)) full = true;
+    const V3 a = full ? V3{0.f, 0.f, 1.f} : V3{sx / sl, sy / sl, sz / sl};
+    float rad = 0.f, reach = 0.f, cs = 1.f;
+    for (uint32_t i = 0; i < m; ++i) {
+        const Node& q = ch[i];
+        if (q.count == 0) continue;
+        const V3 dc = V3{q.c[0] - c.x, q.c[1] - c.y, q.c[2] - c.z};
+        const float dl = length(dc);
+        rad = std::fmax(rad, dl + q.radius);
+        reach = std::fmax(reach, dl + q.reach);
+        if (!full) {
+            float ca = dot(a, V3{q.axis[0], q.axis[1], q.axis[2]});
+            ca = std::fmin(std::fmax(ca, -1.f), 1.f);
+            const float sa = std::sqrt((1.f - ca) * (1.f + ca));
+            cs = std::fmin(cs, ca * q.cos_spread - sa * q.sin_spread);
+        }
+    }
+    cs = cs - kCosMargin;
+    if (!(cs > 0.f)) full = true;
+    nd.c[0] = c.x;
+    nd.c[1] = c.y;
+    nd.c[2] = c.z;
+    nd.radius = rad * kRadSlack;
+    nd.axis[0] = a.x;
+    nd.axis[1] = a.y;
+    nd.axis[2] = a.z;
+    nd.cos_spread = full ? -1.f : cs;
+    nd.sin_spread = full ? 0.f : std::sqrt((1.f - cs) * (1.f + cs));
+    nd.reach = reach * kRadSlack;
+    if (count == 0) {
+        nd.c[0] = nd.c[1] = nd.c[2] = 0.f;
+        nd.radius = 0.f;
+        nd.reach = 0.f;
+    }
+    return nd;
+}
+
+struct ObjH {
+    uint32_t T = 0, cluster = 8, levels = 0;
+    uint32_t off[16] = {}, size[16] = {};
+    std::vector<float> sph;   // 4 per node
+    std::vector<float> tris;  // 12 per triangle, cluster order, w of vertex 0 = original id bits
+    std::vector<uint32_t> order;
+};
+
+void traverse_packet(const Node& p, const ObjH& h, uint32_t L, uint32_t idx, std::vector<uint32_t>& clusters,
+                     uint64_t& tests) {
+    // children of (L, idx): level L-1 nodes [8 idx, ...) or the top level for the virtual root
+    const uint32_t cl = L - 1;
+    const uint32_t first = (L == h.levels) ? 0 : 8 * idx;
+    const uint32_t cnt = std::min<uint32_t>(8, h.size[cl] - first);
+    for (uint32_t c = 0; c < cnt; ++c) {
+        const float* s = &h.sph[4ull * (h.off[cl] + first + c)];
+        ++tests;
+        if (!node_hits_sphere(p, s)) continue;
+        if (cl == 0) clusters.push_back(first + c);
+        else traverse_packet(p, h, cl, first + c, clusters, tests);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_num_threads(void) { return omp_get_max_threads(); }
+void orc_set_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+}
+
+// ---------------------------------------------------------------- hashing / raygen
+void orc_hash_params(const float lo[3], const float hi[3], uint32_t g, float scale_out[3]) {
+    const float G = (float)(1u << g);
+    for (int i = 0; i < 3; ++i) {
+        const float ext = hi[i] - lo[i];
+        scale_out[i] = ext > 0.0f ? G / ext : 0.0f;
+    }
+}
+
+void orc_hash(const float* rays, uint32_t n, const float lo[3], const float scale[3], uint32_t g, uint32_t b,
+              uint32_t tag, uint32_t* keys) {
+    const HashP hp = mkhp(lo, scale, g, b);
+    const Ray* r = reinterpret_cast<const Ray*>(rays);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i)
+        keys[i] = (r[i].tmax > r[i].tmin) ? ray_hash(r[i].o, r[i].d, hp, tag) : KEY_NONE;
+}
+
+// Camera ray (CUDA-Naive-Ray-Tracer RayTracer.cu:606-607; RayTracer.cu:666-667) in 8x8 tile order.
+void orc_raygen_primary(const float* cam /*eye,dir,right,up*/, uint32_t W, uint32_t H, float* rays_out,
+                        uint32_t* pix_out) {
+    const uint32_t tx = (W + 7) / 8, ty = (H + 7) / 8, n = tx * ty * 64;
+    Ray* rays = reinterpret_cast<Ray*>(rays_out);
+#pragma omp parallel for schedule(static)
+    for (int64_t kk = 0; kk < (int64_t)n; ++kk) {
+        const uint32_t k = (uint32_t)kk;
+        const uint32_t tile = k >> 6, within = k & 63u;
+        const uint32_t x = (tile % tx) * 8 + (within & 7u), y = (tile / tx) * 8 + (within >> 3);
+        Ray r{};
+        r.o[0] = cam[0];
+        r.o[1] = cam[1];
+        r.o[2] = cam[2];
+        r.tmin = 0.0f;
+        if (x < W && y < H) {
+            const float a = (float)x / (float)W - 0.5f, b = (float)y / (float)H - 0.5f;
+            const V3 q = V3{(cam[3] + cam[6] * a) + cam[9] * b, (cam[4] + cam[7] * a) + cam[10] * b,
+                            (cam[5] + cam[8] * a) + cam[11] * b};
+            const V3 d = normalize(q);
+            r.d[0] = d.x;
+            r.d[1] = d.y;
+            r.d[2] = d.z;
+            r.tmax = INF;
+            if (pix_out) pix_out[k] = y * W + x;
+        } else {
+            r.d[0] = 0.f;
+            r.d[1] = 0.f;
+            r.d[2] = 1.f;
+            r.tmax = -1.0f;
+            if (pix_out) pix_out[k] = 0xFFFFFFFFu;
+        }
+        rays[k] = r;
+    }
+}
+
+// CreateShadowRays (RayTracer.cu:682-740): origin at the light, direction to the surface point, kept iff
+// N.(-d) > 0; the test interval is (eps, |light - p| - 2 eps) from the eps-offset origin (:1607-1611).
+void orc_raygen_shadow(const float* spos, const float* snrm, uint32_t W, uint32_t H, const float* light_pos,
+                       uint32_t L, float eps, const float lo[3], const float scale[3], uint32_t g, uint32_t b,
+                       float* rays_out, uint32_t* keys) {
+    const HashP hp = mkhp(lo, scale, g, b);
+    Ray* rays = reinterpret_cast<Ray*>(rays_out);
+    const uint64_t n = (uint64_t)W * H * L;
+#pragma omp parallel for schedule(static)
+    for (int64_t si = 0; si < (int64_t)n; ++si) {
+        const uint32_t slot = (uint32_t)si;
+        const uint32_t x = slot % W, l = (slot / W) % L, y = slot / (W * L);
+        const uint32_t pix = y * W + x;
+        uint32_t key = KEY_NONE;
+        if (spos[4ull * pix + 3] != 0.0f) {
+            const V3 p = V3{spos[4ull * pix], spos[4ull * pix + 1], spos[4ull * pix + 2]};
+            const V3 nn = normalize(V3{snrm[4ull * pix], snrm[4ull * pix + 1], snrm[4ull * pix + 2]});
+            const V3 lp = V3{light_pos[3 * l], light_pos[3 * l + 1], light_pos[3 * l + 2]};
+            const V3 v = sub(p, lp);
+            const float len = length(v);
+            const V3 d = V3{v.x / len, v.y / len, v.z / len};
+            const float diffuse = dot(d, V3{-nn.x, -nn.y, -nn.z});
+            const float tmax = len - 2.0f * eps;
+            if (diffuse > 0.0f && tmax > eps) {
+                const V3 o = add(lp, mul(d, eps));
+                Ray r;
+                r.o[0] = o.x;
+                r.o[1] = o.y;
+                r.o[2] = o.z;
+                r.tmin = eps;
+                r.d[0] = d.x;
+                r.d[1] = d.y;
+                r.d[2] = d.z;
+                r.tmax = tmax;
+                rays[slot] = r;
+                key = ray_hash(r.o, r.d, hp, l);
+            }
+        }
+        keys[slot] = key;
+    }
+}
+
+static uint32_t rng_next(uint32_t& state) {
+    state = state * 747796405u + 2891336453u;
+    const uint32_t w = ((state >> ((state >> 28) + 4u)) ^ state) * 277803737u;
+    return (w >> 22) ^ w;
+}
+// Marsaglia (1972): uniform point on the unit sphere by rejection (sqrt only).
+static V3 sphere_sample(uint32_t seed, uint32_t slot, uint32_t bounce) {
+    uint32_t st = seed ^ (slot * 0x9E3779B9u) ^ (bounce * 0x85EBCA6Bu);
+    rng_next(st);
+    for (int it = 0; it < 32; ++it) {
+        const float x1 = (float)(rng_next(st) >> 9) * (1.0f / 4194304.0f) - 1.0f;
+        const float x2 = (float)(rng_next(st) >> 9) * (1.0f / 4194304.0f) - 1.0f;
+        const float q = x1 * x1 + x2 * x2;
+        if (q < 1.0f && q > 0.0f) {
+            const float t = 2.0f * std::sqrt(1.0f - q);
+            return V3{x1 * t, x2 * t, 1.0f - 2.0f * q};
+        }
+    }
+    return V3{0.f, 0.f, 1.f};
+}
+
+// CreateReflectionRays (RayTracer.cu:742-791) / ColorAndCreateReflectionRay (:1995-2016):
+// d = reflect(incident, n), origin offset by eps (:1765), optional cosine-lobe perturbation.
+void orc_raygen_reflect(const float* spos, const float* snrm, const float* prev_rays, const float eye[3],
+                        uint32_t W, uint32_t H, float eps, float jitter, uint32_t seed, uint32_t bounce,
+                        const float lo[3], const float scale[3], uint32_t g, uint32_t b, float* rays_out,
+                        uint32_t* keys) {
+    const HashP hp = mkhp(lo, scale, g, b);
+    Ray* rays = reinterpret_cast<Ray*>(rays_out);
+    const Ray* prev = reinterpret_cast<const Ray*>(prev_rays);
+    const uint64_t n = (uint64_t)W * H;
+#pragma omp parallel for schedule(static)
+    for (int64_t si = 0; si < (int64_t)n; ++si) {
+        const uint32_t slot = (uint32_t)si;
+        uint32_t key = KEY_NONE;
+        if (spos[4ull * slot + 3] != 0.0f) {
+            const V3 p = V3{spos[4ull * slot], spos[4ull * slot + 1], spos[4ull * slot + 2]};
+            const V3 nn = normalize(V3{snrm[4ull * slot], snrm[4ull * slot + 1], snrm[4ull * slot + 2]});
+            V3 i;
+            if (prev) i = V3{prev[slot].d[0], prev[slot].d[1], prev[slot].d[2]};
+            else i = normalize(sub(p, V3{eye[0], eye[1], eye[2]}));
+            const float k2 = 2.0f * dot(nn, i);
+            V3 r = sub(i, mul(nn, k2));
+            if (jitter > 0.0f) {
+                const V3 u = sphere_sample(seed, slot, bounce);
+                r = add(r, mul(u, jitter));
+                const float rn = dot(r, nn);
+                if (rn < 0.0f) r = sub(r, mul(nn, 2.0f * rn));
+            }
+            r = normalize(r);
+            if (r.x == r.x && r.y == r.y && r.z == r.z) {
+                const V3 o = add(p, mul(r, eps));
+                Ray ry;
+                ry.o[0] = o.x;
+                ry.o[1] = o.y;
+                ry.o[2] = o.z;
+                ry.tmin = eps;
+                ry.d[0] = r.x;
+                ry.d[1] = r.y;
+                ry.d[2] = r.z;
+                ry.tmax = INF;
+                rays[slot] = ry;
+                key = ray_hash(ry.o, ry.d, hp, 0u);
+            }
+        }
+        keys[slot] = key;
+    }
+}
+
+// ---------------------------------------------------------------- trim / compress / sort / decompress
+// CreateTrimmedRays (RayTracer.cu:844-884) + CreateChunkFlags/Bases/Sizes (:886-991).
+void orc_compress(const uint32_t* keys, uint32_t n, uint32_t* trimmed, uint32_t* ckeys, uint32_t* cbases,
+                  uint32_t* csizes, uint32_t* counts) {
+    uint32_t R = 0, C = 0;
+    uint32_t last = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t k = keys[i];
+        if (k == KEY_NONE) continue;
+        if (R == 0 || k != last) {
+            ckeys[C] = k;
+            cbases[C] = R;
+            ++C;
+        }
+        trimmed[R++] = i;
+        last = k;
+    }
+    cbases[C] = R;
+    if (csizes)
+        for (uint32_t c = 0; c < C; ++c) csizes[c] = cbases[c + 1] - cbases[c];
+    counts[0] = R;
+    counts[1] = C;
+}
+
+// Stable sort by the low key_bits (cub::DeviceRadixSort::SortPairs semantics, RayTracer.cu:2400-2404).
+void orc_sort_pairs(const uint32_t* keys, const uint32_t* vals, uint32_t n, uint32_t key_bits, uint32_t* ko,
+                    uint32_t* vo) {
+    const uint32_t mask = key_bits >= 32 ? 0xFFFFFFFFu : ((1u << key_bits) - 1u);
+    const uint32_t passes = key_bits == 0 ? 1 : (key_bits + 7) / 8;
+    const uint32_t smask = passes >= 4 ? 0xFFFFFFFFu : ((1u << (8 * passes)) - 1u);
+    (void)mask;
+    std::vector<uint32_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0u);
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](uint32_t a, uint32_t b) { return (keys[a] & smask) < (keys[b] & smask); });
+    for (uint32_t i = 0; i < n; ++i) {
+        ko[i] = keys[idx[i]];
+        vo[i] = vals ? vals[idx[i]] : idx[i];
+    }
+}
+
+// CreateSortedRaySkeleton + ExclusiveSum + CreateSortedRays (RayTracer.cu:993-1059, :2445-2462).
+void orc_decompress(const uint32_t* skeys, const uint32_t* svals, const uint32_t* cbases, const uint32_t* trimmed,
+                    uint32_t R, uint32_t C, uint32_t* sorted_keys, uint32_t* sorted_ids) {
+    (void)R;
+    uint32_t k = 0;
+    for (uint32_t x = 0; x < C; ++x) {
+        const uint32_t c = svals[x];
+        const uint32_t base = cbases[c], size = cbases[c + 1] - cbases[c];
+        for (uint32_t j = 0; j < size; ++j) {
+            sorted_ids[k] = trimmed[base + j];
+            if (sorted_keys) sorted_keys[k] = skeys ? skeys[x] : 0u;
+            ++k;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- ray hierarchy
+uint32_t orc_hierarchy_offsets(uint32_t max_rays, uint32_t P, uint32_t off[4]) {
+    const uint32_t n0 = (max_rays + P - 1) / P, n1 = (n0 + 7) / 8, n2 = (n1 + 7) / 8;
+    off[0] = 0;
+    off[1] = n0;
+    off[2] = n0 + n1;
+    off[3] = n0 + n1 + n2;
+    return off[3];
+}
+
+// HierarchyCreationWrapper (RayTracer.cu:2469-2535). Nodes written at the offsets of max_rays.
+void orc_build_rsh(const float* rays_in, const uint32_t* ids, uint32_t n, uint32_t max_rays, uint32_t P,
+                   void* nodes_out) {
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+    Node* nodes = static_cast<Node*>(nodes_out);
+    uint32_t off[4];
+    orc_hierarchy_offsets(max_rays, P, off);
+    const uint32_t n0 = (n + P - 1) / P, n1 = (n0 + 7) / 8, n2 = (n1 + 7) / 8;
+#pragma omp parallel for schedule(static)
+    for (int64_t j = 0; j < (int64_t)n0; ++j) nodes[off[0] + j] = make_leaf(rays, ids, n, (uint32_t)j * P, P);
+    const uint32_t sizes[3] = {n0, n1, n2};
+    for (int lvl = 1; lvl <= 2; ++lvl) {
+        const uint32_t nc = sizes[lvl - 1], np = sizes[lvl];
+#pragma omp parallel for schedule(static)
+        for (int64_t j = 0; j < (int64_t)np; ++j) {
+            const uint32_t c0 = 8 * (uint32_t)j, c1 = std::min(c0 + 8, nc);
+            nodes[off[lvl] + j] = merge_nodes(&nodes[off[lvl - 1] + c0], c1 - c0);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- object hierarchy
+static ObjH* g_last_objh = nullptr;
+
+static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const float lo[3], const float hi[3],
+                       ObjH& h) {
+    h.T = T;
+    h.cluster = cluster;
+    std::vector<uint32_t> codes(T);
+    float sc[3];
+    for (int i = 0; i < 3; ++i) sc[i] = (hi[i] > lo[i]) ? 1024.0f / (hi[i] - lo[i]) : 0.0f;
+    for (uint32_t t = 0; t < T; ++t) {
+        const float* a = pos + 12ull * t;
+        uint32_t cc[3];
+        for (int i = 0; i < 3; ++i) {
+            const float c = ((a[i] + a[4 + i]) + a[8 + i]) / 3.0f;
+            float f = std::fmin(std::fmax((c - lo[i]) * sc[i], 0.f), 1023.f);
+            cc[i] = (uint32_t)f;
+        }
+        codes[t] = (spread3(cc[0]) << 2) | (spread3(cc[1]) << 1) | spread3(cc[2]);
+    }
+    h.order.resize(T);
+    std::iota(h.order.begin(), h.order.end(), 0u);
+    std::stable_sort(h.order.begin(), h.order.end(), [&](uint32_t a, uint32_t b) { return codes[a] < codes[b]; });
+    h.tris.resize(12ull * T);
+    for (uint32_t k = 0; k < T; ++k) {
+        const uint32_t t = h.order[k];
+        std::memcpy(&h.tris[12ull * k], pos + 12ull * t, 48);
+        h.tris[12ull * k + 3] = u2f(t);
+    }
+    uint32_t sizes[16], levels = 0, cur = (T + cluster - 1) / cluster;
+    sizes[levels++] = cur;
+    while (cur > 8 && levels < 16) {
+        cur = (cur + 7) / 8;
+        sizes[levels++] = cur;
+    }
+    uint32_t total = 0;
+    for (uint32_t l = 0; l < levels; ++l) {
+        h.off[l] = total;
+        h.size[l] = sizes[l];
+        total += sizes[l];
+    }
+    h.levels = T ? levels : 0;
+    h.sph.assign(4ull * total, 0.0f);
+    for (uint32_t j = 0; j < sizes[0] && T; ++j) {
+        const uint32_t t0 = j * cluster, t1 = std::min(t0 + cluster, T);
+        float mn[3] = {INF, INF, INF}, mx[3] = {-INF, -INF, -INF};
+        for (uint32_t t = t0; t < t1; ++t)
+            for (int v = 0; v < 3; ++v)
+                for (int i = 0; i < 3; ++i) {
+                    mn[i] = std::fmin(mn[i], h.tris[12ull * t + 4 * v + i]);
+                    mx[i] = std::fmax(mx[i], h.tris[12ull * t + 4 * v + i]);
+                }
+        const V3 c = V3{(mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f};
+        float r2 = 0.f;
+        for (uint32_t t = t0; t < t1; ++t)
+            for (int v = 0; v < 3; ++v) {
+                const float* p = &h.tris[12ull * t + 4 * v];
+                const V3 d = V3{p[0] - c.x, p[1] - c.y, p[2] - c.z};
+                r2 = std::fmax(r2, dot(d, d));
+            }
+        float* s = &h.sph[4ull * j];
+        s[0] = c.x;
+        s[1] = c.y;
+        s[2] = c.z;
+        s[3] = std::sqrt(r2) * kRadSlack;
+    }
+    for (uint32_t l = 1; l < levels && T; ++l)
+        for (uint32_t j = 0; j < sizes[l]; ++j) {
+            const uint32_t c0 = 8 * j, c1 = std::min(c0 + 8, sizes[l - 1]);
+            float mn[3] = {INF, INF, INF}, mx[3] = {-INF, -INF, -INF};
+            for (uint32_t i = c0; i < c1; ++i) {
+                const float* q = &h.sph[4ull * (h.off[l - 1] + i)];
+                for (int k = 0; k < 3; ++k) {
+                    mn[k] = std::fmin(mn[k], q[k] - q[3]);
+                    mx[k] = std::fmax(mx[k], q[k] + q[3]);
+                }
+            }
+            const V3 c = V3{(mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f};
+            float r = 0.f;
+            for (uint32_t i = c0; i < c1; ++i) {
+                const float* q = &h.sph[4ull * (h.off[l - 1] + i)];
+                const V3 d = V3{q[0] - c.x, q[1] - c.y, q[2] - c.z};
+                r = std::fmax(r, length(d) + q[3]);
+            }
+            float* s = &h.sph[4ull * (h.off[l] + j)];
+            s[0] = c.x;
+            s[1] = c.y;
+            s[2] = c.z;
+            s[3] = r * kRadSlack;
+        }
+}
+
+// Builds the object-sphere hierarchy; returns a handle used by the traversal / intersection calls.
+void* orc_objh_build(const float* pos, uint32_t T, uint32_t cluster, const float lo[3], const float hi[3]) {
+    ObjH* h = new ObjH();
+    build_objh(pos, T, cluster, lo, hi, *h);
+    g_last_objh = h;
+    return h;
+}
+void orc_objh_free(void* hp) { delete static_cast<ObjH*>(hp); }
+uint32_t orc_objh_levels(void* hp) { return static_cast<ObjH*>(hp)->levels; }
+uint32_t orc_objh_level_size(void* hp, uint32_t l) { return static_cast<ObjH*>(hp)->size[l]; }
+void orc_objh_get(void* hp, uint32_t* order, float* tris, float* spheres) {
+    const ObjH* h = static_cast<ObjH*>(hp);
+    if (order) std::memcpy(order, h->order.data(), 4ull * h->T);
+    if (tris) std::memcpy(tris, h->tris.data(), 48ull * h->T);
+    if (spheres) std::memcpy(spheres, h->sph.data(), 4ull * h->sph.size());
+}
+
+// ---------------------------------------------------------------- traversal + intersection
+// Candidate set of the hierarchy-vs-hierarchy traversal (RayTracer.cu:1152-1496 semantics: a packet
+// reaches a triangle cluster iff it passes the node test at the cluster and at all its ancestors).
+// Written sorted ascending; returns the count (capped by cap). node_tests_out may be NULL.
+uint64_t orc_traverse(void* hp, const void* nodes_in, uint32_t n, uint32_t max_rays, uint32_t P, uint64_t* cand,
+                      uint64_t cap, uint64_t* node_tests_out) {
+    const ObjH& h = *static_cast<ObjH*>(hp);
+    const Node* nodes = static_cast<const Node*>(nodes_in);
+    uint32_t off[4];
+    orc_hierarchy_offsets(max_rays, P, off);
+    const uint32_t n0 = (n + P - 1) / P;
+    std::vector<std::vector<uint64_t>> per(n0);
+    uint64_t tests = 0;
+    if (h.levels == 0) return 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : tests)
+    for (int64_t p = 0; p < (int64_t)n0; ++p) {
+        const Node& nd = nodes[off[0] + p];
+        if (nd.count == 0) continue;
+        std::vector<uint32_t> cl;
+        uint64_t t = 0;
+        traverse_packet(nd, h, h.levels, 0, cl, t);
+        tests += t;
+        for (uint32_t c : cl) per[p].push_back(((uint64_t)p << 32) | c);
+    }
+    std::vector<uint64_t> all;
+    for (auto& v : per) all.insert(all.end(), v.begin(), v.end());
+    std::sort(all.begin(), all.end());
+    const uint64_t m = std::min<uint64_t>(all.size(), cap);
+    if (cand) std::memcpy(cand, all.data(), 8 * m);
+    if (node_tests_out) *node_tests_out = tests;
+    return all.size();
+}
+
+// CalculateShadowRayIntersections / CalculateReflectionRayIntersections (RayTracer.cu:1498-1774) over
+// the candidates. Outputs indexed by ray slot; caller initialises flags (0) / hits (HIT_NONE).
+void orc_intersect(void* hp, const float* rays_in, const uint32_t* ids, uint32_t n, uint32_t P,
+                   const uint64_t* cand, uint64_t ncand, int any, uint32_t* flags, uint64_t* hits) {
+    const ObjH& h = *static_cast<ObjH*>(hp);
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+    for (uint64_t c = 0; c < ncand; ++c) {
+        const uint32_t packet = (uint32_t)(cand[c] >> 32), cluster = (uint32_t)cand[c];
+        for (uint32_t j = 0; j < P; ++j) {
+            const uint32_t k = packet * P + j;
+            if (k >= n) break;
+            const uint32_t id = ids ? ids[k] : k;
+            const Ray& r = rays[id];
+            if (!(r.tmax > r.tmin)) continue;
+            const RayWT w = wt_setup(r);
+            const uint32_t t0 = cluster * h.cluster, t1 = std::min(t0 + h.cluster, h.T);
+            for (uint32_t t = t0; t < t1; ++t) {
+                const float* v = &h.tris[12ull * t];
+                float th;
+                if (wt_hit(w, v, v + 4, v + 8, th)) {
+                    if (any) {
+                        flags[id] = OCCLUDED;
+                        break;
+                    }
+                    const uint64_t key = hit_key(th, f2u(v[3]));
+                    if (key < hits[id]) hits[id] = key;
+                }
+            }
+        }
+    }
+}
+
+// Brute force over all triangles (CUDA-Naive-Engine RayTracer.cu:276-291 any-hit, :344-360 closest).
+// pos: original order, 12 floats per triangle. Fills flags (any) or hits (closest) for every ray.
+void orc_brute(const float* pos, uint32_t T, const float* rays_in, uint32_t n, int any, uint32_t* flags,
+               uint64_t* hits) {
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const Ray& r = rays[i];
+        if (any) flags[i] = 0;
+        else hits[i] = HIT_NONE;
+        if (!(r.tmax > r.tmin)) continue;
+        const RayWT w = wt_setup(r);
+        uint64_t best = HIT_NONE;
+        for (uint32_t t = 0; t < T; ++t) {
+            const float* v = pos + 12ull * t;
+            float th;
+            if (wt_hit(w, v, v + 4, v + 8, th)) {
+                if (any) {
+                    flags[i] = OCCLUDED;
+                    break;
+                }
+                const uint64_t key = hit_key(th, t);
+                if (key < best) best = key;
+            }
+        }
+        if (!any) hits[i] = best;
+    }
+}
+
+// Second-nearest hit distance per ray (for the near-tie exception of the hit-ID comparison).
+void orc_brute_second(const float* pos, uint32_t T, const float* rays_in, uint32_t n, float* t1, float* t2) {
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const Ray& r = rays[i];
+        float a = INF, b = INF;
+        if (r.tmax > r.tmin) {
+            const RayWT w = wt_setup(r);
+            for (uint32_t t = 0; t < T; ++t) {
+                const float* v = pos + 12ull * t;
+                float th;
+                if (wt_hit(w, v, v + 4, v + 8, th)) {
+                    if (th < a) {
+                        b = a;
+                        a = th;
+                    } else if (th < b) {
+                        b = th;
+                    }
+                }
+            }
+        }
+        t1[i] = a;
+        t2[i] = b;
+    }
+}
+
+// Hit resolve (RayTracer.cu:1806-1843): hit point and area-ratio barycentric normal.
+void orc_resolve(const float* pos, const float* nrm, const uint32_t* mat, const float* rays_in,
+                 const uint64_t* hits, const uint32_t* pix, uint32_t n, float* spos, float* snrm) {
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+#pragma omp parallel for schedule(static)
+    for (int64_t kk = 0; kk < (int64_t)n; ++kk) {
+        const uint32_t k = (uint32_t)kk;
+        const uint32_t px = pix ? pix[k] : k;
+        if (px == 0xFFFFFFFFu) continue;
+        const uint64_t hk = hits[k];
+        float* sp = spos + 4ull * px;
+        float* sn = snrm + 4ull * px;
+        if (hk == HIT_NONE) {
+            for (int i = 0; i < 4; ++i) sp[i] = sn[i] = 0.f;
+            continue;
+        }
+        const uint32_t tri = (uint32_t)hk;
+        const float t = u2f((uint32_t)(hk >> 32));
+        const Ray& r = rays[k];
+        const V3 p = V3{r.o[0] + r.d[0] * t, r.o[1] + r.d[1] * t, r.o[2] + r.d[2] * t};
+        const float* v = pos + 12ull * tri;
+        const V3 a = V3{v[0], v[1], v[2]}, b = V3{v[4], v[5], v[6]}, c = V3{v[8], v[9], v[10]};
+        const float abc = length(cross(sub(b, a), sub(c, a)));
+        const float pbc = length(cross(sub(b, p), sub(c, p)));
+        const float pca = length(cross(sub(a, p), sub(c, p)));
+        const float b0 = pbc / abc, b1 = pca / abc, b2 = (1.0f - b0) - b1;
+        const float* q = nrm + 12ull * tri;
+        sp[0] = p.x;
+        sp[1] = p.y;
+        sp[2] = p.z;
+        sp[3] = 1.0f;
+        for (int i = 0; i < 3; ++i) sn[i] = (q[i] * b0 + q[4 + i] * b1) + q[8 + i] * b2;
+        sn[3] = u2f(mat ? mat[tri] : 0u);
+    }
+}
+
+// ---------------------------------------------------------------- the whole algorithm on the CPU
+// One keyed batch through compress -> sort -> decompress -> build -> traverse+intersect (per packet, all
+// host threads). Used as the CPU baseline; returns the number of traced rays. stage_ms (8 floats) gets
+// per-stage wall times: compress, sort, decompress, build, traverse+intersect.
+uint32_t orc_trace_keyed(void* hp, const float* rays_in, const uint32_t* keys, uint32_t n_slots, uint32_t key_bits,
+                         uint32_t P, int any, uint32_t* flags, uint64_t* hits, float* stage_ms,
+                         uint64_t* counters /* node tests, tri tests */) {
+    using clk = std::chrono::steady_clock;
+    auto ms = [](clk::time_point a, clk::time_point b) {
+        return std::chrono::duration<float, std::milli>(b - a).count();
+    };
+    const ObjH& h = *static_cast<ObjH*>(hp);
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+    std::vector<uint32_t> trimmed(n_slots), ckeys(n_slots + 1), cbases(n_slots + 1);
+    uint32_t counts[2];
+    auto t0 = clk::now();
+    orc_compress(keys, n_slots, trimmed.data(), ckeys.data(), cbases.data(), nullptr, counts);
+    const uint32_t R = counts[0], C = counts[1];
+    auto t1 = clk::now();
+    std::vector<uint32_t> sk(C), sv(C);
+    orc_sort_pairs(ckeys.data(), nullptr, C, key_bits, sk.data(), sv.data());
+    auto t2 = clk::now();
+    std::vector<uint32_t> sorted(R);
+    orc_decompress(sk.data(), sv.data(), cbases.data(), trimmed.data(), R, C, nullptr, sorted.data());
+    auto t3 = clk::now();
+    uint32_t off[4];
+    const uint32_t cap = orc_hierarchy_offsets(R, P, off);
+    std::vector<Node> nodes(cap ? cap : 1);
+    orc_build_rsh(rays_in, sorted.data(), R, R, P, nodes.data());
+    auto t4 = clk::now();
+    const uint32_t n0 = (R + P - 1) / P;
+    uint64_t ntests = 0, ttests = 0;
+    if (h.levels) {
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : ntests, ttests)
+        for (int64_t p = 0; p < (int64_t)n0; ++p) {
+            const Node& nd = nodes[off[0] + p];
+            if (nd.count == 0) continue;
+            std::vector<uint32_t> cl;
+            uint64_t t = 0;
+            traverse_packet(nd, h, h.levels, 0, cl, t);
+            ntests += t;
+            for (uint32_t j = 0; j < P; ++j) {
+                const uint32_t k = (uint32_t)p * P + j;
+                if (k >= R) break;
+                const uint32_t id = sorted[k];
+                const Ray& r = rays[id];
+                if (!(r.tmax > r.tmin)) continue;
+                const RayWT w = wt_setup(r);
+                uint64_t best = HIT_NONE;
+                bool occl = false;
+                for (uint32_t c : cl) {
+                    const uint32_t a0 = c * h.cluster, a1 = std::min(a0 + h.cluster, h.T);
+                    for (uint32_t t2i = a0; t2i < a1; ++t2i) {
+                        const float* v = &h.tris[12ull * t2i];
+                        float th;
+                        ++ttests;
+                        if (wt_hit(w, v, v + 4, v + 8, th)) {
+                            if (any) {
+                                occl = true;
+                                break;
+                            }
+                            const uint64_t key = hit_key(th, f2u(v[3]));
+                            if (key < best) best = key;
+                        }
+                    }
+                    if (occl) break;
+                }
+                if (any) {
+                    if (occl) flags[id] = OCCLUDED;
+                } else if (best < hits[id]) {
+                    hits[id] = best;
+                }
+            }
+        }
+    }
+    auto t5 = clk::now();
+    if (stage_ms) {
+        stage_ms[0] = ms(t0, t1);
+        stage_ms[1] = ms(t1, t2);
+        stage_ms[2] = ms(t2, t3);
+        stage_ms[3] = ms(t3, t4);
+        stage_ms[4] = ms(t4, t5);
+    }
+    if (counters) {
+        counters[0] = ntests;
+        counters[1] = ttests;
+    }
+    return R;
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// Internal engine state shared by the C-ABI translation units (engine.cu, batch.cu, server.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/rsh.h"
+#include "kernels.h"
+
+namespace rsh {
+
+void set_error(const std::string& msg);
+rsh_status cuda_status(cudaError_t e, const char* where);
+
+#define RSH_CUDA(call)                                                       \
+    do {                                                                     \
+        cudaError_t _e = (call);                                             \
+        if (_e != cudaSuccess) return ::rsh::cuda_status(_e, #call);         \
+    } while (0)
+#define RSH_TRY(call)                              \
+    do {                                           \
+        rsh_status _s = (call);                    \
+        if (_s != RSH_OK) return _s;               \
+    } while (0)
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace rsh
+
+struct rsh_scene {
+    rsh_ctx* owner = nullptr;
+    uint32_t tri_count = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    float4* pos = nullptr;       // original order, 3 per triangle
+    float4* nrm = nullptr;       // original order, 3 per triangle
+    uint32_t* mat = nullptr;     // per triangle
+    rsh_material* materials = nullptr;
+    uint32_t material_count = 0;
+    rsh::ObjHierarchy h;
+    size_t bytes = 0;
+};
+
+struct BounceBufs {
+    rsh::DevBuf shadow_rays, shadow_flags, refl_rays, refl_hits, surf_pos, surf_nrm;
+};
+
+struct rsh_ctx {
+    rsh_config cfg{};
+    int device = 0;
+    int sms = 152;
+    uint64_t budget = 0;
+    uint64_t allocated = 0;
+    std::map<std::string, rsh::DevBuf> bufs;
+    uint32_t* d_err = nullptr;
+    unsigned long long* d_stats = nullptr;   // [0] node tests [1] tri tests [2] candidates [3..] spare
+    uint32_t* h_pinned = nullptr;            // small pinned readback area
+    rsh_light lights[8]{};
+    uint32_t light_count = 0;
+    rsh_camera cam{};
+    bool cam_set = false;
+    // frame state
+    uint32_t fw = 0, fh = 0, fdepth = 0, flights = 0;
+    std::vector<BounceBufs> bounce;
+    rsh::DevBuf prim_rays, prim_hits, prim_pix, surf0_pos, surf0_nrm;
+    rsh_frame_stats stats{};
+    rsh_frame_stats batch_stats{};
+    cudaEvent_t ev[16] = {};
+    cudaStream_t last_stream = nullptr;
+    std::vector<uint32_t> batch_counts_host;
+    uint32_t overflow_passes = 0;
+};
+
+namespace rsh {
+
+rsh_status ensure(rsh_ctx* ctx, const char* name, size_t bytes, void** out);
+rsh_status ensure_buf(rsh_ctx* ctx, DevBuf& b, size_t bytes);
+void release_buf(rsh_ctx* ctx, DevBuf& b);
+rsh_status make_hash_params(const rsh_scene* sc, const rsh_config& cfg, uint32_t tag_bits, HashP& out);
+
+// One secondary batch through compress -> sort -> decompress -> build -> traverse -> intersect.
+// keys: per slot (RSH_KEY_NONE = no ray); rays indexed by slot. Output flags/hits indexed by slot
+// (caller initialises). Accumulates counters into ctx->d_stats; counts_out (device, 2 words) gets
+// (rays, chunks) if non-null.
+rsh_status trace_keyed(rsh_ctx* ctx, const rsh_scene* sc, const rsh_ray* rays, const uint32_t* keys,
+                       uint32_t n_slots, uint32_t key_bits, bool any_hit, uint32_t* flags,
+                       unsigned long long* hits, uint32_t* counts_out, cudaStream_t s);
+// Rays already in traversal order (no hash/sort), e.g. primary rays in tile order.
+rsh_status trace_ordered(rsh_ctx* ctx, const rsh_scene* sc, const rsh_ray* rays, uint32_t n,
+                         bool any_hit, uint32_t* flags, unsigned long long* hits, cudaStream_t s);
+
+}  // namespace rsh

@@ -1,0 +1,78 @@
+// Intersection of traversal candidates: any-hit (shadow) and closest-hit (reflection / primary).
+//
+// Reference: CalculateShadowRayIntersections (RayTracer.cu:1498-1614: per (leaf node, triangle) record
+// test its <= 8 rays with a non-watertight Moller-Trumbore using __fdividef; occluded iff
+// eps < t < |o - p| - 2 eps -> flag = UINT_MAX) and CalculateReflectionRayIntersections (:1711-1774:
+// atomicMin of ((uint)(t*10 + 1) << 20) + triID, i.e. t quantised to 0.1 in 12 bits).
+//
+// Here: P threads per candidate (one per ray of the packet), each testing its ray against the
+// cluster's triangles with the watertight test. Any-hit stores RSH_OCCLUDED and stops (and skips rays
+// already known occluded); closest-hit keeps its best (float bits of t << 32 | original triangle id)
+// and issues one 64-bit atomicMin. A persistent grid-stride loop reads the candidate count on the
+// device, so no host readback sits between traversal and intersection.
+#include "common.cuh"
+#include "kernels.h"
+#include "tests.cuh"
+
+namespace rsh {
+
+template <bool ANY>
+__global__ void __launch_bounds__(256) k_intersect(IsectArgs a) {
+    const uint32_t P = a.packet;
+    const unsigned long long cc = *a.cand_count;
+    const unsigned long long count = cc < a.capacity ? cc : a.capacity;
+    const uint32_t n = dev_count(a.d_count, a.max_rays);
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane_in = gtid % P;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x / P;
+    unsigned long long tests = 0;
+    for (unsigned long long c = gtid / P; c < count; c += stride) {
+        const unsigned long long cand = __ldg(a.cand + c);
+        const uint32_t packet = (uint32_t)(cand >> 32), cluster = (uint32_t)cand;
+        const uint32_t k = packet * P + lane_in;
+        if (k >= n) continue;
+        const uint32_t id = a.sorted_ids ? __ldg(a.sorted_ids + k) : k;
+        if (id >= a.max_rays) continue;
+        float4 o, d;
+        load_ray(a.rays, id, o, d);
+        if (!(d.w > o.w)) continue;
+        if (ANY && *(volatile uint32_t*)(a.flags + id) == RSH_OCCLUDED) continue;
+        const RayWT r = wt_setup(o, d);
+        const uint32_t t0 = cluster * a.cluster;
+        const uint32_t t1 = (t0 + a.cluster < a.tri_count) ? t0 + a.cluster : a.tri_count;
+        unsigned long long best = RSH_HIT_NONE;
+        for (uint32_t t = t0; t < t1; ++t) {
+            const float4 v0 = __ldg(a.tris + 3ull * t);
+            const float4 v1 = __ldg(a.tris + 3ull * t + 1);
+            const float4 v2 = __ldg(a.tris + 3ull * t + 2);
+            float th;
+            ++tests;
+            if (wt_hit(r, v0, v1, v2, th)) {
+                if (ANY) {
+                    a.flags[id] = RSH_OCCLUDED;
+                    break;
+                }
+                const unsigned long long key = hit_key(th, __float_as_uint(v0.w));
+                best = key < best ? key : best;
+            }
+        }
+        if (!ANY && best != RSH_HIT_NONE) {
+            if (best < *(volatile unsigned long long*)(a.hits + id)) atomicMin(a.hits + id, best);
+        }
+    }
+#pragma unroll
+    for (int dd = 16; dd > 0; dd >>= 1) tests += __shfl_xor_sync(0xffffffffu, tests, dd);
+    if ((threadIdx.x & 31u) == 0 && a.tri_tests) atomicAdd(a.tri_tests, tests);
+}
+
+cudaError_t launch_intersect(const IsectArgs& a, bool any_hit, cudaStream_t s) {
+    int sms = 152, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t grid = (uint32_t)sms * 8u;
+    if (any_hit) k_intersect<true><<<grid, 256, 0, s>>>(a);
+    else k_intersect<false><<<grid, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace rsh

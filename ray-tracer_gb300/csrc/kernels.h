@@ -1,0 +1,205 @@
+// Host-side launchers of the sm_103a kernels (one translation unit per stage). Internal to the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rsh.h"
+
+// Device error word bits (bounded waits that gave up, buffer overflows).
+#ifndef RSH_DEVERR_TIMEOUT
+#define RSH_DEVERR_TIMEOUT 1u
+#define RSH_DEVERR_OVERFLOW 2u
+#endif
+
+namespace rsh {
+
+struct HashP {
+    float lo[3];
+    float scale[3];
+    uint32_t grid_bits, dir_log2, tag_bits, key_bits;
+};
+inline HashP to_hashp(const rsh_hash_params& h) {
+    HashP p;
+    for (int i = 0; i < 3; ++i) {
+        p.lo[i] = h.lo[i];
+        p.scale[i] = h.scale[i];
+    }
+    p.grid_bits = h.grid_bits;
+    p.dir_log2 = h.dir_log2;
+    p.tag_bits = h.tag_bits;
+    p.key_bits = h.key_bits;
+    return p;
+}
+
+struct LightsP {
+    uint32_t count;
+    float pos[8][3];
+};
+
+struct CameraP {
+    float eye[3], dir[3], right[3], up[3];
+};
+
+// ---- raygen + hash (raygen.cu)
+cudaError_t launch_raygen_primary(const CameraP& cam, uint32_t w, uint32_t h, rsh_ray* rays,
+                                  uint32_t* pixel_of_ray, cudaStream_t s);
+cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_t w, uint32_t h,
+                                 const LightsP& lights, float eps, const HashP& hp, rsh_ray* rays,
+                                 uint32_t* keys, cudaStream_t s);
+cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const rsh_ray* prev,
+                                  const float eye[3], uint32_t w, uint32_t h, float eps,
+                                  float jitter, uint32_t seed, uint32_t bounce, const HashP& hp,
+                                  rsh_ray* rays, uint32_t* keys, cudaStream_t s);
+cudaError_t launch_hash(const rsh_ray* rays, uint32_t n, const HashP& hp, uint32_t tag,
+                        uint32_t* keys, cudaStream_t s);
+// Segmented hash for the batched form: segment s covers rays [seg_start[s], seg_start[s+1]) of the
+// concatenated ray array; tag = segment index; hash params per segment (scene bounds).
+cudaError_t launch_hash_segments(const rsh_ray* rays, uint32_t n, const uint32_t* seg_start,
+                                 uint32_t nseg, const HashP* hps_dev, uint32_t tag_shift,
+                                 uint32_t* keys, cudaStream_t s);
+
+// ---- trim + compress (compress.cu)
+size_t compress_scratch_bytes(uint32_t n_slots);
+cudaError_t launch_compress(const uint32_t* keys, uint32_t n_slots, uint32_t* trimmed_ids,
+                            uint32_t* chunk_keys, uint32_t* chunk_bases, uint32_t* counts,
+                            void* scratch, uint32_t* err, cudaStream_t s);
+cudaError_t launch_chunk_sizes(const uint32_t* chunk_bases, const uint32_t* counts, uint32_t max_chunks,
+                               uint32_t* chunk_sizes, cudaStream_t s);
+
+// ---- onesweep radix sort (sort.cu)
+size_t sort_scratch_bytes(uint32_t n_max, uint32_t key_bits);
+cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                              uint32_t* vals_out, uint32_t n_max, const uint32_t* d_count,
+                              uint32_t key_bits, void* scratch, uint32_t* err, cudaStream_t s);
+
+// ---- decompress (decompress.cu)
+size_t decompress_scratch_bytes(uint32_t max_chunks);
+cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t* sorted_chunk_vals,
+                              const uint32_t* chunk_bases, const uint32_t* trimmed_ids,
+                              const uint32_t* counts, uint32_t max_rays, uint32_t* sorted_keys,
+                              uint32_t* sorted_ids, void* scratch, uint32_t* err, cudaStream_t s);
+
+// ---- ray-space hierarchy build (build.cu)
+uint32_t hierarchy_capacity(uint32_t max_rays, uint32_t packet, uint32_t offsets[4]);
+cudaError_t launch_build_rsh(const rsh_ray* rays, const uint32_t* sorted_ids, uint32_t max_rays,
+                             const uint32_t* d_count, uint32_t packet, rsh_node* nodes,
+                             cudaStream_t s);
+
+// ---- object-sphere hierarchy (objh.cu)
+struct ObjHierarchy {
+    uint32_t tri_count = 0;
+    uint32_t cluster = 8;
+    uint32_t levels = 0;           // level 0 = clusters; levels-1 = top (<= 8 nodes)
+    uint32_t level_off[16] = {};   // offsets into spheres
+    uint32_t level_size[16] = {};
+    float4* spheres = nullptr;     // all levels
+    float4* tris = nullptr;        // cluster order, 3 per triangle, v0.w = original id bits
+    uint32_t* order = nullptr;     // cluster slot -> original triangle id
+};
+cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t tri_count, uint32_t cluster,
+                                   const float lo[3], const float hi[3], ObjHierarchy& h,
+                                   void* scratch, size_t scratch_bytes, uint32_t* err, cudaStream_t s);
+size_t objh_scratch_bytes(uint32_t tri_count);
+
+// ---- traversal (traverse.cu)
+struct TravArgs {
+    const rsh_node* nodes;
+    uint32_t node_off[4];       // level offsets of the ray hierarchy (from max_rays)
+    uint32_t max_rays;
+    const uint32_t* d_count;
+    uint32_t packet;
+    const float4* spheres;
+    uint32_t lvl_off[16];
+    uint32_t lvl_size[16];
+    uint32_t levels;
+    unsigned long long* cand;
+    unsigned long long capacity;
+    unsigned long long* cand_count;
+    uint32_t* work;              // [0] = next unit, [1] = resume unit (min failed)
+    unsigned long long* node_tests;
+    uint32_t* err;
+};
+cudaError_t launch_traverse(const TravArgs& a, cudaStream_t s);
+
+// ---- intersection (intersect.cu)
+struct IsectArgs {
+    const float4* tris;
+    uint32_t tri_count;
+    uint32_t cluster;
+    const rsh_ray* rays;
+    const uint32_t* sorted_ids;
+    uint32_t max_rays;
+    const uint32_t* d_count;
+    uint32_t packet;
+    const unsigned long long* cand;
+    const unsigned long long* cand_count;
+    unsigned long long capacity;
+    uint32_t* flags;
+    unsigned long long* hits;
+    unsigned long long* tri_tests;
+};
+cudaError_t launch_intersect(const IsectArgs& a, bool any_hit, cudaStream_t s);
+
+// ---- fused persistent traversal + intersection (fused.cu)
+struct FusedSeg {
+    const float4* spheres;
+    const float4* tris;
+    uint32_t tri_count;
+    uint32_t cluster;
+    uint32_t levels;
+    uint32_t lvl_off[16];
+    uint32_t lvl_size[16];
+    uint32_t ray_begin, ray_end;   // sorted ray range of this segment
+    uint32_t unit_begin;           // first work unit (level-1 node) of this segment
+    uint32_t any_hit;
+    uint32_t* flags;               // indexed by slot - slot_base
+    unsigned long long* hits;
+    uint32_t slot_base;
+};
+struct FusedArgs {
+    const rsh_node* nodes;
+    uint32_t node_off[4];
+    uint32_t packet;
+    const rsh_ray* rays;
+    const uint32_t* sorted_ids;
+    const FusedSeg* segs;          // device
+    uint32_t nseg;
+    const uint32_t* unit_seg;      // device: work unit -> segment (size = units)
+    uint32_t units_max;
+    const uint32_t* d_units;       // device count of units
+    uint32_t* work;
+    unsigned long long* node_tests;
+    unsigned long long* tri_tests;
+    uint32_t* err;
+};
+cudaError_t launch_fused(const FusedArgs& a, cudaStream_t s);
+
+// ---- resolve + shade (shade.cu)
+cudaError_t launch_resolve(const float4* tris_orig_pos, const float4* tris_orig_nrm,
+                           const uint32_t* mat_ids, const rsh_ray* rays, const unsigned long long* hits,
+                           const uint32_t* pixel_of_ray, uint32_t n, float4* spos, float4* snrm,
+                           cudaStream_t s);
+struct ShadeArgs {
+    const float4* spos;
+    const float4* snrm;
+    const rsh_material* materials;
+    uint32_t material_count;
+    const uint32_t* shadow;   // W*H*L slots
+    float4* accum;            // W*H rgb accumulators + weight in w
+    uint32_t w, h;
+    uint32_t lights;
+    rsh_light light[8];
+    float eye[3];
+    uint32_t bounce;
+    const rsh_ray* incident;  // reflection rays that produced the surface (bounce>0), else null
+};
+cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t s);
+cudaError_t launch_pack_rgba(const float4* accum, uint32_t n, uint32_t* rgba, cudaStream_t s);
+
+// ---- misc (util kernels in raygen.cu)
+cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s);
+cudaError_t launch_fill_u64(unsigned long long* p, unsigned long long v, size_t n, cudaStream_t s);
+cudaError_t launch_mark_hit_counts(const uint32_t* counts, unsigned long long* acc, cudaStream_t s);
+
+}  // namespace rsh

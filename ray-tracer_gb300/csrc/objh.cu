@@ -1,0 +1,174 @@
+// Object bounding-sphere hierarchy over the scene's triangles.
+//
+// Reference: one minimal enclosing sphere per mesh from the GPL Miniball (BoundingSphere.cpp:9-63),
+// packed as {centre, radius, firstTri, lastTri} (main.cpp:2445-2470) and culled against the top ray
+// nodes (CalculateBoundingSpheresIntersections, RayTracer.cu:1152-1280); triangles then get a bounding
+// sphere each (CreateTriangleBoundingSphere, :301-376) inside the descent. Here the object spheres
+// become a full sphere tree built on the GPU:
+//   1. Morton code (10 bits per axis) of every triangle centroid over the scene box;
+//   2. stable onesweep sort of (code, triangle id) -> cluster order;
+//   3. gather triangles into cluster order (original id kept in the first vertex's w);
+//   4. level 0: one sphere per cluster of `cluster` consecutive triangles: centre = midpoint of the
+//      vertex box, radius = max vertex distance (x (1 + 2^-20));
+//   5. levels 1..: fan-out 8 over consecutive nodes, centre = midpoint of the children's sphere box,
+//      radius = max(|c_i - c| + r_i), until a level has at most 8 nodes.
+// Every sphere encloses every vertex below it, so the hierarchy never culls a real hit.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace rsh {
+
+namespace {
+constexpr float kRadSlack = 1.0f + 1.0f / 1048576.0f;
+}
+
+__global__ void k_morton(const float4* __restrict__ pos, uint32_t n, v3 lo, v3 sc, uint32_t* codes) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = __ldg(pos + 3ull * i), b = __ldg(pos + 3ull * i + 1), c = __ldg(pos + 3ull * i + 2);
+    const float cx = ((a.x + b.x) + c.x) / 3.0f;
+    const float cy = ((a.y + b.y) + c.y) / 3.0f;
+    const float cz = ((a.z + b.z) + c.z) / 3.0f;
+    float fx = fminf(fmaxf((cx - lo.x) * sc.x, 0.f), 1023.f);
+    float fy = fminf(fmaxf((cy - lo.y) * sc.y, 0.f), 1023.f);
+    float fz = fminf(fmaxf((cz - lo.z) * sc.z, 0.f), 1023.f);
+    codes[i] = (spread3((uint32_t)fx) << 2) | (spread3((uint32_t)fy) << 1) | spread3((uint32_t)fz);
+}
+
+__global__ void k_gather_tris(const float4* __restrict__ pos, const uint32_t* __restrict__ perm,
+                              uint32_t n, float4* __restrict__ tris, uint32_t* __restrict__ order) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t t = __ldg(perm + k);
+    float4 a = __ldg(pos + 3ull * t);
+    a.w = __uint_as_float(t);
+    tris[3ull * k] = a;
+    tris[3ull * k + 1] = __ldg(pos + 3ull * t + 1);
+    tris[3ull * k + 2] = __ldg(pos + 3ull * t + 2);
+    order[k] = t;
+}
+
+__global__ void k_leaf_spheres(const float4* __restrict__ tris, uint32_t n, uint32_t cluster,
+                               uint32_t nleaves, float4* __restrict__ sph) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nleaves) return;
+    const uint32_t t0 = j * cluster, t1 = (t0 + cluster < n) ? t0 + cluster : n;
+    const float inf = __int_as_float(0x7f800000);
+    float mnx = inf, mny = inf, mnz = inf, mxx = -inf, mxy = -inf, mxz = -inf;
+    for (uint32_t t = t0; t < t1; ++t)
+        for (int v = 0; v < 3; ++v) {
+            const float4 p = __ldg(tris + 3ull * t + v);
+            mnx = fminf(mnx, p.x);
+            mny = fminf(mny, p.y);
+            mnz = fminf(mnz, p.z);
+            mxx = fmaxf(mxx, p.x);
+            mxy = fmaxf(mxy, p.y);
+            mxz = fmaxf(mxz, p.z);
+        }
+    const v3 c = v3{(mnx + mxx) * 0.5f, (mny + mxy) * 0.5f, (mnz + mxz) * 0.5f};
+    float r2 = 0.f;
+    for (uint32_t t = t0; t < t1; ++t)
+        for (int v = 0; v < 3; ++v) {
+            const float4 p = __ldg(tris + 3ull * t + v);
+            const v3 d = v3{p.x - c.x, p.y - c.y, p.z - c.z};
+            r2 = fmaxf(r2, dot3(d, d));
+        }
+    sph[j] = make_float4(c.x, c.y, c.z, sqrtf(r2) * kRadSlack);
+}
+
+__global__ void k_upper_spheres(float4* __restrict__ sph, uint32_t child_off, uint32_t nchild,
+                                uint32_t parent_off, uint32_t nparent) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nparent) return;
+    const uint32_t c0 = 8 * j, c1 = (8 * j + 8 < nchild) ? 8 * j + 8 : nchild;
+    const float inf = __int_as_float(0x7f800000);
+    float mnx = inf, mny = inf, mnz = inf, mxx = -inf, mxy = -inf, mxz = -inf;
+    for (uint32_t i = c0; i < c1; ++i) {
+        const float4 q = sph[child_off + i];
+        mnx = fminf(mnx, q.x - q.w);
+        mny = fminf(mny, q.y - q.w);
+        mnz = fminf(mnz, q.z - q.w);
+        mxx = fmaxf(mxx, q.x + q.w);
+        mxy = fmaxf(mxy, q.y + q.w);
+        mxz = fmaxf(mxz, q.z + q.w);
+    }
+    const v3 c = v3{(mnx + mxx) * 0.5f, (mny + mxy) * 0.5f, (mnz + mxz) * 0.5f};
+    float r = 0.f;
+    for (uint32_t i = c0; i < c1; ++i) {
+        const float4 q = sph[child_off + i];
+        const v3 d = v3{q.x - c.x, q.y - c.y, q.z - c.z};
+        r = fmaxf(r, len3(d) + q.w);
+    }
+    sph[parent_off + j] = make_float4(c.x, c.y, c.z, r * kRadSlack);
+}
+
+size_t objh_scratch_bytes(uint32_t tri_count) {
+    return 4ull * tri_count * 2 + sort_scratch_bytes(tri_count, 30) + 4096;
+}
+
+cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint32_t cluster,
+                                   const float lo[3], const float hi[3], ObjHierarchy& h,
+                                   void* scratch, size_t scratch_bytes, uint32_t* err, cudaStream_t s) {
+    (void)scratch_bytes;
+    h.tri_count = n;
+    h.cluster = cluster;
+    if (n == 0) {
+        h.levels = 0;
+        return cudaSuccess;
+    }
+    // level sizes
+    uint32_t sizes[16];
+    uint32_t levels = 0;
+    uint32_t cur = (n + cluster - 1) / cluster;
+    sizes[levels++] = cur;
+    while (cur > 8 && levels < 16) {
+        cur = (cur + 7) / 8;
+        sizes[levels++] = cur;
+    }
+    uint32_t total = 0;
+    for (uint32_t l = 0; l < levels; ++l) {
+        h.level_off[l] = total;
+        h.level_size[l] = sizes[l];
+        total += sizes[l];
+    }
+    h.levels = levels;
+    cudaError_t e;
+    if ((e = cudaMalloc(&h.spheres, sizeof(float4) * total)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h.tris, sizeof(float4) * 3ull * n)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h.order, sizeof(uint32_t) * n)) != cudaSuccess) return e;
+
+    char* b = static_cast<char*>(scratch);
+    uint32_t* codes = reinterpret_cast<uint32_t*>(b);
+    uint32_t* sorted_codes = codes + n;
+    uint32_t* perm = reinterpret_cast<uint32_t*>(h.order);  // sorted values land in order[] first
+    void* sort_scratch = b + ((8ull * n + 255) & ~255ull);
+    v3 vlo = v3{lo[0], lo[1], lo[2]};
+    v3 vsc;
+    vsc.x = (hi[0] > lo[0]) ? 1024.0f / (hi[0] - lo[0]) : 0.0f;
+    vsc.y = (hi[1] > lo[1]) ? 1024.0f / (hi[1] - lo[1]) : 0.0f;
+    vsc.z = (hi[2] > lo[2]) ? 1024.0f / (hi[2] - lo[2]) : 0.0f;
+    k_morton<<<(n + 255) / 256, 256, 0, s>>>(positions_dev, n, vlo, vsc, codes);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    uint32_t* perm_tmp = nullptr;
+    if ((e = cudaMalloc(&perm_tmp, sizeof(uint32_t) * n)) != cudaSuccess) return e;
+    e = launch_sort_pairs(codes, nullptr, sorted_codes, perm_tmp, n, nullptr, 30, sort_scratch, err, s);
+    if (e != cudaSuccess) {
+        cudaFree(perm_tmp);
+        return e;
+    }
+    k_gather_tris<<<(n + 255) / 256, 256, 0, s>>>(positions_dev, perm_tmp, n, h.tris, perm);
+    if ((e = cudaGetLastError()) != cudaSuccess) {
+        cudaFree(perm_tmp);
+        return e;
+    }
+    k_leaf_spheres<<<(sizes[0] + 127) / 128, 128, 0, s>>>(h.tris, n, cluster, sizes[0], h.spheres);
+    for (uint32_t l = 1; l < levels; ++l)
+        k_upper_spheres<<<(sizes[l] + 127) / 128, 128, 0, s>>>(h.spheres, h.level_off[l - 1],
+                                                               sizes[l - 1], h.level_off[l], sizes[l]);
+    e = cudaGetLastError();
+    cudaStreamSynchronize(s);
+    cudaFree(perm_tmp);
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+}  // namespace rsh

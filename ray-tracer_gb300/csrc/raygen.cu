@@ -1,0 +1,270 @@
+// Ray generation fused with the 32-bit ray hash.
+//
+// Reference: CreateShadowRays (RayTracer.cu:682-740), CreateReflectionRays (:742-791), the ray
+// creation tail of ColorAndCreateReflectionRay (:1995-2016), the camera ray of RayTracer.cu:666-667 /
+// CUDA-Naive-Ray-Tracer RayTracer.cu:606-607. The reference hash (CreateShadowRayIndex :147-168,
+// CreateReflectionRayIndex :170-198) used atan2(x, x), which is constant, so the key is redefined:
+//   key = tag << (3g + 2b) | morton3(origin cell, g bits per axis) << 2b | morton2(octahedral bin)
+// using only +, -, *, /, abs, min/max and truncation, so a CPU restatement reproduces it bit for bit.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace rsh {
+
+RSH_DEV uint32_t ray_hash(float ox, float oy, float oz, float dx, float dy, float dz, const HashP& hp,
+                          uint32_t tag) {
+    const float gmax = (float)((1u << hp.grid_bits) - 1u);
+    float fx = (ox - hp.lo[0]) * hp.scale[0];
+    float fy = (oy - hp.lo[1]) * hp.scale[1];
+    float fz = (oz - hp.lo[2]) * hp.scale[2];
+    fx = fminf(fmaxf(fx, 0.0f), gmax);
+    fy = fminf(fmaxf(fy, 0.0f), gmax);
+    fz = fminf(fmaxf(fz, 0.0f), gmax);
+    const uint32_t cell = (spread3((uint32_t)fx) << 2) | (spread3((uint32_t)fy) << 1) |
+                          spread3((uint32_t)fz);
+    // octahedral map of the direction (L1-normalised; lower hemisphere folded)
+    const float s = (fabsf(dx) + fabsf(dy)) + fabsf(dz);
+    float px = dx / s;
+    float py = dy / s;
+    if (dz < 0.0f) {
+        const float qx = 1.0f - fabsf(py);
+        const float qy = 1.0f - fabsf(px);
+        px = (px >= 0.0f) ? qx : -qx;
+        py = (py >= 0.0f) ? qy : -qy;
+    }
+    const uint32_t B = 1u << hp.dir_log2;
+    const float half_b = 0.5f * (float)B;
+    const float bmax = (float)(B - 1u);
+    float u = (px + 1.0f) * half_b;
+    float v = (py + 1.0f) * half_b;
+    u = fminf(fmaxf(u, 0.0f), bmax);
+    v = fminf(fmaxf(v, 0.0f), bmax);
+    const uint32_t dir = (spread2((uint32_t)u) << 1) | spread2((uint32_t)v);
+    const uint32_t dbits = 2u * hp.dir_log2;
+    const uint32_t hbits = 3u * hp.grid_bits + dbits;
+    return (tag << hbits) | (cell << dbits) | dir;
+}
+
+// ------------------------------------------------------------------ primary rays (tile order)
+__global__ void k_raygen_primary(CameraP cam, uint32_t w, uint32_t h, uint32_t tiles_x, uint32_t n,
+                                 rsh_ray* rays, uint32_t* pixel_of_ray) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t tile = k >> 6, within = k & 63u;
+    const uint32_t x = (tile % tiles_x) * 8u + (within & 7u);
+    const uint32_t y = (tile / tiles_x) * 8u + (within >> 3);
+    float4 o = make_float4(cam.eye[0], cam.eye[1], cam.eye[2], 0.0f);
+    float4 d;
+    if (x < w && y < h) {
+        const float a = (float)x / (float)w - 0.5f;
+        const float b = (float)y / (float)h - 0.5f;
+        v3 q = mk3((cam.dir[0] + cam.right[0] * a) + cam.up[0] * b,
+                   (cam.dir[1] + cam.right[1] * a) + cam.up[1] * b,
+                   (cam.dir[2] + cam.right[2] * a) + cam.up[2] * b);
+        v3 dn = norm3(q);
+        d = make_float4(dn.x, dn.y, dn.z, __int_as_float(0x7f800000));  // tmax = +inf
+        if (pixel_of_ray) pixel_of_ray[k] = y * w + x;
+    } else {
+        d = make_float4(0.0f, 0.0f, 1.0f, -1.0f);  // tmax < tmin: no ray
+        if (pixel_of_ray) pixel_of_ray[k] = 0xFFFFFFFFu;
+    }
+    store_ray(rays, k, o, d);
+}
+
+cudaError_t launch_raygen_primary(const CameraP& cam, uint32_t w, uint32_t h, rsh_ray* rays,
+                                  uint32_t* pixel_of_ray, cudaStream_t s) {
+    const uint32_t tx = (w + 7u) / 8u, ty = (h + 7u) / 8u;
+    const uint32_t n = tx * ty * 64u;
+    if (n == 0) return cudaSuccess;
+    k_raygen_primary<<<(n + 255u) / 256u, 256, 0, s>>>(cam, w, h, tx, n, rays, pixel_of_ray);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ shadow rays
+__global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* __restrict__ snrm,
+                                uint32_t w, uint32_t h, LightsP lights, float eps, HashP hp,
+                                rsh_ray* rays, uint32_t* keys) {
+    const uint32_t L = lights.count;
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= w * h * L) return;
+    // slot = x + W*(l + L*y)  (RayTracer.cu:700-702)
+    const uint32_t x = slot % w;
+    const uint32_t l = (slot / w) % L;
+    const uint32_t y = slot / (w * L);
+    const uint32_t pix = y * w + x;
+    const float4 p4 = __ldg(spos + pix);
+    uint32_t key = RSH_KEY_NONE;
+    if (p4.w != 0.0f) {
+        const v3 p = mk3(p4);
+        const v3 nn = norm3(mk3(__ldg(snrm + pix)));
+        const v3 lp = mk3(lights.pos[l][0], lights.pos[l][1], lights.pos[l][2]);
+        const v3 v = p - lp;
+        const float len = len3(v);
+        const v3 d = v3{v.x / len, v.y / len, v.z / len};
+        const float diffuse = dot3(d, -nn);
+        const float tmax = len - 2.0f * eps;
+        if (diffuse > 0.0f && tmax > eps) {
+            const v3 o = lp + d * eps;
+            store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps), make_float4(d.x, d.y, d.z, tmax));
+            key = ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, hp, l);
+        }
+    }
+    keys[slot] = key;
+}
+
+cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_t w, uint32_t h,
+                                 const LightsP& lights, float eps, const HashP& hp, rsh_ray* rays,
+                                 uint32_t* keys, cudaStream_t s) {
+    const uint32_t n = w * h * lights.count;
+    if (n == 0) return cudaSuccess;
+    k_raygen_shadow<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, w, h, lights, eps, hp, rays, keys);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ reflection rays
+// Integer hash of (seed, slot, bounce) -> 32 random bits (PCG output permutation on an LCG step).
+RSH_DEV uint32_t rng_next(uint32_t& state) {
+    state = state * 747796405u + 2891336453u;
+    uint32_t w = ((state >> ((state >> 28) + 4u)) ^ state) * 277803737u;
+    return (w >> 22) ^ w;
+}
+// Uniform point on the unit sphere by Marsaglia's (1972) rejection method: sqrt only.
+RSH_DEV v3 sphere_sample(uint32_t seed, uint32_t slot, uint32_t bounce) {
+    uint32_t st = seed ^ (slot * 0x9E3779B9u) ^ (bounce * 0x85EBCA6Bu);
+    rng_next(st);
+    for (int it = 0; it < 32; ++it) {
+        const float x1 = (float)(rng_next(st) >> 9) * (1.0f / 4194304.0f) - 1.0f;
+        const float x2 = (float)(rng_next(st) >> 9) * (1.0f / 4194304.0f) - 1.0f;
+        const float q = x1 * x1 + x2 * x2;
+        if (q < 1.0f && q > 0.0f) {
+            const float t = 2.0f * sqrtf(1.0f - q);
+            return v3{x1 * t, x2 * t, 1.0f - 2.0f * q};
+        }
+    }
+    return v3{0.0f, 0.0f, 1.0f};
+}
+
+__global__ void k_raygen_reflect(const float4* __restrict__ spos, const float4* __restrict__ snrm,
+                                 const rsh_ray* __restrict__ prev, v3 eye, uint32_t n, float eps,
+                                 float jitter, uint32_t seed, uint32_t bounce, HashP hp,
+                                 rsh_ray* rays, uint32_t* keys) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n) return;
+    const float4 p4 = __ldg(spos + slot);
+    uint32_t key = RSH_KEY_NONE;
+    if (p4.w != 0.0f) {
+        const v3 p = mk3(p4);
+        const v3 nn = norm3(mk3(__ldg(snrm + slot)));
+        v3 i;
+        if (prev) {
+            float4 po, pd;
+            load_ray(prev, slot, po, pd);
+            i = mk3(pd);
+        } else {
+            i = norm3(p - eye);
+        }
+        const float k2 = 2.0f * dot3(nn, i);
+        v3 r = i - nn * k2;  // reflect(i, n)
+        if (jitter > 0.0f) {
+            const v3 u = sphere_sample(seed, slot, bounce);
+            r = r + u * jitter;
+            const float rn = dot3(r, nn);
+            if (rn < 0.0f) r = r - nn * (2.0f * rn);
+        }
+        r = norm3(r);
+        if (r.x == r.x && r.y == r.y && r.z == r.z) {  // drop degenerate (NaN) directions
+            const v3 o = p + r * eps;
+            store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps),
+                      make_float4(r.x, r.y, r.z, __int_as_float(0x7f800000)));
+            key = ray_hash(o.x, o.y, o.z, r.x, r.y, r.z, hp, 0u);
+        }
+    }
+    keys[slot] = key;
+}
+
+cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const rsh_ray* prev,
+                                  const float eye[3], uint32_t w, uint32_t h, float eps,
+                                  float jitter, uint32_t seed, uint32_t bounce, const HashP& hp,
+                                  rsh_ray* rays, uint32_t* keys, cudaStream_t s) {
+    const uint32_t n = w * h;
+    if (n == 0) return cudaSuccess;
+    k_raygen_reflect<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, prev, v3{eye[0], eye[1], eye[2]}, n,
+                                                     eps, jitter, seed, bounce, hp, rays, keys);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ hash of given rays
+__global__ void k_hash(const rsh_ray* __restrict__ rays, uint32_t n, HashP hp, uint32_t tag,
+                       uint32_t* keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 o, d;
+    load_ray(rays, i, o, d);
+    keys[i] = (d.w > o.w) ? ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, hp, tag) : RSH_KEY_NONE;
+}
+
+cudaError_t launch_hash(const rsh_ray* rays, uint32_t n, const HashP& hp, uint32_t tag,
+                        uint32_t* keys, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_hash<<<(n + 255u) / 256u, 256, 0, s>>>(rays, n, hp, tag, keys);
+    return cudaGetLastError();
+}
+
+// Segmented: binary search of the segment of ray i; the key's tag is the segment index placed at
+// bit tag_shift (above every segment's hash bits).
+__global__ void k_hash_segments(const rsh_ray* __restrict__ rays, uint32_t n,
+                                const uint32_t* __restrict__ seg_start, uint32_t nseg,
+                                const HashP* __restrict__ hps, uint32_t tag_shift, uint32_t* keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t lo = 0, hi = nseg;  // find last s with seg_start[s] <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(seg_start + mid) <= i) lo = mid; else hi = mid;
+    }
+    float4 o, d;
+    load_ray(rays, i, o, d);
+    uint32_t key = RSH_KEY_NONE;
+    if (d.w > o.w) {
+        const HashP hp = hps[lo];
+        key = (lo << tag_shift) | ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, hp, 0u);
+    }
+    keys[i] = key;
+}
+
+cudaError_t launch_hash_segments(const rsh_ray* rays, uint32_t n, const uint32_t* seg_start,
+                                 uint32_t nseg, const HashP* hps_dev, uint32_t tag_shift,
+                                 uint32_t* keys, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_hash_segments<<<(n + 255u) / 256u, 256, 0, s>>>(rays, n, seg_start, nseg, hps_dev, tag_shift,
+                                                    keys);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ fills
+__global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+__global__ void k_fill_u64(unsigned long long* p, unsigned long long v, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    size_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_fill_u32<<<(unsigned)blocks, 256, 0, s>>>(p, v, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_fill_u64(unsigned long long* p, unsigned long long v, size_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    size_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_fill_u64<<<(unsigned)blocks, 256, 0, s>>>(p, v, n);
+    return cudaGetLastError();
+}
+
+}  // namespace rsh

@@ -1,0 +1,250 @@
+// Stable LSD radix sort of (u32 key, u32 value) pairs, onesweep form (Adinets & Merrill 2022).
+//
+// Reference: RaySortingWrapper -> cub::DeviceRadixSort::SortPairs over all 32 key bits
+// (RayTracer.cu:2385-2409, temp storage sized at :2127-2139). Here: our own kernels, and only the
+// ceil(key_bits / 8) digit passes the hash actually uses.
+//
+//  1. one histogram kernel reads the keys once and builds all passes' 256-bin digit histograms;
+//  2. one kernel per 8-bit digit pass: each CTA takes a 3840-key tile by atomic ticket, ranks its keys
+//     stably (warp match_any + per-warp digit counters), publishes its per-digit counts, resolves the
+//     per-digit exclusive prefix over earlier tiles by decoupled look-back (bounded spin), then
+//     scatters through shared memory so that global writes are runs of one digit.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace rsh {
+
+namespace {
+constexpr int SR_THREADS = 256;
+constexpr int SR_WARPS = SR_THREADS / 32;
+constexpr int SR_ITEMS = 15;
+constexpr int SR_TILE = SR_THREADS * SR_ITEMS;  // 3840
+constexpr uint32_t FLAG_AGG = 1u << 30;
+constexpr uint32_t FLAG_PRE = 2u << 30;
+constexpr uint32_t VAL_MASK = (1u << 30) - 1u;
+
+inline uint32_t num_passes(uint32_t key_bits) { return key_bits == 0 ? 1u : (key_bits + 7u) / 8u; }
+}  // namespace
+
+// --- histograms of every pass in one read
+__global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
+                            const uint32_t* __restrict__ d_count, uint32_t passes,
+                            uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[4][256];
+    for (uint32_t i = threadIdx.x; i < 4u * 256u; i += blockDim.x) (&sh[0][0])[i] = 0u;
+    __syncthreads();
+    const uint32_t n = dev_count(d_count, n_max);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = __ldg(keys + i);
+        for (uint32_t p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8u * p)) & 255u], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < passes * 256u; i += blockDim.x) {
+        const uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(hist + i, v);
+    }
+}
+
+__global__ void __launch_bounds__(SR_THREADS)
+k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+           uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n_max,
+           const uint32_t* __restrict__ d_count, uint32_t shift, const uint32_t* __restrict__ hist,
+           uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* err) {
+    __shared__ uint32_t s_wc[SR_WARPS][256];    // per-warp digit counts -> exclusive warp offsets
+    __shared__ uint32_t s_keys[SR_TILE];
+    __shared__ uint32_t s_vals[SR_TILE];
+    __shared__ uint32_t s_start[256];            // tile-local digit start
+    __shared__ uint32_t s_gbase[256];            // global position of the tile's first key of a digit
+    __shared__ uint32_t s_scan[SR_WARPS];
+    __shared__ uint32_t s_tile;
+
+    const uint32_t n = dev_count(d_count, n_max);
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(ticket, 1u);
+    for (uint32_t i = tid; i < SR_WARPS * 256u; i += SR_THREADS) (&s_wc[0][0])[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t num_tiles = (n + SR_TILE - 1) / SR_TILE;
+    if (tile >= num_tiles) return;
+    const uint32_t base = tile * SR_TILE;
+    const uint32_t wbase = base + warp * (SR_ITEMS * 32u);
+
+    uint32_t key[SR_ITEMS], val[SR_ITEMS], rank[SR_ITEMS];
+#pragma unroll
+    for (int j = 0; j < SR_ITEMS; ++j) {
+        const uint32_t idx = wbase + j * 32u + lane;
+        if (idx < n) {
+            key[j] = __ldg(keys_in + idx);
+            val[j] = vals_in ? __ldg(vals_in + idx) : idx;
+        } else {
+            key[j] = 0xFFFFFFFFu;
+            val[j] = 0u;
+        }
+    }
+    // stable in-warp ranking: items in (j, lane) order = index order
+#pragma unroll
+    for (int j = 0; j < SR_ITEMS; ++j) {
+        const uint32_t idx = wbase + j * 32u + lane;
+        const bool valid = idx < n;
+        const uint32_t d = valid ? ((key[j] >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t before = __popc(peers & lanemask_lt());
+        uint32_t cnt = 0u;
+        if (valid) cnt = s_wc[warp][d];
+        __syncwarp();
+        if (valid && before == 0u) s_wc[warp][d] = cnt + __popc(peers);
+        __syncwarp();
+        rank[j] = cnt + before;
+    }
+    __syncthreads();
+    // per digit (thread = digit): warp-exclusive offsets and the tile count
+    const uint32_t dg = tid;  // SR_THREADS == 256
+    uint32_t tcount = 0u;
+#pragma unroll
+    for (int w = 0; w < SR_WARPS; ++w) {
+        const uint32_t c = s_wc[w][dg];
+        s_wc[w][dg] = tcount;
+        tcount += c;
+    }
+    // publish the tile's count for this digit early so successors can proceed
+    uint32_t* st = status + (size_t)tile * 256u + dg;
+    if (tile == 0) st_release_u32(st, FLAG_PRE | tcount);
+    else st_release_u32(st, FLAG_AGG | tcount);
+    // exclusive scan over digits of tcount -> s_start
+    {
+        uint32_t x = tcount;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= (uint32_t)d) x += y;
+        }
+        if (lane == 31) s_scan[warp] = x;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t r = 0;
+            for (int w = 0; w < SR_WARPS; ++w) {
+                const uint32_t t = s_scan[w];
+                s_scan[w] = r;
+                r += t;
+            }
+        }
+        __syncthreads();
+        s_start[dg] = s_scan[warp] + x - tcount;
+    }
+    // global digit offset of this pass: exclusive scan of hist over digits
+    uint32_t gex;
+    {
+        const uint32_t hv = __ldg(hist + dg);
+        uint32_t x = hv;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= (uint32_t)d) x += y;
+        }
+        __syncthreads();
+        if (lane == 31) s_scan[warp] = x;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t r = 0;
+            for (int w = 0; w < SR_WARPS; ++w) {
+                const uint32_t t = s_scan[w];
+                s_scan[w] = r;
+                r += t;
+            }
+        }
+        __syncthreads();
+        gex = s_scan[warp] + x - hv;
+    }
+    // decoupled look-back for this digit
+    uint32_t excl = 0u;
+    if (tile > 0) {
+        int64_t j = (int64_t)tile - 1;
+        uint32_t spins = 0;
+        while (j >= 0) {
+            const uint32_t s = ld_acquire_u32(status + (size_t)j * 256u + dg);
+            const uint32_t f = s & ~VAL_MASK;
+            if (f == 0u) {
+                if (++spins > RSH_SPIN_LIMIT) {
+                    raise_device_error(err, RSH_DEVERR_TIMEOUT);
+                    break;
+                }
+                if (spins > 64) __nanosleep(32);
+                continue;
+            }
+            excl += s & VAL_MASK;
+            if (f == FLAG_PRE) break;
+            --j;
+        }
+        st_release_u32(st, FLAG_PRE | (excl + tcount));
+    }
+    s_gbase[dg] = gex + excl - s_start[dg];
+    __syncthreads();
+    // scatter into shared memory in tile-sorted order
+#pragma unroll
+    for (int j = 0; j < SR_ITEMS; ++j) {
+        const uint32_t idx = wbase + j * 32u + lane;
+        if (idx < n) {
+            const uint32_t d = (key[j] >> shift) & 255u;
+            const uint32_t pos = s_start[d] + s_wc[warp][d] + rank[j];
+            s_keys[pos] = key[j];
+            s_vals[pos] = val[j];
+        }
+    }
+    __syncthreads();
+    const uint32_t tn = (n - base) < (uint32_t)SR_TILE ? (n - base) : (uint32_t)SR_TILE;
+    for (uint32_t i = tid; i < tn; i += SR_THREADS) {
+        const uint32_t k = s_keys[i];
+        const uint32_t d = (k >> shift) & 255u;
+        const uint32_t g = s_gbase[d] + i;
+        if (g < n) {  // only false after a look-back timeout (error word raised)
+            keys_out[g] = k;
+            vals_out[g] = s_vals[i];
+        }
+    }
+}
+
+size_t sort_scratch_bytes(uint32_t n_max, uint32_t key_bits) {
+    const size_t passes = num_passes(key_bits);
+    const size_t tiles = (n_max + SR_TILE - 1) / SR_TILE + 1;
+    const size_t words = 4 * 256 + 8 + passes * tiles * 256;
+    return words * 4 + 2 * (size_t)n_max * 4 + 1024;
+}
+
+cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                              uint32_t* vals_out, uint32_t n_max, const uint32_t* d_count,
+                              uint32_t key_bits, void* scratch, uint32_t* err, cudaStream_t s) {
+    if (n_max == 0) return cudaSuccess;
+    const uint32_t passes = num_passes(key_bits);
+    const size_t tiles = (n_max + SR_TILE - 1) / SR_TILE + 1;
+    uint32_t* w = static_cast<uint32_t*>(scratch);
+    uint32_t* hist = w;                       // passes * 256 (room for 4)
+    uint32_t* tickets = w + 4 * 256;          // 8
+    uint32_t* status = tickets + 8;           // passes * tiles * 256
+    uint32_t* alt_keys = status + passes * tiles * 256;
+    alt_keys = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(alt_keys) + 255) & ~uintptr_t(255));
+    uint32_t* alt_vals = alt_keys + n_max;
+    cudaError_t e = cudaMemsetAsync(w, 0, (4 * 256 + 8 + passes * tiles * 256) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    k_sort_hist<<<152 * 2, 256, 0, s>>>(keys_in, n_max, d_count, passes, hist);
+    // ping-pong so that the last pass lands in the output
+    const uint32_t* ki = keys_in;
+    const uint32_t* vi = vals_in;
+    for (uint32_t p = 0; p < passes; ++p) {
+        const bool last = (p + 1 == passes);
+        // choose destinations: passes alternate between out and alt, ending in out
+        const bool to_out = ((passes - 1 - p) % 2u) == 0u;
+        uint32_t* ko = to_out ? keys_out : alt_keys;
+        uint32_t* vo = to_out ? vals_out : alt_vals;
+        (void)last;
+        const uint32_t grid = (uint32_t)(tiles - 1 > 0 ? tiles - 1 : 1);
+        k_onesweep<<<grid, SR_THREADS, 0, s>>>(ki, vi, ko, vo, n_max, d_count, 8u * p, hist + 256u * p,
+                                               status + p * tiles * 256, tickets + p, err);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        ki = ko;
+        vi = vo;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace rsh
