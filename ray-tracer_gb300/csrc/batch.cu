@@ -1,0 +1,435 @@
+// Batched form: many ray batches of uneven size over several resident scenes in one pass.
+//
+// The reference has no batched path: every batch is a host loop of wrappers with a blocking count
+// readback after each stage (main.cpp:951-1054, RayTracer.cu:2316-2832). Here, for S segments:
+//   k_batch_prep     one pass over all rays: gather into one array, key = segment << shift | hash
+//                    (per-segment scene box), pre-fill each segment's output;
+//   compress / sort / decompress over all keys at once (the segment tag is the top key digit, so the
+//                    sorted order is segment-major: a segmented sort for free);
+//   k_batch_bounds   per-segment ray ranges of the sorted order (binary search on the tag), padded so
+//                    that no level-1 ray node straddles two segments;
+//   k_batch_pad      padded ray order (empty slots = inactive rays);
+//   build            ray-space hierarchy over the padded order;
+//   fused            ONE persistent traversal + intersection launch over every segment's work units.
+// Nothing reads a count back to the host, so the whole sequence is captured in a CUDA graph.
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+#include "hash.cuh"
+
+namespace rsh {
+
+namespace {
+constexpr uint32_t INVALID_ID = 0xFFFFFFFFu;
+
+struct PrepSeg {  // per-segment table of k_batch_prep
+    const rsh_ray* rays;
+    uint32_t start;
+    uint32_t any_hit;
+    uint32_t* flags;
+    unsigned long long* hits;
+    HashP hp;
+};
+}  // namespace
+
+__global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, uint32_t total, uint32_t tag_shift,
+                             rsh_ray* __restrict__ rays_all, uint32_t* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&segs[mid].start) <= i) lo = mid; else hi = mid;
+    }
+    const PrepSeg& sg = segs[lo];
+    const uint32_t j = i - sg.start;
+    float4 o, d;
+    load_ray(sg.rays, j, o, d);
+    store_ray(rays_all, i, o, d);
+    uint32_t key = RSH_KEY_NONE;
+    if (d.w > o.w) {
+        key = (lo << tag_shift) | ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, sg.hp, 0u);
+    }
+    keys[i] = key;
+    if (sg.any_hit) sg.flags[j] = 0u;
+    else sg.hits[j] = RSH_HIT_NONE;
+}
+
+// Per-segment ranges in the sorted (segment-major) order and the padded layout; one block.
+__global__ void k_batch_bounds(const uint32_t* __restrict__ sorted_keys, const uint32_t* __restrict__ counts,
+                               uint32_t nseg, uint32_t tag_shift, uint32_t unit_rays, uint32_t* __restrict__ seg_begin,
+                               uint32_t* __restrict__ seg_cnt, uint32_t* __restrict__ pstart,
+                               FusedSeg* __restrict__ fsegs, uint32_t* __restrict__ totals) {
+    const uint32_t R = counts[0];
+    for (uint32_t s = threadIdx.x; s < nseg; s += blockDim.x) {
+        auto lower = [&](uint32_t key) {
+            uint32_t lo = 0, hi = R;  // first index with sorted_keys >= key
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (sorted_keys[mid] < key) lo = mid + 1; else hi = mid;
+            }
+            return lo;
+        };
+        const uint32_t b = lower(s << tag_shift);
+        const uint32_t e = lower((s + 1) << tag_shift);
+        seg_begin[s] = b;
+        seg_cnt[s] = e - b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (uint32_t s = 0; s < nseg; ++s) {
+            pstart[s] = acc;
+            fsegs[s].unit_begin = acc / unit_rays;
+            acc += ((seg_cnt[s] + unit_rays - 1) / unit_rays) * unit_rays;
+        }
+        pstart[nseg] = acc;
+        totals[0] = acc;              // padded ray count
+        totals[1] = acc / unit_rays;  // work units
+    }
+}
+
+__global__ void k_batch_pad(const uint32_t* __restrict__ sorted_ids, const uint32_t* __restrict__ seg_begin,
+                            const uint32_t* __restrict__ seg_cnt, const uint32_t* __restrict__ pstart, uint32_t nseg,
+                            uint32_t max_padded, const uint32_t* __restrict__ totals, uint32_t* __restrict__ padded) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= max_padded || q >= totals[0]) return;
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(pstart + mid) <= q) lo = mid; else hi = mid;
+    }
+    const uint32_t j = q - pstart[lo];
+    padded[q] = (j < seg_cnt[lo]) ? sorted_ids[seg_begin[lo] + j] : INVALID_ID;
+}
+
+}  // namespace rsh
+
+using namespace rsh;
+
+namespace {
+
+struct BatchPlan {
+    uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0;
+    void *rays_all, *keys, *trimmed, *ckeys, *cbases, *counts, *skeys, *svals, *sorted_keys, *sorted_ids, *scr;
+    void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work;
+    std::vector<PrepSeg> h_prep;
+    std::vector<FusedSeg> h_fsegs;
+};
+
+rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count, BatchPlan& pl) {
+    if (!ctx || (!segs && count)) return RSH_ERR_INVALID;
+    if (count > 1024) {
+        set_error("at most 1024 batch segments");
+        return RSH_ERR_INVALID;
+    }
+    pl.nseg = count;
+    uint64_t total = 0;
+    for (uint32_t s = 0; s < count; ++s) {
+        const rsh_batch_segment& g = segs[s];
+        if (!g.scene || (g.n && !g.rays) || (g.any_hit ? !g.flags : !g.hits)) return RSH_ERR_INVALID;
+        total += g.n;
+    }
+    if (total >= (1ull << 31)) return RSH_ERR_INVALID;
+    pl.total = (uint32_t)total;
+    uint32_t tag_bits = 0;
+    while ((1u << tag_bits) < count) ++tag_bits;
+    pl.tag_shift = 3 * ctx->cfg.grid_bits + 2 * ctx->cfg.dir_log2;
+    pl.key_bits = pl.tag_shift + tag_bits;
+    if (pl.key_bits > 31) {
+        set_error("segment tag + hash exceed 31 key bits: lower grid_bits / dir_log2");
+        return RSH_ERR_INVALID;
+    }
+    pl.P = ctx->cfg.packet_size;
+    pl.unit_rays = 8 * pl.P;
+    pl.max_padded = pl.total + count * pl.unit_rays;
+    const uint32_t n = pl.total ? pl.total : 1;
+    RSH_TRY(ensure(ctx, "b_rays", sizeof(rsh_ray) * (size_t)n, &pl.rays_all));
+    RSH_TRY(ensure(ctx, "b_keys", 4ull * n, &pl.keys));
+    RSH_TRY(ensure(ctx, "trimmed", 4ull * n, &pl.trimmed));
+    RSH_TRY(ensure(ctx, "ckeys", 4ull * n + 4, &pl.ckeys));
+    RSH_TRY(ensure(ctx, "cbases", 4ull * n + 4, &pl.cbases));
+    RSH_TRY(ensure(ctx, "b_counts", 64, &pl.counts));
+    RSH_TRY(ensure(ctx, "skeys", 4ull * n, &pl.skeys));
+    RSH_TRY(ensure(ctx, "svals", 4ull * n, &pl.svals));
+    RSH_TRY(ensure(ctx, "sorted_keys", 4ull * n, &pl.sorted_keys));
+    RSH_TRY(ensure(ctx, "sorted_ids", 4ull * n, &pl.sorted_ids));
+    size_t scr = std::max(compress_scratch_bytes(n), sort_scratch_bytes(n, pl.key_bits));
+    scr = std::max(scr, decompress_scratch_bytes(n));
+    RSH_TRY(ensure(ctx, "scratch", scr, &pl.scr));
+    RSH_TRY(ensure(ctx, "b_padded", 4ull * pl.max_padded, &pl.padded));
+    uint32_t off[4];
+    const uint32_t capn = hierarchy_capacity(pl.max_padded, pl.P, off);
+    RSH_TRY(ensure(ctx, "b_nodes", sizeof(rsh_node) * (size_t)capn, &pl.nodes));
+    RSH_TRY(ensure(ctx, "b_prep", sizeof(PrepSeg) * (count ? count : 1), &pl.prep));
+    RSH_TRY(ensure(ctx, "b_fsegs", sizeof(FusedSeg) * (count ? count : 1), &pl.fsegs));
+    RSH_TRY(ensure(ctx, "b_seg_begin", 4ull * (count + 1), &pl.seg_begin));
+    RSH_TRY(ensure(ctx, "b_seg_cnt", 4ull * (count + 1), &pl.seg_cnt));
+    RSH_TRY(ensure(ctx, "b_pstart", 4ull * (count + 1), &pl.pstart));
+    RSH_TRY(ensure(ctx, "b_totals", 64, &pl.totals));
+    RSH_TRY(ensure(ctx, "b_work", 64, &pl.work));
+    pl.h_prep.resize(count);
+    pl.h_fsegs.resize(count);
+    uint32_t start = 0;
+    for (uint32_t s = 0; s < count; ++s) {
+        const rsh_batch_segment& g = segs[s];
+        const rsh_scene* sc = g.scene;
+        PrepSeg& p = pl.h_prep[s];
+        p.rays = g.rays;
+        p.start = start;
+        p.any_hit = g.any_hit ? 1u : 0u;
+        p.flags = g.flags;
+        p.hits = reinterpret_cast<unsigned long long*>(g.hits);
+        RSH_TRY(make_hash_params(sc, ctx->cfg, 0, p.hp));
+        FusedSeg& f = pl.h_fsegs[s];
+        std::memset(&f, 0, sizeof(f));
+        f.spheres = sc->h.spheres;
+        f.tris = sc->h.tris;
+        f.tri_count = sc->tri_count;
+        f.cluster = sc->h.cluster;
+        f.levels = sc->h.levels;
+        for (uint32_t l = 0; l < sc->h.levels; ++l) {
+            f.lvl_off[l] = sc->h.level_off[l];
+            f.lvl_size[l] = sc->h.level_size[l];
+        }
+        f.any_hit = p.any_hit;
+        f.flags = g.flags;
+        f.hits = reinterpret_cast<unsigned long long*>(g.hits);
+        f.slot_base = start;
+        start += g.n;
+    }
+    return RSH_OK;
+}
+
+// Host staging of the segment tables: pinned memory owned per context, which a captured graph reads
+// again on every replay.
+struct HostStage {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+std::map<const rsh_ctx*, HostStage> g_stage;
+
+rsh_status stage_tables(rsh_ctx* ctx, BatchPlan& pl, void** prep_h, void** fsegs_h) {
+    HostStage& hs = g_stage[ctx];
+    const size_t need = sizeof(PrepSeg) * pl.nseg + sizeof(FusedSeg) * pl.nseg + 256;
+    if (hs.bytes < need) {
+        if (hs.ptr) cudaFreeHost(hs.ptr);
+        hs.ptr = nullptr;
+        RSH_CUDA(cudaMallocHost(&hs.ptr, need));
+        hs.bytes = need;
+    }
+    char* b = static_cast<char*>(hs.ptr);
+    std::memcpy(b, pl.h_prep.data(), sizeof(PrepSeg) * pl.nseg);
+    std::memcpy(b + sizeof(PrepSeg) * pl.nseg, pl.h_fsegs.data(), sizeof(FusedSeg) * pl.nseg);
+    *prep_h = b;
+    *fsegs_h = b + sizeof(PrepSeg) * pl.nseg;
+    return RSH_OK;
+}
+
+rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s) {
+    if (pl.nseg == 0) return RSH_OK;
+    void *prep_h, *fsegs_h;
+    RSH_TRY(stage_tables(ctx, pl, &prep_h, &fsegs_h));
+    RSH_CUDA(cudaMemcpyAsync(pl.prep, prep_h, sizeof(PrepSeg) * pl.nseg, cudaMemcpyHostToDevice, s));
+    RSH_CUDA(cudaMemcpyAsync(pl.fsegs, fsegs_h, sizeof(FusedSeg) * pl.nseg, cudaMemcpyHostToDevice, s));
+    RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
+    if (pl.total == 0) return RSH_OK;
+    uint32_t* cnt = static_cast<uint32_t*>(pl.counts);
+    k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
+                                                       pl.tag_shift, static_cast<rsh_ray*>(pl.rays_all),
+                                                       static_cast<uint32_t*>(pl.keys));
+    RSH_CUDA(cudaGetLastError());
+    RSH_CUDA(launch_compress(static_cast<uint32_t*>(pl.keys), pl.total, static_cast<uint32_t*>(pl.trimmed),
+                             static_cast<uint32_t*>(pl.ckeys), static_cast<uint32_t*>(pl.cbases), cnt, pl.scr,
+                             ctx->d_err, s));
+    RSH_CUDA(launch_sort_pairs(static_cast<uint32_t*>(pl.ckeys), nullptr, static_cast<uint32_t*>(pl.skeys),
+                               static_cast<uint32_t*>(pl.svals), pl.total, cnt + 1, pl.key_bits, pl.scr, ctx->d_err,
+                               s));
+    RSH_CUDA(launch_decompress(static_cast<uint32_t*>(pl.skeys), static_cast<uint32_t*>(pl.svals),
+                               static_cast<uint32_t*>(pl.cbases), static_cast<uint32_t*>(pl.trimmed), cnt, pl.total,
+                               static_cast<uint32_t*>(pl.sorted_keys), static_cast<uint32_t*>(pl.sorted_ids), pl.scr,
+                               ctx->d_err, s));
+    uint32_t* totals = static_cast<uint32_t*>(pl.totals);
+    k_batch_bounds<<<1, 1024, 0, s>>>(static_cast<uint32_t*>(pl.sorted_keys), cnt, pl.nseg, pl.tag_shift,
+                                      pl.unit_rays, static_cast<uint32_t*>(pl.seg_begin),
+                                      static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart),
+                                      static_cast<FusedSeg*>(pl.fsegs), totals);
+    RSH_CUDA(cudaGetLastError());
+    k_batch_pad<<<(pl.max_padded + 255) / 256, 256, 0, s>>>(
+        static_cast<uint32_t*>(pl.sorted_ids), static_cast<uint32_t*>(pl.seg_begin),
+        static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart), pl.nseg, pl.max_padded, totals,
+        static_cast<uint32_t*>(pl.padded));
+    RSH_CUDA(cudaGetLastError());
+    RSH_CUDA(launch_build_rsh(static_cast<rsh_ray*>(pl.rays_all), static_cast<uint32_t*>(pl.padded), pl.max_padded,
+                              totals, pl.P, static_cast<rsh_node*>(pl.nodes), s));
+    RSH_CUDA(cudaMemsetAsync(pl.work, 0, 16, s));
+    FusedArgs fa{};
+    fa.nodes = static_cast<rsh_node*>(pl.nodes);
+    hierarchy_capacity(pl.max_padded, pl.P, fa.node_off);
+    fa.packet = pl.P;
+    fa.rays = static_cast<rsh_ray*>(pl.rays_all);
+    fa.sorted_ids = static_cast<uint32_t*>(pl.padded);
+    fa.segs = static_cast<FusedSeg*>(pl.fsegs);
+    fa.nseg = pl.nseg;
+    fa.unit_seg = nullptr;
+    fa.units_max = pl.max_padded / pl.unit_rays;
+    fa.d_units = totals + 1;
+    fa.work = static_cast<uint32_t*>(pl.work);
+    fa.node_tests = ctx->d_stats;
+    fa.tri_tests = ctx->d_stats + 1;
+    fa.err = ctx->d_err;
+    RSH_CUDA(launch_fused(fa, s));
+    return RSH_OK;
+}
+
+struct GraphExec {
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    rsh_ctx* ctx = nullptr;
+};
+
+}  // namespace
+
+extern "C" {
+
+rsh_status rsh_batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, rsh_stream_t stream) {
+    BatchPlan pl;
+    RSH_TRY(batch_prepare(ctx, segments, count, pl));
+    ctx->last_stream = stream;
+    RSH_TRY(batch_enqueue(ctx, pl, stream));
+    ctx->batch_counts_host.assign(1, pl.total);
+    return RSH_OK;
+}
+
+rsh_status rsh_batch_graph_create(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count,
+                                  rsh_stream_t stream, void** graph_exec) {
+    if (!ctx || !graph_exec) return RSH_ERR_INVALID;
+    if (stream == nullptr) {
+        set_error("graph capture needs a non-default stream");
+        return RSH_ERR_INVALID;
+    }
+    BatchPlan pl;
+    RSH_TRY(batch_prepare(ctx, segments, count, pl));
+    // warm-up run outside capture (sizes buffers, sets kernel attributes)
+    RSH_TRY(batch_enqueue(ctx, pl, stream));
+    RSH_CUDA(cudaStreamSynchronize(stream));
+    GraphExec* g = new GraphExec();
+    g->ctx = ctx;
+    cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        delete g;
+        return cuda_status(e, "cudaStreamBeginCapture");
+    }
+    rsh_status st = batch_enqueue(ctx, pl, stream);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(stream, &graph);
+    if (st != RSH_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        delete g;
+        return st != RSH_OK ? st : cuda_status(e, "cudaStreamEndCapture");
+    }
+    g->graph = graph;
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        delete g;
+        return cuda_status(e, "cudaGraphInstantiate");
+    }
+    ctx->last_stream = stream;
+    *graph_exec = g;
+    return RSH_OK;
+}
+
+rsh_status rsh_batch_graph_launch(void* graph_exec, rsh_stream_t stream) {
+    GraphExec* g = static_cast<GraphExec*>(graph_exec);
+    if (!g || !g->exec) return RSH_ERR_INVALID;
+    RSH_CUDA(cudaGraphLaunch(g->exec, stream));
+    g->ctx->last_stream = stream;
+    return RSH_OK;
+}
+
+rsh_status rsh_batch_graph_destroy(void* graph_exec) {
+    GraphExec* g = static_cast<GraphExec*>(graph_exec);
+    if (!g) return RSH_ERR_INVALID;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return RSH_OK;
+}
+
+rsh_status rsh_batch_stats_get(rsh_ctx* ctx, rsh_frame_stats* out) {
+    if (!ctx || !out) return RSH_ERR_INVALID;
+    RSH_CUDA(cudaStreamSynchronize(ctx->last_stream));
+    rsh_frame_stats st{};
+    uint32_t cnt[2] = {0, 0};
+    void* counts = ctx->bufs.count("b_counts") ? ctx->bufs["b_counts"].ptr : nullptr;
+    if (counts) RSH_CUDA(cudaMemcpy(cnt, counts, 8, cudaMemcpyDeviceToHost));
+    unsigned long long d[2] = {0, 0};
+    RSH_CUDA(cudaMemcpy(d, ctx->d_stats, 16, cudaMemcpyDeviceToHost));
+    st.reflection_rays = cnt[0];
+    st.chunks = cnt[1];
+    st.node_tests = d[0];
+    st.tri_tests = d[1];
+    *out = st;
+    return RSH_OK;
+}
+
+rsh_status rsh_trace_rays_fused(rsh_ctx* ctx, const rsh_scene* sc, const rsh_ray* rays, uint32_t n, int any_hit,
+                                uint64_t* hits, uint32_t* flags, rsh_stream_t stream) {
+    if (!ctx || !sc || !rays) return RSH_ERR_INVALID;
+    if (any_hit ? !flags : !hits) return RSH_ERR_INVALID;
+    rsh_batch_segment seg;
+    seg.scene = sc;
+    seg.rays = rays;
+    seg.n = n;
+    seg.any_hit = any_hit;
+    seg.hits = hits;
+    seg.flags = flags;
+    return rsh_batch_trace(ctx, &seg, 1, stream);
+}
+
+rsh_status rsh_autotune(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, const uint32_t* grid_bits,
+                        uint32_t n_grid, const uint32_t* dir_log2, uint32_t n_dir, const uint32_t* packet_sizes,
+                        uint32_t n_packet, rsh_stream_t stream, rsh_config* best) {
+    if (!ctx || !grid_bits || !dir_log2 || !packet_sizes || !n_grid || !n_dir || !n_packet) return RSH_ERR_INVALID;
+    const rsh_config base = ctx->cfg;
+    rsh_config best_cfg = base;
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    RSH_CUDA(cudaEventCreate(&e0));
+    RSH_CUDA(cudaEventCreate(&e1));
+    for (uint32_t a = 0; a < n_grid; ++a)
+        for (uint32_t b = 0; b < n_dir; ++b)
+            for (uint32_t c = 0; c < n_packet; ++c) {
+                rsh_config cfg = base;
+                cfg.grid_bits = grid_bits[a];
+                cfg.dir_log2 = dir_log2[b];
+                cfg.packet_size = packet_sizes[c];
+                if (rsh_set_config(ctx, &cfg) != RSH_OK) continue;
+                BatchPlan pl;
+                if (batch_prepare(ctx, segments, count, pl) != RSH_OK) continue;
+                if (batch_enqueue(ctx, pl, stream) != RSH_OK) continue;  // warm-up
+                cudaEventRecord(e0, stream);
+                const int reps = 2;
+                rsh_status st = RSH_OK;
+                for (int r = 0; r < reps && st == RSH_OK; ++r) st = batch_enqueue(ctx, pl, stream);
+                cudaEventRecord(e1, stream);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (st == RSH_OK && ms / reps < best_ms) {
+                    best_ms = ms / reps;
+                    best_cfg = cfg;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    rsh_set_config(ctx, &best_cfg);
+    if (best) *best = best_cfg;
+    return best_ms < 1e30f ? RSH_OK : RSH_ERR_INVALID;
+}
+
+}  // extern "C"

@@ -46,8 +46,12 @@ __global__ void k_build_leaves(const rsh_ray* __restrict__ rays, const uint32_t*
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 0.f, -1.f);
     if (active) {
         const uint32_t id = sorted_ids ? __ldg(sorted_ids + k) : k;
-        load_ray(rays, id, o, d);
-        active = d.w > o.w;
+        if (id != 0xFFFFFFFFu) {  // padding slot of the batched layout: no ray
+            load_ray(rays, id, o, d);
+            active = d.w > o.w;
+        } else {
+            active = false;
+        }
     }
     const float inf = __int_as_float(0x7f800000);
     float mnx = active ? o.x : inf, mny = active ? o.y : inf, mnz = active ? o.z : inf;

@@ -1,0 +1,300 @@
+// Fused persistent traversal + intersection (the batched form's single launch).
+//
+// Reference: the per-frame loop of HierarchyTraversalWarmUpWrapper -> HierarchyTraversalWrapper ->
+// Shadow/ReflectionRayIntersectionWrapper (main.cpp:685-755, RayTracer.cu:2537-3031), which materialises
+// (node, triangle) records and resolves hits with atomics. Here one persistent kernel takes work units
+// (level-1 ray nodes = 8 packets, never straddling a batch segment) from an atomic counter; each warp
+// keeps the unit's rays in shared memory (watertight setup precomputed), walks the segment's
+// object-sphere tree depth-first with (node, packet-mask) stack entries, children pushed farthest-first
+// so that the nearest subtree is visited first, and at every triangle cluster immediately tests the
+// surviving packets' rays against the cluster's triangles staged in shared memory.
+//   closest hit: per-ray best (t bits << 32 | triangle id) kept in shared memory; after each cluster a
+//     packet's `reach` shrinks to max(|o - c| + best t), so later subtrees beyond every current hit are
+//     culled by the node test (early termination without changing any result);
+//   any hit: a packet leaves the traversal once all its rays are occluded.
+// Each ray belongs to exactly one work unit, so results are written with plain stores (no atomics).
+#include "common.cuh"
+#include "kernels.h"
+#include "tests.cuh"
+
+namespace rsh {
+
+namespace {
+constexpr int FW = 4;            // warps per block
+constexpr int F_STACK = 96;
+constexpr int F_MAXK = 32;       // max cluster size staged in shared memory
+constexpr uint32_t INVALID_ID = 0xFFFFFFFFu;
+}
+
+template <int P>
+struct FusedSmem {
+    float4 ro[8 * P];             // origin xyz, tmin
+    float4 rs[8 * P];             // shear sx, sy, sz, tmax (original)
+    uint32_t meta[8 * P];         // kx | ky << 2 | kz << 4 | active << 6 | occluded << 7
+    uint32_t slot[8 * P];
+    float roc[8 * P];             // |o - packet centre|
+    unsigned long long best[8 * P];
+    float4 tri[F_MAXK * 3];
+    uint32_t stack[F_STACK];
+    float cdist[8];
+};
+
+RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
+    uint32_t lo = 0, hi = nseg;  // last s with unit_begin <= u
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&segs[mid].unit_begin) <= u) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <int P>
+__global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FusedSmem<P>& S = reinterpret_cast<FusedSmem<P>*>(smem_raw)[threadIdx.x >> 5];
+    const uint32_t lane = lane_id();
+    const uint32_t ch = lane & 7u, q = lane >> 3;
+    const uint32_t units = dev_count(a.d_units, a.units_max);
+    unsigned long long ntests = 0, ttests = 0;
+    constexpr uint32_t R = 8 * P;
+
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(&a.work[0], 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= units) break;
+        const uint32_t sidx = find_segment(a.segs, a.nseg, u);
+        const FusedSeg& sg = a.segs[sidx];
+        const bool any = sg.any_hit != 0;
+        // ---- rays of the unit -> shared memory
+        const NodeR U = load_node(a.nodes, a.node_off[1] + u);
+        for (uint32_t i = lane; i < R; i += 32) {
+            const uint32_t k = u * R + i;
+            const uint32_t id = __ldg(a.sorted_ids + k);
+            uint32_t meta = 0;
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, -1.f);
+            if (id != INVALID_ID) load_ray(a.rays, id, o, d);
+            const bool active = (id != INVALID_ID) && (d.w > o.w);
+            const RayWT w = wt_setup(o, d);
+            meta = (uint32_t)w.kx | ((uint32_t)w.ky << 2) | ((uint32_t)w.kz << 4) | (active ? 64u : 0u);
+            S.ro[i] = make_float4(o.x, o.y, o.z, o.w);
+            S.rs[i] = make_float4(w.sx, w.sy, w.sz, d.w);
+            S.meta[i] = meta;
+            S.slot[i] = id;
+            S.best[i] = RSH_HIT_NONE;
+            S.roc[i] = 0.f;
+        }
+        // ---- the lane's two packets (2q, 2q+1) in registers
+        const uint32_t p0 = 8u * u + 2u * q, p1 = p0 + 1u;
+        NodeR P0 = load_node(a.nodes, a.node_off[0] + p0);
+        NodeR P1 = load_node(a.nodes, a.node_off[0] + p1);
+        const bool v0 = P0.count > 0, v1 = P1.count > 0;
+        __syncwarp();
+        // |o - packet centre| per ray (for the shrinking reach of closest-hit packets)
+        for (uint32_t i = lane; i < R; i += 32) {
+            const NodeR& Pk = ((i / P) & 1u) ? P1 : P0;  // placeholder; recomputed below
+            (void)Pk;
+        }
+        {
+            // lane ch of group q computes for packet 2q (rays [2q*P, 2q*P+P)) and 2q+1, spread over 8 lanes
+            for (uint32_t j = ch; j < 2u * P; j += 8u) {
+                const uint32_t pk = 2u * q + (j / P);
+                const uint32_t i = pk * P + (j % P);
+                const NodeR& Pk = (j / P) ? P1 : P0;
+                const float4 o = S.ro[i];
+                const v3 dd = v3{o.x - Pk.cx, o.y - Pk.cy, o.z - Pk.cz};
+                S.roc[i] = len3(dd);
+            }
+        }
+        const uint32_t b0 = __ballot_sync(0xffffffffu, v0), b1 = __ballot_sync(0xffffffffu, v1);
+        uint32_t mask = 0;
+#pragma unroll
+        for (uint32_t g = 0; g < 4; ++g)
+            mask |= (((b0 >> (8u * g)) & 1u) << (2u * g)) | (((b1 >> (8u * g)) & 1u) << (2u * g + 1u));
+        uint32_t alive = mask;
+        __syncwarp();
+        if (mask != 0) {
+            int sp = 1;
+            if (lane == 0) S.stack[0] = (sg.levels << 28) | mask;
+            __syncwarp();
+            while (sp > 0) {
+                const uint32_t e = S.stack[sp - 1];
+                __syncwarp();
+                --sp;
+                const uint32_t L = e >> 28, idx = (e >> 8) & 0xFFFFFu;
+                const uint32_t m = (e & 0xFFu) & alive;
+                if (m == 0) continue;
+                const uint32_t cl = L - 1u;
+                const uint32_t first = (L == sg.levels) ? 0u : 8u * idx;
+                const uint32_t size = sg.lvl_size[cl];
+                const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+                const bool has = ch < cnt;
+                float4 Sph = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (has) Sph = __ldg(sg.spheres + sg.lvl_off[cl] + first + ch);
+                const bool t0 = has && ((m >> (2u * q)) & 1u);
+                const bool t1 = has && ((m >> (2u * q + 1u)) & 1u);
+                const bool r0 = t0 && node_hits_sphere(P0, Sph);
+                const bool r1 = t1 && node_hits_sphere(P1, Sph);
+                ntests += (t0 ? 1u : 0u) + (t1 ? 1u : 0u);
+                const uint32_t h0 = __ballot_sync(0xffffffffu, r0), h1 = __ballot_sync(0xffffffffu, r1);
+                uint32_t cm = 0;
+#pragma unroll
+                for (uint32_t g = 0; g < 4; ++g)
+                    cm |= (((h0 >> (ch + 8u * g)) & 1u) << (2u * g)) | (((h1 >> (ch + 8u * g)) & 1u) << (2u * g + 1u));
+                if (lane >= 8u) cm = 0;
+                // distance of each surviving child from the unit centre -> order
+                const bool live = cm != 0u;
+                const float dist = live ? len3(v3{Sph.x - U.cx, Sph.y - U.cy, Sph.z - U.cz}) - Sph.w : 0.f;
+                const uint32_t lb = __ballot_sync(0xffffffffu, live);
+                if (lb == 0) continue;
+                uint32_t farther = 0;  // children farther than this one (ties: larger index counts as farther)
+#pragma unroll
+                for (uint32_t o2 = 0; o2 < 8; ++o2) {
+                    const float od = __shfl_sync(0xffffffffu, dist, o2);
+                    if (live && ((lb >> o2) & 1u) && o2 != lane && (od > dist || (od == dist && o2 > lane))) ++farther;
+                }
+                const uint32_t nlive = __popc(lb);
+                if (cl == 0) {
+                    // visit clusters nearest first: rank r = nlive-1-farther
+                    for (uint32_t rk = 0; rk < nlive; ++rk) {
+                        const uint32_t sel = __ballot_sync(0xffffffffu, live && (nlive - 1u - farther) == rk);
+                        const uint32_t c = __ffs(sel) - 1u;
+                        const uint32_t pm = __shfl_sync(0xffffffffu, cm, c) & alive;
+                        if (pm == 0) continue;
+                        const uint32_t cluster = first + c;
+                        const uint32_t t0i = cluster * sg.cluster;
+                        const uint32_t t1i = (t0i + sg.cluster < sg.tri_count) ? t0i + sg.cluster : sg.tri_count;
+                        const uint32_t K = t1i - t0i;
+                        for (uint32_t j = lane; j < 3u * K; j += 32) S.tri[j] = __ldg(sg.tris + 3ull * t0i + j);
+                        __syncwarp();
+                        const uint32_t np_ = __popc(pm);
+                        const uint32_t pairs = np_ * P * K;
+                        for (uint32_t qq = lane; qq < pairs; qq += 32) {
+                            const uint32_t ir = qq / K, j = qq - ir * K;
+                            // ir-th ray among the packets of pm
+                            uint32_t pmm = pm;
+                            for (uint32_t s2 = 0; s2 < ir / P; ++s2) pmm &= pmm - 1u;
+                            const uint32_t pk = __ffs(pmm) - 1u;
+                            const uint32_t i = pk * P + (ir % P);
+                            const uint32_t meta = S.meta[i];
+                            if (!(meta & 64u)) continue;
+                            if (any && (*(volatile uint32_t*)&S.meta[i] & 128u)) continue;
+                            RayWT w;
+                            const float4 o = S.ro[i], sh = S.rs[i];
+                            w.ox = o.x;
+                            w.oy = o.y;
+                            w.oz = o.z;
+                            w.tmin = o.w;
+                            w.sx = sh.x;
+                            w.sy = sh.y;
+                            w.sz = sh.z;
+                            w.tmax = sh.w;
+                            w.kx = meta & 3u;
+                            w.ky = (meta >> 2) & 3u;
+                            w.kz = (meta >> 4) & 3u;
+                            float th;
+                            ++ttests;
+                            if (wt_hit(w, S.tri[3 * j], S.tri[3 * j + 1], S.tri[3 * j + 2], th)) {
+                                if (any) atomicOr(&S.meta[i], 128u);
+                                else atomicMin(&S.best[i], hit_key(th, __float_as_uint(S.tri[3 * j].w)));
+                            }
+                        }
+                        __syncwarp();
+                        // refresh the packets' state: occlusion (any) or shrunken reach (closest)
+                        if (any) {
+                            bool all0 = true, all1 = true;
+                            for (uint32_t jj = 0; jj < P; ++jj) {
+                                const uint32_t m0 = S.meta[(2u * q) * P + jj], m1 = S.meta[(2u * q + 1u) * P + jj];
+                                if ((m0 & 64u) && !(m0 & 128u)) all0 = false;
+                                if ((m1 & 64u) && !(m1 & 128u)) all1 = false;
+                            }
+                            const uint32_t d0 = __ballot_sync(0xffffffffu, all0 && ch == 0);
+                            const uint32_t d1 = __ballot_sync(0xffffffffu, all1 && ch == 0);
+                            uint32_t dead = 0;
+#pragma unroll
+                            for (uint32_t g = 0; g < 4; ++g)
+                                dead |= (((d0 >> (8u * g)) & 1u) << (2u * g)) | (((d1 >> (8u * g)) & 1u) << (2u * g + 1u));
+                            alive &= ~dead;
+                            if (alive == 0) break;
+                        } else {
+                            float r0m = 0.f, r1m = 0.f;
+                            for (uint32_t jj = 0; jj < P; ++jj) {
+                                const uint32_t i0 = (2u * q) * P + jj, i1 = (2u * q + 1u) * P + jj;
+                                if (S.meta[i0] & 64u) {
+                                    const unsigned long long b = S.best[i0];
+                                    const float tb = (b == RSH_HIT_NONE) ? S.rs[i0].w : __uint_as_float((uint32_t)(b >> 32));
+                                    r0m = fmaxf(r0m, S.roc[i0] + tb);
+                                }
+                                if (S.meta[i1] & 64u) {
+                                    const unsigned long long b = S.best[i1];
+                                    const float tb = (b == RSH_HIT_NONE) ? S.rs[i1].w : __uint_as_float((uint32_t)(b >> 32));
+                                    r1m = fmaxf(r1m, S.roc[i1] + tb);
+                                }
+                            }
+                            const float k0 = r0m * (1.0f + 1.0f / 1048576.0f);
+                            const float k1 = r1m * (1.0f + 1.0f / 1048576.0f);
+                            P0.reach = fminf(P0.reach, k0);
+                            P1.reach = fminf(P1.reach, k1);
+                        }
+                    }
+                } else {
+                    if (sp + nlive > F_STACK) {
+                        raise_device_error(a.err, RSH_DEVERR_OVERFLOW);
+                        break;
+                    }
+                    if (live) S.stack[sp + farther] = (cl << 28) | ((first + ch) << 8) | cm;
+                    sp += nlive;
+                    __syncwarp();
+                }
+                if (alive == 0) break;
+            }
+        }
+        __syncwarp();
+        // ---- results (each ray belongs to exactly one unit)
+        for (uint32_t i = lane; i < R; i += 32) {
+            const uint32_t meta = S.meta[i];
+            if (!(meta & 64u)) continue;
+            const uint32_t slot = S.slot[i] - sg.slot_base;
+            if (any) sg.flags[slot] = (meta & 128u) ? RSH_OCCLUDED : 0u;
+            else sg.hits[slot] = S.best[i];
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        ntests += __shfl_xor_sync(0xffffffffu, ntests, d);
+        ttests += __shfl_xor_sync(0xffffffffu, ttests, d);
+    }
+    if (lane == 0) {
+        if (a.node_tests) atomicAdd(a.node_tests, ntests);
+        if (a.tri_tests) atomicAdd(a.tri_tests, ttests);
+    }
+}
+
+template <int P>
+static cudaError_t launch_fused_p(const FusedArgs& a, cudaStream_t s) {
+    const size_t smem = sizeof(FusedSmem<P>) * FW;
+    cudaError_t e = cudaFuncSetAttribute(k_fused<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused<P>, FW * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    uint32_t grid = (uint32_t)(sms * per_sm);
+    const uint32_t need = (a.units_max + FW - 1) / FW;
+    if (need < grid) grid = need > 0 ? need : 1;
+    k_fused<P><<<grid, FW * 32, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused(const FusedArgs& a, cudaStream_t s) {
+    switch (a.packet) {
+        case 8: return launch_fused_p<8>(a, s);
+        case 16: return launch_fused_p<16>(a, s);
+        case 32: return launch_fused_p<32>(a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace rsh

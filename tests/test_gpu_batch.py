@@ -1,0 +1,118 @@
+"""Batched form: fused persistent traversal + intersection, segmented hash/sort over many scenes, CUDA-graph
+replay and the autotuner, all checked against the brute-force oracle through the C ABI."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+import rsh
+from rsh import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8)
+    yield c
+    c.destroy()
+
+
+@pytest.mark.parametrize("P", [8, 16, 32])
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_fused_vs_brute(P, any_hit):
+    c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=P, cluster_size=8)
+    s = scenes.random_soup(40_000, np.random.default_rng(P))
+    sc = c.scene(s.positions, s.normals, s.material_ids, s.materials)
+    rng = np.random.default_rng(100 + P)
+    rays = scenes.surface_rays(s, 70_001, rng)
+    if any_hit:
+        rays["tmax"] = rng.uniform(0.05, 15.0, len(rays)).astype(np.float32)
+    rays["tmax"][::97] = -1.0
+    out = c.trace(sc, rays, any_hit, fused=True)
+    c.check_device_errors()
+    bf = oracle.brute(s.positions, rays, any_hit)
+    assert np.array_equal(out, bf)
+    sc.destroy()
+    c.destroy()
+
+
+def test_fused_cornell_closest_and_ties(ctx, cornell):
+    s = cornell
+    sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+    rays = scenes.surface_rays(s, 50_000, np.random.default_rng(9))
+    out = ctx.trace(sc, rays, False, fused=True)
+    assert np.array_equal(out, oracle.brute(s.positions, rays, False))
+    sc.destroy()
+
+
+def test_batch_segments_many_scenes(ctx):
+    rng = np.random.default_rng(77)
+    sd = [scenes.random_soup(int(t), np.random.default_rng(200 + i)) for i, t in enumerate([12_000, 35_000, 80_000])]
+    scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]
+    sizes = [5_000, 1, 0, 40_000, 4_099, 17_000, 64, 3]
+    which = [0, 1, 2, 2, 1, 0, 2, 1]
+    anyh = [False, True, False, True, False, True, False, True]
+    host_rays, dev = [], []
+    segs = (rsh.BatchSegment * len(sizes))()
+    for i, (n, w, a) in enumerate(zip(sizes, which, anyh)):
+        r = scenes.surface_rays(sd[w], max(n, 1), rng)[:n]
+        if a:
+            r["tmax"] = rng.uniform(0.1, 10.0, n).astype(np.float32)
+        host_rays.append(r)
+        dr = rsh.DeviceArray.from_numpy(r) if n else rsh.DeviceArray(1, rsh.RAY_DTYPE)
+        out = rsh.DeviceArray(max(n, 1), np.uint32 if a else np.uint64)
+        dev.append((dr, out))
+        segs[i].scene = scs[w].handle
+        segs[i].rays = dr.ptr
+        segs[i].n = n
+        segs[i].any_hit = int(a)
+        segs[i].hits = None if a else out.ptr
+        segs[i].flags = out.ptr if a else None
+    rsh.check(rsh.lib().rsh_batch_trace(ctx.handle, segs, len(sizes), None), "batch")
+    ctx.check_device_errors()
+    for i, (n, w, a) in enumerate(zip(sizes, which, anyh)):
+        if n == 0:
+            continue
+        got = dev[i][1].numpy(n)
+        want = oracle.brute(sd[w].positions, host_rays[i], a)
+        assert np.array_equal(got, want), f"segment {i}"
+    # graph capture + replay gives the same results
+    st = C.c_void_p()
+    rsh.check(rsh.lib().rsh_stream_create(C.byref(st)), "stream")
+    g = C.c_void_p()
+    rsh.check(rsh.lib().rsh_batch_graph_create(ctx.handle, segs, len(sizes), st, C.byref(g)), "graph")
+    for i, (n, w, a) in enumerate(zip(sizes, which, anyh)):
+        if n:
+            dev[i][1].fill_bytes(0x5A)
+    rsh.check(rsh.lib().rsh_batch_graph_launch(g, st), "launch")
+    rsh.check(rsh.lib().rsh_stream_synchronize(st), "sync")
+    for i, (n, w, a) in enumerate(zip(sizes, which, anyh)):
+        if n == 0:
+            continue
+        assert np.array_equal(dev[i][1].numpy(n), oracle.brute(sd[w].positions, host_rays[i], a)), f"graph seg {i}"
+    rsh.lib().rsh_batch_graph_destroy(g)
+    rsh.lib().rsh_stream_destroy(st)
+    for sc in scs:
+        sc.destroy()
+
+
+def test_autotune_picks_a_valid_config(ctx):
+    s = scenes.random_soup(20_000, np.random.default_rng(5))
+    sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+    rays = scenes.surface_rays(s, 30_000, np.random.default_rng(6))
+    dr = rsh.DeviceArray.from_numpy(rays)
+    out = rsh.DeviceArray(len(rays), np.uint64)
+    segs = (rsh.BatchSegment * 1)()
+    segs[0].scene, segs[0].rays, segs[0].n, segs[0].any_hit, segs[0].hits = sc.handle, dr.ptr, len(rays), 0, out.ptr
+    gb = (C.c_uint32 * 2)(4, 6)
+    db = (C.c_uint32 * 2)(3, 5)
+    ps = (C.c_uint32 * 2)(8, 16)
+    best = rsh.Config()
+    rsh.check(rsh.lib().rsh_autotune(ctx.handle, segs, 1, gb, 2, db, 2, ps, 2, None, C.byref(best)), "autotune")
+    assert best.grid_bits in (4, 6) and best.dir_log2 in (3, 5) and best.packet_size in (8, 16)
+    rsh.check(rsh.lib().rsh_batch_trace(ctx.handle, segs, 1, None), "batch")
+    assert np.array_equal(out.numpy(), oracle.brute(s.positions, rays, False))
+    ctx.set_config(grid_bits=5, dir_log2=4, packet_size=8)
+    sc.destroy()

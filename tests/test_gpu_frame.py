@@ -1,0 +1,88 @@
+"""The per-frame path (rsh_render_frame) checked stage by stage against the oracle: every intermediate
+buffer of the frame is recomputed on the CPU from the GPU's previous stage and must match bit for bit;
+every hit record / shadow flag must equal the brute-force oracle."""
+import numpy as np
+import pytest
+
+import oracle
+import rsh
+from rsh import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_frame(ctx, s, sc, W, H, depth, jitter):
+    lights = s.lights
+    L = len(lights)
+    cam = rsh.camera_look_at(s.eye, s.target, s.up, s.fov, W, H)
+    ctx.set_camera(cam)
+    ctx.set_lights(lights)
+    rgba = rsh.DeviceArray(W * H, np.uint32)
+    ctx.render(sc, W, H, depth, rgba)
+    ctx.check_device_errors()
+    st = ctx.stats()
+    npix = W * H
+    lo, hi = sc.bounds()
+    g, b = ctx.config.grid_bits, ctx.config.dir_log2
+    scale = oracle.hash_scale(lo, hi, g)
+    # primary
+    prays, pix = oracle.raygen_primary(cam.as_array(), W, H)
+    assert ctx.frame_rays(-1, False, len(prays)).tobytes() == prays.tobytes()
+    bf = oracle.brute(s.positions, prays, False)
+    ph = ctx.frame_hits(-1, npix)
+    want = np.zeros(npix, np.uint64)
+    want[pix[pix != 0xFFFFFFFF]] = bf[pix != 0xFFFFFFFF]
+    assert np.array_equal(ph, want)
+    spos, snrm = ctx.frame_surface(-1, npix)
+    ospos, osnrm = oracle.resolve(s.positions, s.normals, s.material_ids, prays, bf, pix, npix)
+    assert spos.tobytes() == ospos.tobytes() and snrm.tobytes() == osnrm.tobytes()
+    prev = None
+    lp = np.array([l["position"] for l in lights], np.float32)
+    nshadow = nrefl = 0
+    for bnc in range(depth):
+        srays = ctx.frame_rays(bnc, True, npix * L)
+        orays, okeys = oracle.raygen_shadow(spos, snrm, W, H, lp, ctx.config.epsilon, lo, scale, g, b)
+        v = okeys != oracle.KEY_NONE
+        nshadow += int(v.sum())
+        assert srays[v].tobytes() == orays[v].tobytes()
+        sflags = ctx.frame_shadow(bnc, npix * L)
+        assert np.array_equal(sflags[v], oracle.brute(s.positions, orays[v], True))
+        assert np.all(sflags[~v] == 0)
+        rrays = ctx.frame_rays(bnc, False, npix)
+        o_r, o_k = oracle.raygen_reflect(spos, snrm, prev, cam.as_array()[:3] if prev is None else None, W, H,
+                                         ctx.config.epsilon, jitter, ctx.config.seed, bnc, lo, scale, g, b)
+        v = o_k != oracle.KEY_NONE
+        nrefl += int(v.sum())
+        assert rrays[v].tobytes() == o_r[v].tobytes()
+        rh = ctx.frame_hits(bnc, npix)
+        bfr = oracle.brute(s.positions, o_r[v], False)
+        assert np.array_equal(rh[v], bfr)
+        assert np.all(rh[~v] == oracle.HIT_NONE)
+        spos2, snrm2 = ctx.frame_surface(bnc, npix)
+        o2p, o2n = oracle.resolve(s.positions, s.normals, s.material_ids, rrays, rh, None, npix)
+        assert spos2.tobytes() == o2p.tobytes() and snrm2.tobytes() == o2n.tobytes()
+        spos, snrm, prev = spos2, snrm2, rrays
+    assert st["shadow_rays"] == nshadow and st["reflection_rays"] == nrefl
+    img = rgba.numpy()
+    assert np.any(img & 0xFFFFFF)  # something was lit
+    return st
+
+
+@pytest.mark.parametrize("jitter", [0.0, 1.0])
+def test_frame_cornell(cornell, jitter):
+    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, reflect_jitter=jitter)
+    sc = ctx.scene(cornell.positions, cornell.normals, cornell.material_ids, cornell.materials)
+    st = _check_frame(ctx, cornell, sc, 128, 96, 2, jitter)
+    assert st["secondary_ms"] > 0
+    sc.destroy()
+    ctx.destroy()
+
+
+def test_frame_soup_small():
+    s = scenes.soup(n_spheres=300, width=96, height=64, extent=20.0)
+    s.lights = s.lights[:2]
+    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=16, cluster_size=8)
+    sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+    _check_frame(ctx, s, sc, 96, 64, 3, 0.0)
+    sc.destroy()
+    ctx.destroy()

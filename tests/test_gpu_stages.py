@@ -53,7 +53,7 @@ def test_raygen_primary_bitexact(W, H, cornell):
     assert g.tobytes() == o_rays.tobytes()
 
 
-@pytest.mark.parametrize("g,b,tag_bits,tag", [(5, 4, 0, 0), (10, 5, 0, 0), (1, 1, 2, 3), (7, 6, 2, 1)])
+@pytest.mark.parametrize("g,b,tag_bits,tag", [(5, 4, 0, 0), (9, 2, 0, 0), (1, 1, 2, 3), (6, 5, 2, 1), (2, 6, 3, 5)])
 def test_hash_bitexact(g, b, tag_bits, tag):
     rng = np.random.default_rng(11 + g)
     rays = random_rays(rng, 200_000, -3, 3)
