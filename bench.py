@@ -1,0 +1,450 @@
+#!/usr/bin/env python3
+"""Benchmark: secondary-ray Mrays/s of the per-frame ray-space-hierarchy path on the 1M-triangle scene.
+
+Workload (default): the procedural-architecture scene (40x40 tessellated pillars + slabs + arches,
+1,010,240 triangles), 1920x1080, 4 point lights, depth 2 (shadow + cosine-lobe-perturbed reflection per
+bounce), FP32, seeded synthetic input. One step = one frame through rsh_render_frame.
+
+  value       secondary rays traced (after trimming) / GPU time from the first secondary ray generation to
+              the last secondary intersection of each frame (CUDA events on the frame's stream), plain path
+  fused       the same frames with the batched form (one segmented sort + one persistent fused
+              traversal/intersection launch per bounce)
+  e2e         the same metric through the C ABI with host buffers: camera + lights from host structs in,
+              the RGBA8 frame copied to pinned host memory, both inside the timed region
+  roofline    the dominant kernel's achieved rate against its roofline (per-stage CUDA events)
+  cpu_baseline the oracle's C++/OpenMP restatement of the same algorithm on a bounded crop of the frame
+
+`--impl reference` times the CPU restatement alone (the reference ships no CPU path and cannot be built
+here) on the same workload and metric, and prints its own line.
+Multi-GPU: replicas only (each rank renders its own frames; max time over ranks).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path[:0] = [str(ROOT), str(ROOT / "ray-tracer_gb300")]
+
+import numpy as np  # noqa: E402
+
+METRIC = "secondary-ray Mrays/s at 1M tris"
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+# algorithmic work per unit (bytes or FP32 flops), used for every roofline fraction
+ALGO = {
+    "raygen": ("hbm", 64.0),       # bytes / ray slot: surface pos+normal read, ray + key written
+    "compress": ("hbm", None),     # 4N + 12C bytes (computed from counts)
+    "sort": ("hbm", None),         # C * (4 + 16 P) bytes
+    "decompress": ("hbm", None),   # 12C + 4R bytes
+    "build": ("hbm", 32.0),        # bytes / ray
+    "traverse": ("fp32", 24.0),    # flops / packet-node x sphere test
+    "intersect": ("fp32", 46.0),   # flops / ray x triangle test
+}
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "0x1", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def load_peaks() -> dict:
+    if PEAKS_FILE.exists():
+        d = json.loads(PEAKS_FILE.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured", "sm_max_mhz": float(d.get("sm_max_mhz", 2070))}
+    return {"hbm_gbs": 6800.0, "source": "fallback", "sm_max_mhz": 2070.0}
+
+
+# ---------------------------------------------------------------- distributed (replicas)
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as td
+
+        backend = "nccl"
+        try:
+            import torch
+
+            torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        td.init_process_group(backend=backend)
+        return rank, world, td
+    return rank, world, None
+
+
+def reduce_max(td, value: float) -> float:
+    if td is None:
+        return value
+    import torch
+
+    dev = "cuda" if td.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(td, value: float) -> float:
+    if td is None:
+        return value
+    import torch
+
+    dev = "cuda" if td.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    td.all_reduce(t, op=td.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(td):
+    if td is not None:
+        td.barrier()
+
+
+# ---------------------------------------------------------------- workload
+def make_workload(name: str):
+    from rsh import scenes
+
+    return scenes.by_name(name)
+
+
+def cpu_baseline(s, crop=(240, 136), threads=None, steps=1):
+    """The oracle (C++/OpenMP restatement of the same algorithm) on a centred crop of the frame:
+    primary hits, then `depth` bounces of shadow + reflection batches through compress -> sort ->
+    decompress -> build -> traverse+intersect. Times the secondary part only (the GPU metric's window)."""
+    import oracle
+
+    lib = oracle.lib()
+    if threads:
+        lib.orc_set_threads(int(threads))
+    nthreads = oracle.threads()
+    W, H = s.width, s.height
+    cw, chh = crop
+    x0, y0 = (W - cw) // 2, (H - chh) // 2
+    import rsh
+
+    cam = rsh.camera_look_at(s.eye, s.target, s.up, s.fov, W, H).as_array()
+    lo = s.positions[..., :3].reshape(-1, 3).min(0)
+    hi = s.positions[..., :3].reshape(-1, 3).max(0)
+    g, b, P, K = 5, 4, 8, 8
+    t0 = time.perf_counter()
+    oh = oracle.ObjH(s.positions, K, lo, hi)
+    build_s = time.perf_counter() - t0
+    prays, pix = oracle.raygen_primary(cam, W, H)
+    px, py = pix % W, pix // W
+    sel = (pix != 0xFFFFFFFF) & (px >= x0) & (px < x0 + cw) & (py >= y0) & (py < y0 + chh)
+    crays = prays[sel]
+    cpix = ((py[sel] - y0) * cw + (px[sel] - x0)).astype(np.uint32)
+    scale = oracle.hash_scale(lo, hi, g)
+    keys = oracle.hash_rays(crays, lo, scale, g, b)
+    hits, _, _, _ = oh.trace_keyed(crays, keys, 3 * g + 2 * b, P, False)
+    spos0, snrm0 = oracle.resolve(s.positions, s.normals, s.material_ids, crays, hits, cpix, cw * chh)
+    lp = np.array([l["position"] for l in s.lights], np.float32)
+    L = len(lp)
+    lbits = max(0, int(np.ceil(np.log2(L)))) if L > 1 else 0
+    results = []
+    for _ in range(steps):
+        spos, snrm, prev = spos0, snrm0, None
+        rays_total = 0
+        t_sec = 0.0
+        for bnc in range(s.depth):
+            t1 = time.perf_counter()
+            srays, skeys = oracle.raygen_shadow(spos, snrm, cw, chh, lp, 0.01, lo, scale, g, b)
+            flags, R1, _, _ = oh.trace_keyed(srays, skeys, lbits + 3 * g + 2 * b, P, True)
+            rrays, rkeys = oracle.raygen_reflect(spos, snrm, prev, cam[:3] if prev is None else None, cw, chh, 0.01,
+                                                 s.jitter, s.seed, bnc, lo, scale, g, b)
+            rh, R2, _, _ = oh.trace_keyed(rrays, rkeys, 3 * g + 2 * b, P, False)
+            spos, snrm = oracle.resolve(s.positions, s.normals, s.material_ids, rrays, rh, None, cw * chh)
+            t_sec += time.perf_counter() - t1
+            rays_total += R1 + R2
+            prev = rrays
+        results.append((rays_total, t_sec))
+    return {"results": results, "threads": nthreads, "crop": crop, "objh_build_s": build_s}
+
+
+def gpu_arm(args, s, rank, world, td):
+    import ctypes as C
+
+    import rsh
+
+    lib = rsh.load()
+    if lib.rsh_device_count() < 1:
+        raise RuntimeError("bench needs a CUDA device")
+    peaks = load_peaks()
+    W, H, depth = s.width, s.height, s.depth
+    npix = W * H
+    cfg = rsh.default_config(reflect_jitter=float(s.jitter), seed=s.seed)
+    ctx = rsh.Context(cfg)
+    t0 = time.perf_counter()
+    sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+    upload_s = time.perf_counter() - t0
+    cam = rsh.camera_look_at(s.eye, s.target, s.up, s.fov, W, H)
+    ctx.set_camera(cam)
+    ctx.set_lights(s.lights)
+    stream = C.c_void_p()
+    rsh.check(lib.rsh_stream_create(C.byref(stream)), "stream")
+    st = stream.value
+    rgba = rsh.DeviceArray(npix, np.uint32)
+    host_img = C.c_void_p()
+    rsh.check(lib.rsh_malloc_host(C.byref(host_img), npix * 4), "pinned")
+    ev0, ev1 = C.c_void_p(), C.c_void_p()
+    lib.rsh_event_create(C.byref(ev0))
+    lib.rsh_event_create(C.byref(ev1))
+    L0 = lib.rsh_kernel_launches()
+
+    def frame(flags):
+        cfg.flags = flags
+        lib.rsh_set_config(ctx.handle, C.byref(cfg))
+        rsh.check(lib.rsh_render_frame(ctx.handle, sc.handle, W, H, depth, rgba.ptr, st), "render")
+
+    def timed(flags, k, e2e=False):
+        stats = []
+        lights_arr = rsh.make_lights(s.lights)
+        barrier(td)
+        lib.rsh_stream_synchronize(st)
+        lib.rsh_event_record(ev0, st)
+        for _ in range(k):
+            if e2e:  # host inputs -> device (camera, lights), frame, result -> pinned host
+                lib.rsh_camera_set(ctx.handle, C.byref(cam))
+                lib.rsh_lights_set(ctx.handle, lights_arr, len(s.lights))
+            frame(flags)
+            if e2e:
+                rsh.check(lib.rsh_memcpy_d2h(host_img, rgba.ptr, npix * 4, st), "d2h")
+            fs = rsh.FrameStats()
+            rsh.check(lib.rsh_frame_stats_get(ctx.handle, C.byref(fs)), "stats")
+            stats.append(fs.as_dict())
+        lib.rsh_event_record(ev1, st)
+        lib.rsh_stream_synchronize(st)
+        ms = C.c_float()
+        lib.rsh_event_elapsed(ev0, ev1, C.byref(ms))
+        barrier(td)
+        return ms.value, stats
+
+    # warm-up (also sizes every buffer)
+    for _ in range(args.warmup):
+        frame(0)
+    lib.rsh_stream_synchronize(st)
+    clocks = ClockSampler()
+    clocks.start()
+    launches_before = lib.rsh_kernel_launches()
+    wall_ms, stats = timed(0, args.steps)
+    launches = lib.rsh_kernel_launches() - launches_before
+    clk = clocks.stop()
+    sec_rays = sum(x["shadow_rays"] + x["reflection_rays"] for x in stats)
+    sec_ms = sum(x["secondary_ms"] for x in stats)
+    sec_ms_max = reduce_max(td, sec_ms)
+    total_rays = reduce_sum(td, sec_rays)
+    value = total_rays / (sec_ms_max * 1e3) if sec_ms_max > 0 else 0.0
+    ms_per_step = reduce_max(td, wall_ms) / args.steps
+
+    # fused (batched) form on the same frames
+    for _ in range(max(1, args.warmup // 2)):
+        frame(2)
+    f_ms, f_stats = timed(2, args.steps)
+    f_rays = sum(x["shadow_rays"] + x["reflection_rays"] for x in f_stats)
+    f_sec = sum(x["secondary_ms"] for x in f_stats)
+    fused_value = reduce_sum(td, f_rays) / (reduce_max(td, f_sec) * 1e3) if f_sec > 0 else 0.0
+
+    # e2e through the C ABI with host buffers
+    e_ms, e_stats = timed(0, args.steps, e2e=True)
+    e_rays = sum(x["shadow_rays"] + x["reflection_rays"] for x in e_stats)
+    e2e_value = reduce_sum(td, e_rays) / (reduce_max(td, e_ms) * 1e3)
+
+    # per-stage timers (separate frames: events between stages)
+    t_ms, t_stats = timed(1, max(1, min(args.steps, 3)))
+    stage_names = ["primary", "raygen", "compress", "sort", "decompress", "build", "traverse", "intersect", "shade"]
+    nst = len(t_stats)
+    stage_ms = {nm: sum(x["stage_ms"][i] for x in t_stats) / nst for i, nm in enumerate(stage_names)}
+    last = t_stats[-1]
+    chunks = last["chunks"]
+    R = last["shadow_rays"] + last["reflection_rays"]
+    slots = npix * (len(s.lights) + 1) * depth
+    key_bits = 3 * cfg.grid_bits + 2 * cfg.dir_log2 + 2
+    passes = (key_bits + 7) // 8
+    bytes_stage = {
+        "raygen": 64.0 * slots,
+        "compress": 4.0 * slots + 12.0 * chunks + 4.0 * R,
+        "sort": chunks * (4.0 + 16.0 * passes),
+        "decompress": 12.0 * chunks + 4.0 * R,
+        "build": 32.0 * R,
+    }
+    flops_stage = {"traverse": 24.0 * last["node_tests"], "intersect": 46.0 * last["tri_tests"]}
+    per_stage = {}
+    for nm in ("raygen", "compress", "sort", "decompress", "build"):
+        ms = stage_ms[nm]
+        gbs = bytes_stage[nm] / (ms * 1e6) if ms > 0 else 0.0
+        per_stage[nm] = {"ms": round(ms, 4), "GB/s": round(gbs, 1), "frac_hbm": round(gbs / peaks["hbm_gbs"], 4)}
+    sm_clock = clk.get("sm_mhz") or peaks["sm_max_mhz"]
+    n_sm = lib.rsh_sm_count()
+    fp32_peak = n_sm * 128 * 2 * sm_clock * 1e6 / 1e12   # TFLOP/s at the observed SM clock
+    for nm in ("traverse", "intersect"):
+        ms = stage_ms[nm]
+        tf = flops_stage[nm] / (ms * 1e9) if ms > 0 else 0.0
+        per_stage[nm] = {"ms": round(ms, 4), "TFLOP/s": round(tf, 3), "frac_fp32": round(tf / fp32_peak, 4)}
+    dom = max(("raygen", "compress", "sort", "decompress", "build", "traverse", "intersect"), key=lambda k: stage_ms[k])
+    if dom in flops_stage:
+        ach = per_stage[dom]["TFLOP/s"]
+        roof = {"bound": "fp32", "kernel": dom, "achieved": ach, "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
+                "frac": round(ach / fp32_peak, 4), "traffic": None,
+                "peak_note": f"FP32 issue: {n_sm} SMs x 128 lanes x 2 flops x {sm_clock:.0f} MHz (no measured FP32 peak)"}
+    else:
+        ach = per_stage[dom]["GB/s"]
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": None,
+                "peak_note": f"{peaks['source']} HBM copy bandwidth"}
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            tr = json.loads(prof.read_text())
+            if dom in tr:
+                roof["traffic"] = tr[dom]
+        except Exception:
+            pass
+    ctx_err = lib.rsh_check_device_errors(ctx.handle, st)
+    out = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": "Mrays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded procedural architecture scene)",
+        "config": {"workload": f"procedural architecture {s.tri_count} tris, {W}x{H}, {len(s.lights)} point lights, "
+                               f"depth {depth}, cosine-lobe reflections",
+                   "triangles": s.tri_count, "width": W, "height": H, "lights": len(s.lights), "depth": depth,
+                   "grid_bits": cfg.grid_bits, "dir_log2": cfg.dir_log2, "packet_size": cfg.packet_size,
+                   "cluster_size": cfg.cluster_size, "l2": "inputs larger than L2 (scene + per-frame rays > 129 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "secondary_rays_per_step": round(sec_rays / args.steps),
+        "secondary_ms_per_step": round(sec_ms / args.steps, 3),
+        "fused": {"value": round(fused_value, 3), "unit": "Mrays/s", "ratio_vs_plain": round(fused_value / value, 3)
+                  if value else None, "ms_per_step": round(f_ms / args.steps, 3),
+                  "secondary_ms_per_step": round(f_sec / args.steps, 3)},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 48 + 32 * len(s.lights),
+                "d2h_bytes_per_step": npix * 4, "ms_per_step": round(e_ms / args.steps, 3)},
+        "roofline": roof,
+        "stages": per_stage,
+        "counters_per_frame": {"chunks": chunks, "candidates": last["candidates"], "node_tests": last["node_tests"],
+                               "tri_tests": last["tri_tests"], "overflow_passes": last["overflow_passes"]},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "scene_upload_s": round(upload_s, 3),
+        "device_errors": int(ctx_err),
+    }
+    lib.rsh_free_host(host_img)
+    sc.destroy()
+    ctx.destroy()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="rsh", choices=["rsh", "reference"])
+    ap.add_argument("--config", default="P", choices=["S", "O", "P"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-crop", default="240x136")
+    args = ap.parse_args()
+    rank, world, td = dist_setup(args.gpus)
+    s = make_workload(args.config)
+    crop = tuple(int(x) for x in args.cpu_crop.split("x"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        cb = cpu_baseline(s, crop=crop, steps=args.warmup + args.steps)
+        res = cb["results"][args.warmup:]
+        rays = sum(r for r, _ in res)
+        secs = sum(t for _, t in res)
+        val = rays / secs / 1e6
+        line = {"impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "Mrays/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / len(res), 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded procedural architecture scene)",
+                "config": {"workload": f"procedural architecture {s.tri_count} tris, {s.width}x{s.height}, "
+                                       f"{len(s.lights)} point lights, depth {s.depth}, cosine-lobe reflections"},
+                "cpu_baseline": {"value": round(val, 4), "unit": "Mrays/s", "cores": cb["threads"], "kind": "port",
+                                 "sample": f"centred {crop[0]}x{crop[1]} crop of the frame per step, all bounces"},
+                "e2e": {"value": round(val, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    out = gpu_arm(args, s, rank, world, td)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            cb = cpu_baseline(s, crop=crop, steps=1)
+            rays, secs = cb["results"][0]
+            out["cpu_baseline"] = {"value": round(rays / secs / 1e6, 4), "unit": "Mrays/s", "cores": cb["threads"],
+                                   "kind": "port", "sample": f"centred {crop[0]}x{crop[1]} crop of the same frame, "
+                                                             f"{rays} secondary rays, {secs:.2f} s"}
+        print(json.dumps(out))
+    if td is not None:
+        td.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -145,6 +145,7 @@ typedef struct rsh_config {
 } rsh_config;
 
 #define RSH_FLAG_STAGE_TIMERS 1u   /* record per-stage CUDA events (TestManager timers) */
+#define RSH_FLAG_FUSED 2u          /* rsh_render_frame traces each bounce through the batched form */
 
 /* Per-frame statistics (TestManager::dump, TestManager.cpp:229-313, as a struct). */
 typedef struct rsh_frame_stats {
@@ -203,6 +204,8 @@ rsh_status rsh_event_record(void* ev, rsh_stream_t stream);
 rsh_status rsh_event_elapsed(void* start, void* stop, float* ms);
 int rsh_device_count(void);
 int rsh_sm_count(void);
+/* Number of this library's kernels launched by this process so far (all contexts). */
+uint64_t rsh_kernel_launches(void);
 
 /* ---------------------------------------------------------------- scene, lights, camera */
 

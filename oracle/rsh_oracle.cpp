@@ -181,6 +181,23 @@ inline uint32_t f2u(float f) {
     return u;
 }
 
+// Per-ray filter against a cluster sphere before its triangle tests (same arithmetic as the GPU).
+inline bool ray_hits_sphere(const Ray& r, const float* s) {
+    const float vx = s[0] - r.o[0], vy = s[1] - r.o[1], vz = s[2] - r.o[2];
+    const float t = (vx * r.d[0] + vy * r.d[1]) + vz * r.d[2];
+    const float wx = vy * r.d[2] - vz * r.d[1];
+    const float wy = vz * r.d[0] - vx * r.d[2];
+    const float wz = vx * r.d[1] - vy * r.d[0];
+    const float perp = std::sqrt((wx * wx + wy * wy) + wz * wz);
+    const float dist = std::sqrt((vx * vx + vy * vy) + vz * vz);
+    const float slack = (dist + s[3]) * 1e-5f;
+    const float rr = s[3] + slack;
+    if (perp > rr) return false;
+    if (t + rr < r.tmin) return false;
+    if (t - rr > r.tmax) return false;
+    return true;
+}
+
 // ------------------------------------------------------------- node test (RayTracer.cu:283-298 + reach)
 inline bool node_hits_sphere(const Node& p, const float* s) {
     const float vx = s[0] - p.c[0], vy = s[1] - p.c[1], vz = s[2] - p.c[2];
@@ -461,6 +478,7 @@ void orc_raygen_shadow(const float* spos, const float* snrm, uint32_t W, uint32_
                 key = ray_hash(r.o, r.d, hp, l);
             }
         }
+        if (key == KEY_NONE) rays[slot] = Ray{{0.f, 0.f, 0.f}, 0.f, {0.f, 0.f, 0.f}, -1.f};
         keys[slot] = key;
     }
 }
@@ -530,6 +548,7 @@ void orc_raygen_reflect(const float* spos, const float* snrm, const float* prev_
                 key = ray_hash(ry.o, ry.d, hp, 0u);
             }
         }
+        if (key == KEY_NONE) rays[slot] = Ray{{0.f, 0.f, 0.f}, 0.f, {0.f, 0.f, 0.f}, -1.f};
         keys[slot] = key;
     }
 }
@@ -778,6 +797,7 @@ void orc_intersect(void* hp, const float* rays_in, const uint32_t* ids, uint32_t
             const uint32_t id = ids ? ids[k] : k;
             const Ray& r = rays[id];
             if (!(r.tmax > r.tmin)) continue;
+            if (!ray_hits_sphere(r, &h.sph[4ull * cluster])) continue;
             const RayWT w = wt_setup(r);
             const uint32_t t0 = cluster * h.cluster, t1 = std::min(t0 + h.cluster, h.T);
             for (uint32_t t = t0; t < t1; ++t) {
@@ -939,6 +959,7 @@ uint32_t orc_trace_keyed(void* hp, const float* rays_in, const uint32_t* keys, u
                 uint64_t best = HIT_NONE;
                 bool occl = false;
                 for (uint32_t c : cl) {
+                    if (!ray_hits_sphere(r, &h.sph[4ull * c])) continue;
                     const uint32_t a0 = c * h.cluster, a1 = std::min(a0 + h.cluster, h.T);
                     for (uint32_t t2i = a0; t2i < a1; ++t2i) {
                         const float* v = &h.tris[12ull * t2i];

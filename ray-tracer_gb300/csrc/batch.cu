@@ -241,6 +241,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s) {
     k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
                                                        pl.tag_shift, static_cast<rsh_ray*>(pl.rays_all),
                                                        static_cast<uint32_t*>(pl.keys));
+    note_launch();
     RSH_CUDA(cudaGetLastError());
     RSH_CUDA(launch_compress(static_cast<uint32_t*>(pl.keys), pl.total, static_cast<uint32_t*>(pl.trimmed),
                              static_cast<uint32_t*>(pl.ckeys), static_cast<uint32_t*>(pl.cbases), cnt, pl.scr,
@@ -257,11 +258,13 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s) {
                                       pl.unit_rays, static_cast<uint32_t*>(pl.seg_begin),
                                       static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart),
                                       static_cast<FusedSeg*>(pl.fsegs), totals);
+    note_launch();
     RSH_CUDA(cudaGetLastError());
     k_batch_pad<<<(pl.max_padded + 255) / 256, 256, 0, s>>>(
         static_cast<uint32_t*>(pl.sorted_ids), static_cast<uint32_t*>(pl.seg_begin),
         static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart), pl.nseg, pl.max_padded, totals,
         static_cast<uint32_t*>(pl.padded));
+    note_launch();
     RSH_CUDA(cudaGetLastError());
     RSH_CUDA(launch_build_rsh(static_cast<rsh_ray*>(pl.rays_all), static_cast<uint32_t*>(pl.padded), pl.max_padded,
                               totals, pl.P, static_cast<rsh_node*>(pl.nodes), s));

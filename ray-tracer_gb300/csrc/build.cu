@@ -196,6 +196,7 @@ cudaError_t launch_build_rsh(const rsh_ray* rays, const uint32_t* sorted_ids, ui
         case 32: k_build_leaves<32><<<grid, 256, 0, s>>>(rays, sorted_ids, max_rays, d_count, nodes); break;
         default: return cudaErrorInvalidValue;
     }
+    note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     for (uint32_t lvl = 1; lvl <= 2; ++lvl) {
@@ -203,6 +204,7 @@ cudaError_t launch_build_rsh(const rsh_ray* rays, const uint32_t* sorted_ids, ui
         if (np == 0) break;
         k_build_level<<<(np + 127) / 128, 128, 0, s>>>(nodes, off[lvl - 1], off[lvl], max_rays, d_count,
                                                        packet, lvl);
+        note_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

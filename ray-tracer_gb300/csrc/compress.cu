@@ -240,6 +240,7 @@ cudaError_t launch_compress(const uint32_t* keys, uint32_t n_slots, uint32_t* tr
     const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
     k_compress<<<tiles, CT_THREADS, 0, s>>>(keys, n_slots, tiles, vec_ok, trimmed_ids, chunk_keys,
                                             chunk_bases, counts, sc, err);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -255,6 +256,7 @@ cudaError_t launch_chunk_sizes(const uint32_t* chunk_bases, const uint32_t* coun
                                uint32_t* chunk_sizes, cudaStream_t s) {
     if (max_chunks == 0) return cudaSuccess;
     k_chunk_sizes<<<(max_chunks + 255) / 256, 256, 0, s>>>(chunk_bases, counts, max_chunks, chunk_sizes);
+    note_launch();
     return cudaGetLastError();
 }
 

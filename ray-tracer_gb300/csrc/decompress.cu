@@ -181,11 +181,13 @@ cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t*
     if (e != cudaSuccess) return e;
     k_dc_scan<<<(unsigned)(tiles - 1 > 0 ? tiles - 1 : 1), DS_THREADS, 0, s>>>(
         sorted_chunk_vals, chunk_bases, counts, max_chunks, off, status, ticket, err);
+    note_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_dc_expand<<<(max_rays + DE_TILE - 1) / DE_TILE, DE_THREADS, 0, s>>>(
         sorted_chunk_keys, sorted_chunk_vals, chunk_bases, trimmed_ids, counts, max_rays, off,
         sorted_keys, sorted_ids);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -17,6 +18,28 @@
 namespace rsh {
 
 static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+void note_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int stage_begin(rsh_ctx* ctx, int stage, cudaStream_t s) {
+    if (!(ctx->cfg.flags & RSH_FLAG_STAGE_TIMERS)) return -1;
+    while (ctx->tev.size() < ctx->tev_used + 2) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) return -1;
+        ctx->tev.push_back(ev);
+    }
+    const uint32_t i = ctx->tev_used;
+    ctx->tev_used += 2;
+    cudaEventRecord(ctx->tev[i], s);
+    ctx->tmarks.push_back({stage, i});
+    return (int)i;
+}
+
+void stage_end(rsh_ctx* ctx, int handle, cudaStream_t s) {
+    if (handle < 0) return;
+    cudaEventRecord(ctx->tev[handle + 1], s);
+}
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -92,7 +115,6 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     RSH_TRY(ensure(ctx, "work", 64, &work));
     uint32_t* w = static_cast<uint32_t*>(work);
     unsigned long long* cc = reinterpret_cast<unsigned long long*>(w + 4);
-    const uint32_t init[4] = {0u, 0xFFFFFFFFu, 0u, 0u};
     TravArgs ta{};
     ta.nodes = nodes;
     hierarchy_capacity(max_rays, P, ta.node_off);
@@ -112,6 +134,7 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ta.node_tests = ctx->d_stats + 0;
     ta.err = ctx->d_err;
     IsectArgs ia{};
+    ia.spheres = sc->h.spheres;
     ia.tris = sc->h.tris;
     ia.tri_count = sc->tri_count;
     ia.cluster = sc->h.cluster;
@@ -126,15 +149,23 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ia.flags = flags;
     ia.hits = hits;
     ia.tri_tests = ctx->d_stats + 1;
-    uint32_t start = 0;
-    for (int pass = 0; pass < 1 << 20; ++pass) {
+    // Passes over a window of work units [start, start + window). Without overflow the first pass covers
+    // every unit. After an overflow the window restarts at the first unfinished unit; if a pass made no
+    // progress the window shrinks (units of one pass race for the buffer), down to a single unit, which
+    // then has the whole buffer to itself.
+    const uint32_t units = (((max_rays + P - 1) / P) + 7) / 8;
+    uint32_t start = 0, window = units;
+    while (start < units) {
+        ta.unit_end = (window >= units - start) ? units : start + window;
         uint32_t iw[4] = {start, 0xFFFFFFFFu, 0u, 0u};
-        (void)init;
         RSH_CUDA(cudaMemcpyAsync(w, iw, sizeof(iw), cudaMemcpyHostToDevice, s));
         RSH_CUDA(cudaMemsetAsync(cc, 0, 8, s));
+        int th = stage_begin(ctx, RSH_STAGE_TRAVERSE, s);
         RSH_CUDA(launch_traverse(ta, s));
+        stage_end(ctx, th, s);
+        th = stage_begin(ctx, RSH_STAGE_INTERSECT, s);
         RSH_CUDA(launch_intersect(ia, any_hit, s));
-        // accumulate the candidate count into the stats
+        stage_end(ctx, th, s);
         RSH_CUDA(cudaMemcpyAsync(ctx->h_pinned, w, 16, cudaMemcpyDeviceToHost, s));
         RSH_CUDA(cudaMemcpyAsync(ctx->h_pinned + 4, cc, 8, cudaMemcpyDeviceToHost, s));
         RSH_CUDA(cudaStreamSynchronize(s));
@@ -142,8 +173,18 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
         unsigned long long got = 0;
         std::memcpy(&got, ctx->h_pinned + 4, 8);
         ctx->stats.candidates += got < cap ? got : cap;
-        if (resume == 0xFFFFFFFFu) break;
+        if (resume == 0xFFFFFFFFu) {
+            start = ta.unit_end;
+            continue;
+        }
         ++ctx->overflow_passes;
+        if (resume == start) {
+            if (window == 1) {
+                set_error("the candidates of one work unit exceed the candidate buffer");
+                return RSH_ERR_OVERFLOW;
+            }
+            window = std::max<uint32_t>(1, window / 4);
+        }
         start = resume;
     }
     return RSH_OK;
@@ -171,16 +212,24 @@ rsh_status trace_keyed(rsh_ctx* ctx, const rsh_scene* sc, const rsh_ray* rays, c
     scr_bytes = std::max(scr_bytes, decompress_scratch_bytes(n_slots));
     RSH_TRY(ensure(ctx, "scratch", scr_bytes, &scr));
     uint32_t* cnt = counts_out ? counts_out : static_cast<uint32_t*>(counts);
+    int th = stage_begin(ctx, RSH_STAGE_COMPRESS, s);
     RSH_CUDA(launch_compress(keys, n_slots, static_cast<uint32_t*>(trimmed), static_cast<uint32_t*>(ckeys),
                              static_cast<uint32_t*>(cbases), cnt, scr, ctx->d_err, s));
+    stage_end(ctx, th, s);
+    th = stage_begin(ctx, RSH_STAGE_SORT, s);
     RSH_CUDA(launch_sort_pairs(static_cast<uint32_t*>(ckeys), nullptr, static_cast<uint32_t*>(skeys),
                                static_cast<uint32_t*>(svals), n_slots, cnt + 1, key_bits, scr, ctx->d_err, s));
+    stage_end(ctx, th, s);
+    th = stage_begin(ctx, RSH_STAGE_DECOMPRESS, s);
     RSH_CUDA(launch_decompress(static_cast<uint32_t*>(skeys), static_cast<uint32_t*>(svals),
                                static_cast<uint32_t*>(cbases), static_cast<uint32_t*>(trimmed), cnt,
                                n_slots, static_cast<uint32_t*>(sorted_keys),
                                static_cast<uint32_t*>(sorted_ids), scr, ctx->d_err, s));
+    stage_end(ctx, th, s);
+    th = stage_begin(ctx, RSH_STAGE_BUILD, s);
     RSH_CUDA(launch_build_rsh(rays, static_cast<uint32_t*>(sorted_ids), n_slots, cnt, P,
                               static_cast<rsh_node*>(nodes), s));
+    stage_end(ctx, th, s);
     return traverse_and_intersect(ctx, sc, static_cast<rsh_node*>(nodes), rays,
                                   static_cast<uint32_t*>(sorted_ids), n_slots, cnt, any_hit, flags, hits, s);
 }
@@ -402,6 +451,8 @@ int rsh_device_count(void) {
     }
     return n;
 }
+uint64_t rsh_kernel_launches(void) { return g_launches.load(); }
+
 int rsh_sm_count(void) {
     int dev = 0, n = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -771,6 +822,7 @@ rsh_status rsh_traverse(rsh_ctx* ctx, const rsh_scene* sc, const rsh_node* nodes
     ta.capacity = capacity;
     ta.cand_count = reinterpret_cast<unsigned long long*>(d_cand_count);
     ta.work = w;
+    ta.unit_end = 0xFFFFFFFFu;
     ta.node_tests = ctx->d_stats;
     ta.err = ctx->d_err;
     RSH_CUDA(launch_traverse(ta, stream));
@@ -792,6 +844,7 @@ static rsh_status isect_stage(const rsh_scene* sc, const rsh_ray* rays, const ui
     if (packet_size != 8 && packet_size != 16 && packet_size != 32) return RSH_ERR_INVALID;
     if (sc->tri_count == 0 || max_rays == 0) return RSH_OK;
     IsectArgs ia{};
+    ia.spheres = sc->h.spheres;
     ia.tris = sc->h.tris;
     ia.tri_count = sc->tri_count;
     ia.cluster = sc->h.cluster;
@@ -863,16 +916,17 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     cudaStream_t s = stream;
     const uint32_t L = ctx->light_count;
     const uint32_t npix = W * H;
+    const bool fused = (ctx->cfg.flags & RSH_FLAG_FUSED) != 0;
     ctx->fw = W;
     ctx->fh = H;
     ctx->fdepth = depth;
     ctx->flights = L;
     ctx->last_stream = s;
     ctx->overflow_passes = 0;
+    ctx->tev_used = 0;
+    ctx->tmarks.clear();
     std::memset(&ctx->stats, 0, sizeof(ctx->stats));
     RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
-    const bool timers = (ctx->cfg.flags & RSH_FLAG_STAGE_TIMERS) != 0;
-    (void)timers;
     uint32_t lbits = 0;
     while ((1u << lbits) < L) ++lbits;
     HashP hp_s, hp_r;
@@ -887,9 +941,10 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     RSH_TRY(ensure_buf(ctx, ctx->prim_pix, 4ull * np));
     RSH_TRY(ensure_buf(ctx, ctx->surf0_pos, 16ull * npix));
     RSH_TRY(ensure_buf(ctx, ctx->surf0_nrm, 16ull * npix));
-    void *accum, *keys;
+    void *accum, *keys, *keys2;
     RSH_TRY(ensure(ctx, "accum", 16ull * npix, &accum));
     RSH_TRY(ensure(ctx, "keys", 4ull * npix * (L ? L : 1), &keys));
+    RSH_TRY(ensure(ctx, "keys2", 4ull * npix, &keys2));
     for (uint32_t b = 0; b < depth; ++b) {
         BounceBufs& bb = ctx->bounce[b];
         RSH_TRY(ensure_buf(ctx, bb.shadow_rays, sizeof(rsh_ray) * (size_t)npix * L));
@@ -899,15 +954,26 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
         RSH_TRY(ensure_buf(ctx, bb.surf_pos, 16ull * npix));
         RSH_TRY(ensure_buf(ctx, bb.surf_nrm, 16ull * npix));
     }
+    void* cnt_acc;
+    RSH_TRY(ensure(ctx, "frame_counts", 8ull * 2 * (depth + 1), &cnt_acc));
+    uint32_t* fc = static_cast<uint32_t*>(cnt_acc);
+    RSH_CUDA(cudaMemsetAsync(fc, 0, 8ull * 2 * (depth + 1), s));
     RSH_CUDA(cudaEventRecord(ctx->ev[0], s));
+    int th = stage_begin(ctx, RSH_STAGE_PRIMARY, s);
     rsh_ray* prays = static_cast<rsh_ray*>(ctx->prim_rays.ptr);
     unsigned long long* phits = static_cast<unsigned long long*>(ctx->prim_hits.ptr);
     uint32_t* ppix = static_cast<uint32_t*>(ctx->prim_pix.ptr);
     RSH_CUDA(launch_raygen_primary(to_camp(ctx->cam), W, H, prays, ppix, s));
-    RSH_CUDA(launch_fill_u64(phits, RSH_HIT_NONE, np, s));
-    RSH_TRY(trace_ordered(ctx, sc, prays, np, false, nullptr, phits, s));
+    if (fused) {
+        rsh_batch_segment seg{sc, prays, np, 0, reinterpret_cast<uint64_t*>(phits), nullptr};
+        RSH_TRY(rsh_batch_trace(ctx, &seg, 1, s));
+    } else {
+        RSH_CUDA(launch_fill_u64(phits, RSH_HIT_NONE, np, s));
+        RSH_TRY(trace_ordered(ctx, sc, prays, np, false, nullptr, phits, s));
+    }
     RSH_CUDA(launch_resolve(sc->pos, sc->nrm, sc->mat, prays, phits, ppix, np,
                             static_cast<float4*>(ctx->surf0_pos.ptr), static_cast<float4*>(ctx->surf0_nrm.ptr), s));
+    stage_end(ctx, th, s);
     RSH_CUDA(cudaEventRecord(ctx->ev[1], s));  // secondary window starts
 
     const float4* spos = static_cast<const float4*>(ctx->surf0_pos.ptr);
@@ -917,10 +983,6 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     lp.count = L;
     for (uint32_t l = 0; l < L; ++l)
         for (int i = 0; i < 3; ++i) lp.pos[l][i] = ctx->lights[l].position[i];
-    void* cnt_acc;
-    RSH_TRY(ensure(ctx, "frame_counts", 8ull * 2 * (depth + 1), &cnt_acc));
-    uint32_t* fc = static_cast<uint32_t*>(cnt_acc);
-    RSH_CUDA(cudaMemsetAsync(fc, 0, 8ull * 2 * (depth + 1), s));
     ShadeArgs sa{};
     sa.materials = sc->materials;
     sa.material_count = sc->material_count;
@@ -936,20 +998,47 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
         uint32_t* sflags = static_cast<uint32_t*>(bb.shadow_flags.ptr);
         rsh_ray* rrays = static_cast<rsh_ray*>(bb.refl_rays.ptr);
         unsigned long long* rhits = static_cast<unsigned long long*>(bb.refl_hits.ptr);
-        // shadow batch
-        RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays,
-                                      static_cast<uint32_t*>(keys), s));
-        RSH_CUDA(cudaMemsetAsync(sflags, 0, 4ull * npix * L, s));
-        RSH_TRY(trace_keyed(ctx, sc, srays, static_cast<uint32_t*>(keys), npix * L, hp_s.key_bits, true, sflags,
-                            nullptr, fc + 4 * b, s));
-        // reflection batch
-        RSH_CUDA(launch_raygen_reflect(spos, snrm, incident, ctx->cam.eye, W, H, ctx->cfg.epsilon,
-                                       ctx->cfg.reflect_jitter, ctx->cfg.seed, b, hp_r, rrays,
-                                       static_cast<uint32_t*>(keys), s));
-        RSH_CUDA(launch_fill_u64(rhits, RSH_HIT_NONE, npix, s));
-        RSH_TRY(trace_keyed(ctx, sc, rrays, static_cast<uint32_t*>(keys), npix, hp_r.key_bits, false, nullptr,
-                            rhits, fc + 4 * b + 2, s));
+        if (fused) {
+            // both batches of the bounce in one batched call: 2 segments, one persistent launch
+            th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);
+            RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays,
+                                          static_cast<uint32_t*>(keys), s));
+            RSH_CUDA(launch_raygen_reflect(spos, snrm, incident, ctx->cam.eye, W, H, ctx->cfg.epsilon,
+                                           ctx->cfg.reflect_jitter, ctx->cfg.seed, b, hp_r, rrays,
+                                           static_cast<uint32_t*>(keys2), s));
+            stage_end(ctx, th, s);
+            rsh_batch_segment segs[2] = {
+                {sc, srays, npix * L, 1, nullptr, sflags},
+                {sc, rrays, npix, 0, reinterpret_cast<uint64_t*>(rhits), nullptr}};
+            th = stage_begin(ctx, RSH_STAGE_TRAVERSE, s);
+            RSH_TRY(rsh_batch_trace(ctx, segs, 2, s));
+            stage_end(ctx, th, s);
+            const uint32_t* seg_cnt = static_cast<const uint32_t*>(ctx->bufs["b_seg_cnt"].ptr);
+            const uint32_t* bcnt = static_cast<const uint32_t*>(ctx->bufs["b_counts"].ptr);
+            RSH_CUDA(cudaMemcpyAsync(fc + 4 * b, seg_cnt, 4, cudaMemcpyDeviceToDevice, s));
+            RSH_CUDA(cudaMemcpyAsync(fc + 4 * b + 2, seg_cnt + 1, 4, cudaMemcpyDeviceToDevice, s));
+            RSH_CUDA(cudaMemcpyAsync(fc + 4 * b + 1, bcnt + 1, 4, cudaMemcpyDeviceToDevice, s));
+        } else {
+            // shadow batch
+            th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);
+            RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays,
+                                          static_cast<uint32_t*>(keys), s));
+            RSH_CUDA(cudaMemsetAsync(sflags, 0, 4ull * npix * L, s));
+            stage_end(ctx, th, s);
+            RSH_TRY(trace_keyed(ctx, sc, srays, static_cast<uint32_t*>(keys), npix * L, hp_s.key_bits, true, sflags,
+                                nullptr, fc + 4 * b, s));
+            // reflection batch
+            th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);
+            RSH_CUDA(launch_raygen_reflect(spos, snrm, incident, ctx->cam.eye, W, H, ctx->cfg.epsilon,
+                                           ctx->cfg.reflect_jitter, ctx->cfg.seed, b, hp_r, rrays,
+                                           static_cast<uint32_t*>(keys), s));
+            RSH_CUDA(launch_fill_u64(rhits, RSH_HIT_NONE, npix, s));
+            stage_end(ctx, th, s);
+            RSH_TRY(trace_keyed(ctx, sc, rrays, static_cast<uint32_t*>(keys), npix, hp_r.key_bits, false, nullptr,
+                                rhits, fc + 4 * b + 2, s));
+        }
         // shade this bounce's surface, then resolve the reflection hits into the next surface
+        th = stage_begin(ctx, RSH_STAGE_SHADE, s);
         if (rgba_out) {
             sa.spos = spos;
             sa.snrm = snrm;
@@ -960,23 +1049,22 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
         }
         RSH_CUDA(launch_resolve(sc->pos, sc->nrm, sc->mat, rrays, rhits, nullptr, npix,
                                 static_cast<float4*>(bb.surf_pos.ptr), static_cast<float4*>(bb.surf_nrm.ptr), s));
+        stage_end(ctx, th, s);
         spos = static_cast<const float4*>(bb.surf_pos.ptr);
         snrm = static_cast<const float4*>(bb.surf_nrm.ptr);
         incident = rrays;
     }
     RSH_CUDA(cudaEventRecord(ctx->ev[2], s));  // secondary window ends
     if (rgba_out) {
+        th = stage_begin(ctx, RSH_STAGE_SHADE, s);
         sa.spos = spos;
         sa.snrm = snrm;
         sa.shadow = nullptr;
         sa.bounce = depth;
         sa.incident = incident;
-        if (depth == 0) {
-            sa.bounce = 0;
-            sa.lights = L;
-        }
         RSH_CUDA(launch_shade(sa, s));
         RSH_CUDA(launch_pack_rgba(static_cast<float4*>(accum), npix, rgba_out, s));
+        stage_end(ctx, th, s);
     }
     RSH_CUDA(cudaEventRecord(ctx->ev[3], s));
     // counters (async; read by rsh_frame_stats_get)
@@ -1003,7 +1091,13 @@ rsh_status rsh_frame_stats_get(rsh_ctx* ctx, rsh_frame_stats* out) {
     st.tri_tests = d[1];
     cudaEventElapsedTime(&st.secondary_ms, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&st.frame_ms, ctx->ev[0], ctx->ev[3]);
-    cudaEventElapsedTime(&st.stage_ms[RSH_STAGE_PRIMARY], ctx->ev[0], ctx->ev[1]);
+    for (float& v : st.stage_ms) v = 0.0f;
+    for (const auto& m : ctx->tmarks) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ctx->tev[m.second], ctx->tev[m.second + 1]) == cudaSuccess && m.first < 12)
+            st.stage_ms[m.first] += ms;
+    }
+    cudaGetLastError();
     st.overflow_passes = ctx->overflow_passes;
     *out = st;
     return RSH_OK;

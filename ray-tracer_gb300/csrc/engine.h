@@ -75,11 +75,18 @@ struct rsh_ctx {
     cudaStream_t last_stream = nullptr;
     std::vector<uint32_t> batch_counts_host;
     uint32_t overflow_passes = 0;
+    // per-stage CUDA events (RSH_FLAG_STAGE_TIMERS): pool and the (stage, start event) pairs of a frame
+    std::vector<cudaEvent_t> tev;
+    std::vector<std::pair<int, uint32_t>> tmarks;
+    uint32_t tev_used = 0;
 };
 
 namespace rsh {
 
 rsh_status ensure(rsh_ctx* ctx, const char* name, size_t bytes, void** out);
+// Stage timers: begin returns a handle (or -1 when timers are off); end records the closing event.
+int stage_begin(rsh_ctx* ctx, int stage, cudaStream_t s);
+void stage_end(rsh_ctx* ctx, int handle, cudaStream_t s);
 rsh_status ensure_buf(rsh_ctx* ctx, DevBuf& b, size_t bytes);
 void release_buf(rsh_ctx* ctx, DevBuf& b);
 rsh_status make_hash_params(const rsh_scene* sc, const rsh_config& cfg, uint32_t tag_bits, HashP& out);

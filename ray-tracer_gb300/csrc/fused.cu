@@ -30,13 +30,14 @@ template <int P>
 struct FusedSmem {
     float4 ro[8 * P];             // origin xyz, tmin
     float4 rs[8 * P];             // shear sx, sy, sz, tmax (original)
+    float4 rd[8 * P];             // direction (for the per-ray cluster-sphere filter)
+    uint16_t list[8 * P];         // rays of the current cluster that pass the sphere filter
     uint32_t meta[8 * P];         // kx | ky << 2 | kz << 4 | active << 6 | occluded << 7
     uint32_t slot[8 * P];
     float roc[8 * P];             // |o - packet centre|
     unsigned long long best[8 * P];
     float4 tri[F_MAXK * 3];
     uint32_t stack[F_STACK];
-    float cdist[8];
 };
 
 RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
@@ -79,6 +80,7 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
             meta = (uint32_t)w.kx | ((uint32_t)w.ky << 2) | ((uint32_t)w.kz << 4) | (active ? 64u : 0u);
             S.ro[i] = make_float4(o.x, o.y, o.z, o.w);
             S.rs[i] = make_float4(w.sx, w.sy, w.sz, d.w);
+            S.rd[i] = d;
             S.meta[i] = meta;
             S.slot[i] = id;
             S.best[i] = RSH_HIT_NONE;
@@ -91,10 +93,6 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
         const bool v0 = P0.count > 0, v1 = P1.count > 0;
         __syncwarp();
         // |o - packet centre| per ray (for the shrinking reach of closest-hit packets)
-        for (uint32_t i = lane; i < R; i += 32) {
-            const NodeR& Pk = ((i / P) & 1u) ? P1 : P0;  // placeholder; recomputed below
-            (void)Pk;
-        }
         {
             // lane ch of group q computes for packet 2q (rays [2q*P, 2q*P+P)) and 2q+1, spread over 8 lanes
             for (uint32_t j = ch; j < 2u * P; j += 8u) {
@@ -167,17 +165,35 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
                         const uint32_t K = t1i - t0i;
                         for (uint32_t j = lane; j < 3u * K; j += 32) S.tri[j] = __ldg(sg.tris + 3ull * t0i + j);
                         __syncwarp();
-                        const uint32_t np_ = __popc(pm);
-                        const uint32_t pairs = np_ * P * K;
+                        // per-ray filter against the cluster sphere, compacted into S.list
+                        const float4 csph = make_float4(__shfl_sync(0xffffffffu, Sph.x, c), __shfl_sync(0xffffffffu, Sph.y, c),
+                                                        __shfl_sync(0xffffffffu, Sph.z, c), __shfl_sync(0xffffffffu, Sph.w, c));
+                        const uint32_t nr = __popc(pm) * P;
+                        uint32_t nlist = 0;
+                        for (uint32_t base = 0; base < nr; base += 32) {
+                            const uint32_t ir = base + lane;
+                            bool pass = false;
+                            uint32_t i = 0;
+                            if (ir < nr) {
+                                uint32_t pmm = pm;
+                                for (uint32_t s2 = 0; s2 < ir / P; ++s2) pmm &= pmm - 1u;
+                                i = (__ffs(pmm) - 1u) * P + (ir % P);
+                                const uint32_t mt = S.meta[i];
+                                if ((mt & 64u) && !(any && (mt & 128u))) {
+                                    const float4 o = S.ro[i], dd = S.rd[i];
+                                    pass = ray_hits_sphere(o.x, o.y, o.z, dd.x, dd.y, dd.z, o.w, dd.w, csph);
+                                }
+                            }
+                            const uint32_t bl = __ballot_sync(0xffffffffu, pass);
+                            if (pass) S.list[nlist + __popc(bl & lanemask_lt())] = (uint16_t)i;
+                            nlist += __popc(bl);
+                        }
+                        __syncwarp();
+                        const uint32_t pairs = nlist * K;
                         for (uint32_t qq = lane; qq < pairs; qq += 32) {
                             const uint32_t ir = qq / K, j = qq - ir * K;
-                            // ir-th ray among the packets of pm
-                            uint32_t pmm = pm;
-                            for (uint32_t s2 = 0; s2 < ir / P; ++s2) pmm &= pmm - 1u;
-                            const uint32_t pk = __ffs(pmm) - 1u;
-                            const uint32_t i = pk * P + (ir % P);
+                            const uint32_t i = S.list[ir];
                             const uint32_t meta = S.meta[i];
-                            if (!(meta & 64u)) continue;
                             if (any && (*(volatile uint32_t*)&S.meta[i] & 128u)) continue;
                             RayWT w;
                             const float4 o = S.ro[i], sh = S.rs[i];
@@ -285,6 +301,7 @@ static cudaError_t launch_fused_p(const FusedArgs& a, cudaStream_t s) {
     const uint32_t need = (a.units_max + FW - 1) / FW;
     if (need < grid) grid = need > 0 ? need : 1;
     k_fused<P><<<grid, FW * 32, smem, s>>>(a);
+    note_launch();
     return cudaGetLastError();
 }
 

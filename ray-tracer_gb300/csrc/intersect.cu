@@ -5,8 +5,8 @@
 // eps < t < |o - p| - 2 eps -> flag = UINT_MAX) and CalculateReflectionRayIntersections (:1711-1774:
 // atomicMin of ((uint)(t*10 + 1) << 20) + triID, i.e. t quantised to 0.1 in 12 bits).
 //
-// Here: P threads per candidate (one per ray of the packet), each testing its ray against the
-// cluster's triangles with the watertight test. Any-hit stores RSH_OCCLUDED and stops (and skips rays
+// Here: P threads per candidate (one per ray of the packet); a ray first tests the cluster's bounding
+// sphere, then the cluster's triangles with the watertight test. Any-hit stores RSH_OCCLUDED and stops (and skips rays
 // already known occluded); closest-hit keeps its best (float bits of t << 32 | original triangle id)
 // and issues one 64-bit atomicMin. A persistent grid-stride loop reads the candidate count on the
 // device, so no host readback sits between traversal and intersection.
@@ -37,6 +37,7 @@ __global__ void __launch_bounds__(256) k_intersect(IsectArgs a) {
         load_ray(a.rays, id, o, d);
         if (!(d.w > o.w)) continue;
         if (ANY && *(volatile uint32_t*)(a.flags + id) == RSH_OCCLUDED) continue;
+        if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, __ldg(a.spheres + cluster))) continue;
         const RayWT r = wt_setup(o, d);
         const uint32_t t0 = cluster * a.cluster;
         const uint32_t t1 = (t0 + a.cluster < a.tri_count) ? t0 + a.cluster : a.tri_count;
@@ -72,6 +73,7 @@ cudaError_t launch_intersect(const IsectArgs& a, bool any_hit, cudaStream_t s) {
     const uint32_t grid = (uint32_t)sms * 8u;
     if (any_hit) k_intersect<true><<<grid, 256, 0, s>>>(a);
     else k_intersect<false><<<grid, 256, 0, s>>>(a);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -14,6 +14,9 @@
 
 namespace rsh {
 
+// Counts this library's kernel launches (rsh_kernel_launches).
+void note_launch(unsigned n = 1);
+
 struct HashP {
     float lo[3];
     float scale[3];
@@ -117,6 +120,7 @@ struct TravArgs {
     unsigned long long capacity;
     unsigned long long* cand_count;
     uint32_t* work;              // [0] = next unit, [1] = resume unit (min failed)
+    uint32_t unit_end;           // units >= unit_end are left for a later pass
     unsigned long long* node_tests;
     uint32_t* err;
 };
@@ -124,6 +128,7 @@ cudaError_t launch_traverse(const TravArgs& a, cudaStream_t s);
 
 // ---- intersection (intersect.cu)
 struct IsectArgs {
+    const float4* spheres;       // cluster spheres (object-hierarchy level 0)
     const float4* tris;
     uint32_t tri_count;
     uint32_t cluster;

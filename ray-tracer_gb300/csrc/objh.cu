@@ -148,6 +148,7 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     vsc.y = (hi[1] > lo[1]) ? 1024.0f / (hi[1] - lo[1]) : 0.0f;
     vsc.z = (hi[2] > lo[2]) ? 1024.0f / (hi[2] - lo[2]) : 0.0f;
     k_morton<<<(n + 255) / 256, 256, 0, s>>>(positions_dev, n, vlo, vsc, codes);
+    note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     uint32_t* perm_tmp = nullptr;
     if ((e = cudaMalloc(&perm_tmp, sizeof(uint32_t) * n)) != cudaSuccess) return e;
@@ -157,14 +158,17 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
         return e;
     }
     k_gather_tris<<<(n + 255) / 256, 256, 0, s>>>(positions_dev, perm_tmp, n, h.tris, perm);
+    note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) {
         cudaFree(perm_tmp);
         return e;
     }
     k_leaf_spheres<<<(sizes[0] + 127) / 128, 128, 0, s>>>(h.tris, n, cluster, sizes[0], h.spheres);
+    note_launch();
     for (uint32_t l = 1; l < levels; ++l)
         k_upper_spheres<<<(sizes[l] + 127) / 128, 128, 0, s>>>(h.spheres, h.level_off[l - 1],
                                                                sizes[l - 1], h.level_off[l], sizes[l]);
+        note_launch();
     e = cudaGetLastError();
     cudaStreamSynchronize(s);
     cudaFree(perm_tmp);

@@ -44,6 +44,7 @@ cudaError_t launch_raygen_primary(const CameraP& cam, uint32_t w, uint32_t h, rs
     const uint32_t n = tx * ty * 64u;
     if (n == 0) return cudaSuccess;
     k_raygen_primary<<<(n + 255u) / 256u, 256, 0, s>>>(cam, w, h, tx, n, rays, pixel_of_ray);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -76,6 +77,8 @@ __global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* _
             key = ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, hp, l);
         }
     }
+    if (key == RSH_KEY_NONE)  // empty slot: an explicit no-ray (tmax < tmin) for consumers without keys
+        store_ray(rays, slot, make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, -1.f));
     keys[slot] = key;
 }
 
@@ -85,6 +88,7 @@ cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_
     const uint32_t n = w * h * lights.count;
     if (n == 0) return cudaSuccess;
     k_raygen_shadow<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, w, h, lights, eps, hp, rays, keys);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -146,6 +150,8 @@ __global__ void k_raygen_reflect(const float4* __restrict__ spos, const float4* 
             key = ray_hash(o.x, o.y, o.z, r.x, r.y, r.z, hp, 0u);
         }
     }
+    if (key == RSH_KEY_NONE)
+        store_ray(rays, slot, make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, -1.f));
     keys[slot] = key;
 }
 
@@ -157,6 +163,7 @@ cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const 
     if (n == 0) return cudaSuccess;
     k_raygen_reflect<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, prev, v3{eye[0], eye[1], eye[2]}, n,
                                                      eps, jitter, seed, bounce, hp, rays, keys);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -174,6 +181,7 @@ cudaError_t launch_hash(const rsh_ray* rays, uint32_t n, const HashP& hp, uint32
                         uint32_t* keys, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_hash<<<(n + 255u) / 256u, 256, 0, s>>>(rays, n, hp, tag, keys);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -205,6 +213,7 @@ cudaError_t launch_hash_segments(const rsh_ray* rays, uint32_t n, const uint32_t
     if (n == 0) return cudaSuccess;
     k_hash_segments<<<(n + 255u) / 256u, 256, 0, s>>>(rays, n, seg_start, nseg, hps_dev, tag_shift,
                                                     keys);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -224,6 +233,7 @@ cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s) {
     size_t blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     k_fill_u32<<<(unsigned)blocks, 256, 0, s>>>(p, v, n);
+    note_launch();
     return cudaGetLastError();
 }
 cudaError_t launch_fill_u64(unsigned long long* p, unsigned long long v, size_t n, cudaStream_t s) {
@@ -231,6 +241,7 @@ cudaError_t launch_fill_u64(unsigned long long* p, unsigned long long v, size_t 
     size_t blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     k_fill_u64<<<(unsigned)blocks, 256, 0, s>>>(p, v, n);
+    note_launch();
     return cudaGetLastError();
 }
 

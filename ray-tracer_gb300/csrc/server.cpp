@@ -1,0 +1,384 @@
+// Serving loop: continuous batching of render requests over resident scenes.
+//
+// The reference renders one scene per GLUT frame callback (display(), main.cpp:1077-1368) with no
+// request queue. Here a host thread runs steps: every step (1) admits queued requests while their
+// device memory fits the server's HBM budget, (2) generates the current stage's rays of every in-flight
+// request (primary rays, or one bounce's shadow + reflection rays), (3) traces all of them in ONE
+// batched call (segmented hash/compress/sort/decompress, hierarchy build, one persistent fused
+// traversal + intersection launch), (4) resolves hits and advances each request; finished requests
+// leave and new ones join between steps. Ray state and results stay on the device until rsh_server_wait
+// copies them out. A request's results do not depend on what else is in the batch: its rays form their
+// own key segment, sort stably within it, and pack into work units of their own.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "engine.h"
+
+using namespace rsh;
+
+namespace {
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Req {
+    uint64_t id = 0;
+    rsh_request r{};
+    int32_t status = RSH_OK;
+    double submit_ms = 0, start_ms = 0, finish_ms = 0;
+    uint64_t rays = 0;
+    bool done = false, cancelled = false, collected = false;
+    uint32_t stage = 0;  // 0 = primary; 1 + b = bounce b
+    size_t bytes = 0;
+    // device buffers
+    void* buf = nullptr;
+    rsh_ray* prim_rays = nullptr;
+    uint32_t* prim_pix = nullptr;
+    unsigned long long* prim_hits = nullptr;
+    float4* spos = nullptr;
+    float4* snrm = nullptr;
+    rsh_ray* srays = nullptr;
+    rsh_ray* rrays[2] = {nullptr, nullptr};
+    uint32_t* keys = nullptr;
+    unsigned long long* hits = nullptr;  // depth x npix
+    uint32_t* flags = nullptr;           // depth x npix x L
+};
+
+size_t request_bytes(const rsh_request& r) {
+    const size_t npix = (size_t)r.width * r.height;
+    const size_t np = (size_t)((r.width + 7) / 8) * ((r.height + 7) / 8) * 64;
+    const size_t L = r.light_count;
+    size_t b = np * (32 + 4 + 8) + npix * (16 + 16 + 32 * L + 64 + 4 * std::max<size_t>(L, 1)) +
+               npix * 8 * r.depth + npix * L * 4 * r.depth;
+    return (b + 4095) & ~size_t(4095);
+}
+
+}  // namespace
+
+struct rsh_server {
+    rsh_ctx* ctx = nullptr;
+    std::vector<const rsh_scene*> scenes;
+    uint64_t budget = 0;
+    uint32_t max_inflight = 64;
+    cudaStream_t stream = nullptr;
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Req*> queue;
+    std::vector<Req*> inflight;
+    std::map<uint64_t, Req*> all;
+    uint64_t next_id = 1;
+    bool stop = false;
+    uint64_t completed = 0, steps = 0, peak_inflight = 0, bytes_in_use = 0, peak_bytes = 0;
+    rsh_status fatal = RSH_OK;
+};
+
+namespace {
+
+rsh_status alloc_request(Req* q) {
+    const rsh_request& r = q->r;
+    const size_t npix = (size_t)r.width * r.height;
+    const size_t np = (size_t)((r.width + 7) / 8) * ((r.height + 7) / 8) * 64;
+    const size_t L = r.light_count;
+    char* p = nullptr;
+    RSH_CUDA(cudaMalloc(&p, q->bytes));
+    q->buf = p;
+    auto take = [&](size_t n) {
+        char* x = p;
+        p += (n + 255) & ~size_t(255);
+        return x;
+    };
+    q->prim_rays = reinterpret_cast<rsh_ray*>(take(np * 32));
+    q->prim_pix = reinterpret_cast<uint32_t*>(take(np * 4));
+    q->prim_hits = reinterpret_cast<unsigned long long*>(take(np * 8));
+    q->spos = reinterpret_cast<float4*>(take(npix * 16));
+    q->snrm = reinterpret_cast<float4*>(take(npix * 16));
+    q->srays = reinterpret_cast<rsh_ray*>(take(npix * L * 32));
+    q->rrays[0] = reinterpret_cast<rsh_ray*>(take(npix * 32));
+    q->rrays[1] = reinterpret_cast<rsh_ray*>(take(npix * 32));
+    q->keys = reinterpret_cast<uint32_t*>(take(npix * std::max<size_t>(L, 1) * 4));
+    q->hits = reinterpret_cast<unsigned long long*>(take(npix * 8 * r.depth));
+    q->flags = reinterpret_cast<uint32_t*>(take(npix * L * 4 * r.depth));
+    return RSH_OK;
+}
+
+void free_request(rsh_server* s, Req* q) {
+    if (q->buf) {
+        cudaFree(q->buf);
+        q->buf = nullptr;
+        s->bytes_in_use -= q->bytes;
+    }
+}
+
+// one step of the loop (server thread, no lock held while the GPU works)
+rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
+    cudaStream_t st = s->stream;
+    std::vector<rsh_batch_segment> segs;
+    segs.reserve(act.size() * 2);
+    for (Req* q : act) {
+        const rsh_request& r = q->r;
+        const rsh_scene* sc = s->scenes[r.scene_index];
+        const uint32_t W = r.width, H = r.height, npix = W * H, L = r.light_count;
+        if (q->stage == 0) {
+            CameraP cp;
+            for (int i = 0; i < 3; ++i) {
+                cp.eye[i] = r.camera.eye[i];
+                cp.dir[i] = r.camera.direction[i];
+                cp.right[i] = r.camera.right[i];
+                cp.up[i] = r.camera.up[i];
+            }
+            RSH_CUDA(launch_raygen_primary(cp, W, H, q->prim_rays, q->prim_pix, st));
+            const uint32_t np = ((W + 7) / 8) * ((H + 7) / 8) * 64;
+            segs.push_back(rsh_batch_segment{sc, q->prim_rays, np, 0, reinterpret_cast<uint64_t*>(q->prim_hits),
+                                             nullptr});
+        } else {
+            const uint32_t b = q->stage - 1;
+            uint32_t lbits = 0;
+            while ((1u << lbits) < L) ++lbits;
+            HashP hp_s, hp_r;
+            RSH_TRY(make_hash_params(sc, s->ctx->cfg, lbits, hp_s));
+            RSH_TRY(make_hash_params(sc, s->ctx->cfg, 0, hp_r));
+            LightsP lp{};
+            lp.count = L;
+            for (uint32_t l = 0; l < L; ++l)
+                for (int i = 0; i < 3; ++i) lp.pos[l][i] = r.lights[l].position[i];
+            RSH_CUDA(launch_raygen_shadow(q->spos, q->snrm, W, H, lp, s->ctx->cfg.epsilon, hp_s, q->srays, q->keys, st));
+            const rsh_ray* prev = (b == 0) ? nullptr : q->rrays[(b - 1) & 1];
+            rsh_ray* cur = q->rrays[b & 1];
+            RSH_CUDA(launch_raygen_reflect(q->spos, q->snrm, prev, r.camera.eye, W, H, s->ctx->cfg.epsilon,
+                                           s->ctx->cfg.reflect_jitter, s->ctx->cfg.seed, b, hp_r, cur, q->keys, st));
+            segs.push_back(rsh_batch_segment{sc, q->srays, npix * L, 1, nullptr, q->flags + (size_t)b * npix * L});
+            segs.push_back(rsh_batch_segment{sc, cur, npix, 0,
+                                             reinterpret_cast<uint64_t*>(q->hits + (size_t)b * npix), nullptr});
+        }
+    }
+    RSH_TRY(rsh_batch_trace(s->ctx, segs.data(), (uint32_t)segs.size(), st));
+    // advance: resolve hits into the next surface
+    for (Req* q : act) {
+        const rsh_request& r = q->r;
+        const rsh_scene* sc = s->scenes[r.scene_index];
+        const uint32_t W = r.width, H = r.height, npix = W * H;
+        if (q->stage == 0) {
+            const uint32_t np = ((W + 7) / 8) * ((H + 7) / 8) * 64;
+            RSH_CUDA(launch_resolve(sc->pos, sc->nrm, sc->mat, q->prim_rays, q->prim_hits, q->prim_pix, np, q->spos,
+                                    q->snrm, st));
+        } else {
+            const uint32_t b = q->stage - 1;
+            RSH_CUDA(launch_resolve(sc->pos, sc->nrm, sc->mat, q->rrays[b & 1], q->hits + (size_t)b * npix, nullptr,
+                                    npix, q->spos, q->snrm, st));
+            q->rays += (uint64_t)npix * (r.light_count + 1);
+        }
+    }
+    RSH_CUDA(cudaStreamSynchronize(st));
+    return rsh_check_device_errors(s->ctx, st);
+}
+
+void server_main(rsh_server* s) {
+    cudaSetDevice(s->ctx->device);
+    for (;;) {
+        std::vector<Req*> act;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            // admission by HBM budget
+            while (!s->queue.empty() && s->inflight.size() < s->max_inflight) {
+                Req* q = s->queue.front();
+                if (q->cancelled) {
+                    s->queue.pop_front();
+                    q->done = true;
+                    q->status = RSH_ERR_INVALID;
+                    q->finish_ms = now_ms();
+                    s->cv_done.notify_all();
+                    continue;
+                }
+                if (s->bytes_in_use + q->bytes > s->budget && !s->inflight.empty()) break;
+                if (q->bytes > s->budget) {  // can never fit
+                    s->queue.pop_front();
+                    q->done = true;
+                    q->status = RSH_ERR_OOM;
+                    q->finish_ms = now_ms();
+                    s->cv_done.notify_all();
+                    continue;
+                }
+                s->queue.pop_front();
+                s->bytes_in_use += q->bytes;
+                if (alloc_request(q) != RSH_OK) {
+                    s->bytes_in_use -= q->bytes;
+                    q->done = true;
+                    q->status = RSH_ERR_OOM;
+                    q->finish_ms = now_ms();
+                    s->cv_done.notify_all();
+                    continue;
+                }
+                q->start_ms = now_ms();
+                s->inflight.push_back(q);
+            }
+            s->peak_inflight = std::max<uint64_t>(s->peak_inflight, s->inflight.size());
+            s->peak_bytes = std::max(s->peak_bytes, s->bytes_in_use);
+            // drop cancelled in-flight requests between steps
+            for (auto it = s->inflight.begin(); it != s->inflight.end();) {
+                if ((*it)->cancelled) {
+                    free_request(s, *it);
+                    (*it)->done = true;
+                    (*it)->status = RSH_ERR_INVALID;
+                    (*it)->finish_ms = now_ms();
+                    it = s->inflight.erase(it);
+                    s->cv_done.notify_all();
+                } else {
+                    ++it;
+                }
+            }
+            if (s->inflight.empty()) {
+                if (s->stop) return;
+                s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+                continue;
+            }
+            act = s->inflight;
+        }
+        rsh_status st = run_step(s, act);
+        std::lock_guard<std::mutex> lk(s->mu);
+        ++s->steps;
+        for (Req* q : act) {
+            if (st != RSH_OK) {
+                q->status = st;
+                q->stage = q->r.depth + 1;
+            } else {
+                q->stage += 1;
+            }
+            if (q->stage > q->r.depth) {
+                q->done = true;
+                q->finish_ms = now_ms();
+                ++s->completed;
+                s->inflight.erase(std::find(s->inflight.begin(), s->inflight.end(), q));
+            }
+        }
+        if (st != RSH_OK) s->fatal = st;
+        s->cv_done.notify_all();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+rsh_status rsh_server_create(rsh_ctx* ctx, const rsh_scene* const* scenes, uint32_t scene_count, uint64_t hbm_budget,
+                             uint32_t max_inflight, rsh_server** out) {
+    if (!ctx || !scenes || !scene_count || !out) return RSH_ERR_INVALID;
+    rsh_server* s = new rsh_server();
+    s->ctx = ctx;
+    s->scenes.assign(scenes, scenes + scene_count);
+    s->budget = hbm_budget ? hbm_budget : (8ull << 30);
+    s->max_inflight = max_inflight ? max_inflight : 64;
+    if (2 * s->max_inflight > 1024) s->max_inflight = 512;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return cuda_status(e, "rsh_server_create");
+    }
+    s->th = std::thread(server_main, s);
+    *out = s;
+    return RSH_OK;
+}
+
+rsh_status rsh_server_submit(rsh_server* s, const rsh_request* req, uint64_t* id_out) {
+    if (!s || !req || req->scene_index >= s->scenes.size() || req->width == 0 || req->height == 0 ||
+        req->depth < 1 || req->depth > 4 || req->light_count < 1 || req->light_count > 8)
+        return RSH_ERR_INVALID;
+    Req* q = new Req();
+    q->r = *req;
+    q->bytes = request_bytes(*req);
+    q->submit_ms = now_ms();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        q->id = s->next_id++;
+        s->all[q->id] = q;
+        s->queue.push_back(q);
+    }
+    s->cv_work.notify_one();
+    if (id_out) *id_out = q->id;
+    return RSH_OK;
+}
+
+rsh_status rsh_server_wait(rsh_server* s, uint64_t id, uint32_t timeout_ms, rsh_request_result* result,
+                           uint64_t* hits_host, uint32_t* flags_host) {
+    if (!s) return RSH_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return RSH_ERR_INVALID;
+    Req* q = it->second;
+    if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return q->done; })) {
+        set_error("request not finished");
+        return RSH_ERR_TIMEOUT;
+    }
+    if (result) {
+        result->id = q->id;
+        result->status = q->status;
+        result->submit_ms = q->submit_ms;
+        result->start_ms = q->start_ms;
+        result->finish_ms = q->finish_ms;
+        result->rays = q->rays;
+    }
+    const rsh_request& r = q->r;
+    const size_t npix = (size_t)r.width * r.height;
+    if (q->buf && q->status == RSH_OK) {
+        if (hits_host) RSH_CUDA(cudaMemcpy(hits_host, q->hits, npix * 8 * r.depth, cudaMemcpyDeviceToHost));
+        if (flags_host)
+            RSH_CUDA(cudaMemcpy(flags_host, q->flags, npix * r.light_count * 4 * r.depth, cudaMemcpyDeviceToHost));
+    }
+    free_request(s, q);
+    s->all.erase(it);
+    const int32_t st = q->status;
+    delete q;
+    s->cv_work.notify_one();
+    return (rsh_status)st;
+}
+
+rsh_status rsh_server_cancel(rsh_server* s, uint64_t id) {
+    if (!s) return RSH_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return RSH_ERR_INVALID;
+    it->second->cancelled = true;
+    s->cv_work.notify_one();
+    return RSH_OK;
+}
+
+rsh_status rsh_server_stats(rsh_server* s, uint64_t* completed, uint64_t* steps, uint64_t* peak_inflight,
+                            uint64_t* peak_bytes) {
+    if (!s) return RSH_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (completed) *completed = s->completed;
+    if (steps) *steps = s->steps;
+    if (peak_inflight) *peak_inflight = s->peak_inflight;
+    if (peak_bytes) *peak_bytes = s->peak_bytes;
+    return s->fatal;
+}
+
+rsh_status rsh_server_destroy(rsh_server* s) {
+    if (!s) return RSH_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        for (Req* q : s->queue) q->cancelled = true;
+    }
+    s->cv_work.notify_all();
+    if (s->th.joinable()) s->th.join();
+    for (auto& kv : s->all) {
+        free_request(s, kv.second);
+        delete kv.second;
+    }
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return RSH_OK;
+}
+
+}  // extern "C"

@@ -53,6 +53,7 @@ cudaError_t launch_resolve(const float4* tris_orig_pos, const float4* tris_orig_
     if (n == 0) return cudaSuccess;
     k_resolve<<<(n + 255) / 256, 256, 0, s>>>(tris_orig_pos, tris_orig_nrm, mat_ids, rays, hits,
                                               pixel_of_ray, n, spos, snrm);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -112,6 +113,7 @@ cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t s) {
     const uint32_t n = a.w * a.h;
     if (n == 0) return cudaSuccess;
     k_shade<<<(n + 255) / 256, 256, 0, s>>>(a);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -128,6 +130,7 @@ __global__ void k_pack(const float4* __restrict__ acc, uint32_t n, uint32_t* rgb
 cudaError_t launch_pack_rgba(const float4* accum, uint32_t n, uint32_t* rgba, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_pack<<<(n + 255) / 256, 256, 0, s>>>(accum, n, rgba);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -226,6 +226,7 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
     cudaError_t e = cudaMemsetAsync(w, 0, (4 * 256 + 8 + passes * tiles * 256) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     k_sort_hist<<<152 * 2, 256, 0, s>>>(keys_in, n_max, d_count, passes, hist);
+    note_launch();
     // ping-pong so that the last pass lands in the output
     const uint32_t* ki = keys_in;
     const uint32_t* vi = vals_in;
@@ -239,6 +240,7 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
         const uint32_t grid = (uint32_t)(tiles - 1 > 0 ? tiles - 1 : 1);
         k_onesweep<<<grid, SR_THREADS, 0, s>>>(ki, vi, ko, vo, n_max, d_count, 8u * p, hist + 256u * p,
                                                status + p * tiles * 256, tickets + p, err);
+        note_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         ki = ko;

@@ -55,6 +55,27 @@ RSH_DEV bool node_hits_sphere(const NodeR& p, float4 s) {
     return true;
 }
 
+// Can ray (o, d, [tmin, tmax]) touch sphere s? Conservative per-ray filter applied before a cluster's
+// triangle tests: the distance from the sphere centre to the ray line (through a cross product) and the
+// parameter interval of the sphere along the ray, each with a 1e-5 relative slack for FP32 rounding
+// and |d| = 1 +- 1e-7. A miss here implies every triangle inside the sphere is missed.
+RSH_DEV bool ray_hits_sphere(float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
+                             float4 s) {
+    const float vx = s.x - ox, vy = s.y - oy, vz = s.z - oz;
+    const float t = (vx * dx + vy * dy) + vz * dz;
+    const float wx = vy * dz - vz * dy;
+    const float wy = vz * dx - vx * dz;
+    const float wz = vx * dy - vy * dx;
+    const float perp = sqrtf((wx * wx + wy * wy) + wz * wz);
+    const float dist = sqrtf((vx * vx + vy * vy) + vz * vz);
+    const float slack = (dist + s.w) * 1e-5f;
+    const float r = s.w + slack;
+    if (perp > r) return false;
+    if (t + r < tmin) return false;
+    if (t - r > tmax) return false;
+    return true;
+}
+
 // ---------------------------------------------------------------- watertight ray/triangle test
 // Woop, Benthin & Wald, "Watertight Ray/Triangle Intersection", JCGT 2(1), 2013: shear the triangle
 // into the ray's frame (largest |d| axis becomes z), evaluate the 2-D edge functions, fall back to

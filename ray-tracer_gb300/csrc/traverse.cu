@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(TV_WARPS * 32) k_traverse(TravArgs a) {
         uint32_t u = 0;
         if (lane == 0) u = atomicAdd(&a.work[0], 1u);
         u = __shfl_sync(0xffffffffu, u, 0);
-        if (u >= n1) break;
+        if (u >= n1 || u >= a.unit_end) break;
         if (*(volatile uint32_t*)&a.work[1] != 0xFFFFFFFFu) break;  // an overflow happened: stop
         // this lane's two packets: 2q and 2q+1 of the unit
         const uint32_t p0 = 8u * u + 2u * q, p1 = p0 + 1u;
@@ -151,6 +151,7 @@ cudaError_t launch_traverse(const TravArgs& a, cudaStream_t s) {
     const uint32_t need = (units + TV_WARPS - 1) / TV_WARPS;
     if (need < grid) grid = need > 0 ? need : 1;
     k_traverse<<<grid, TV_WARPS * 32, 0, s>>>(a);
+    note_launch();
     return cudaGetLastError();
 }
 

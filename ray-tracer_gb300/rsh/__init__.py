@@ -24,6 +24,7 @@ KEY_NONE = 0xFFFFFFFF
 HIT_NONE = 0xFFFFFFFFFFFFFFFF
 OCCLUDED = 0xFFFFFFFF
 FLAG_STAGE_TIMERS = 1
+FLAG_FUSED = 2
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 NODE_DTYPE = np.dtype([("c", "<f4", 3), ("radius", "<f4"), ("axis", "<f4", 3), ("cos_spread", "<f4"),
@@ -136,6 +137,7 @@ SIGNATURES = {
     "rsh_event_elapsed": (C.c_int, [_P, _P, _P]),
     "rsh_device_count": (C.c_int, []),
     "rsh_sm_count": (C.c_int, []),
+    "rsh_kernel_launches": (_U64, []),
     "rsh_scene_upload": (C.c_int, [_P, _P, _P]),
     "rsh_scene_destroy": (C.c_int, [_P, _P]),
     "rsh_scene_bounds": (C.c_int, [_P, _P, _P]),

@@ -86,3 +86,29 @@ def test_frame_soup_small():
     _check_frame(ctx, s, sc, 96, 64, 3, 0.0)
     sc.destroy()
     ctx.destroy()
+
+
+def test_fused_frame_equals_plain_frame():
+    """RSH_FLAG_FUSED (batched form inside the frame) must give the same hits, flags and image."""
+    s = scenes.soup(n_spheres=400, width=128, height=96, extent=25.0)
+    outs = []
+    for flags in (0, rsh.FLAG_FUSED):
+        ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, reflect_jitter=1.0, flags=flags)
+        sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+        ctx.set_camera(rsh.camera_look_at(s.eye, s.target, s.up, s.fov, 128, 96))
+        ctx.set_lights(s.lights)
+        rgba = rsh.DeviceArray(128 * 96, np.uint32)
+        ctx.render(sc, 128, 96, 3, rgba)
+        ctx.check_device_errors()
+        st = ctx.stats()
+        res = [ctx.frame_hits(-1, 128 * 96)]
+        for b in range(3):
+            res += [ctx.frame_hits(b, 128 * 96), ctx.frame_shadow(b, 128 * 96 * len(s.lights))]
+        res.append(rgba.numpy())
+        outs.append((res, st))
+        sc.destroy()
+        ctx.destroy()
+    for a, b in zip(outs[0][0], outs[1][0]):
+        assert np.array_equal(a, b)
+    assert outs[0][1]["shadow_rays"] == outs[1][1]["shadow_rays"]
+    assert outs[0][1]["reflection_rays"] == outs[1][1]["reflection_rays"]

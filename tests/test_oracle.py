@@ -1,0 +1,148 @@
+"""CPU checks of the oracle itself: against the committed golden vectors, against independent numpy
+restatements of the hash / compression / sort / decompression semantics, and the hierarchy path against
+its own brute force (conservativeness of the sphere/cone culling)."""
+import numpy as np
+import pytest
+
+import oracle
+from rsh import scenes
+
+GOLDEN = np.load(__import__("pathlib").Path(__file__).with_name("golden") / "cornell_32.npz")
+
+
+def test_golden_vectors_reproduce():
+    import importlib.util
+    from pathlib import Path
+
+    spec = importlib.util.spec_from_file_location("mg", Path(__file__).with_name("golden") / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    got = mg.compute()
+    for k in GOLDEN.files:
+        assert np.array_equal(np.asarray(got[k]), GOLDEN[k]), k
+
+
+# ---------------------------------------------------------------- independent numpy restatements
+def _spread(v, stride, bits):
+    r = np.zeros_like(v, dtype=np.uint32)
+    for i in range(bits):
+        r |= ((v >> np.uint32(i)) & np.uint32(1)) << np.uint32(stride * i)
+    return r
+
+
+def np_hash(rays, lo, scale, g, b, tag=0):
+    f32 = np.float32
+    o = rays["o"].astype(f32)
+    d = rays["d"].astype(f32)
+    gmax = f32((1 << g) - 1)
+    f = (o - lo.astype(f32)) * scale.astype(f32)
+    f = np.fmin(np.fmax(f, f32(0)), gmax)
+    c = f.astype(np.uint32)
+    cell = (_spread(c[:, 0], 3, 10) << np.uint32(2)) | (_spread(c[:, 1], 3, 10) << np.uint32(1)) | _spread(c[:, 2], 3, 10)
+    s = (np.abs(d[:, 0]) + np.abs(d[:, 1])) + np.abs(d[:, 2])
+    px = d[:, 0] / s
+    py = d[:, 1] / s
+    neg = d[:, 2] < 0
+    qx = f32(1) - np.abs(py)
+    qy = f32(1) - np.abs(px)
+    px2 = np.where(px >= 0, qx, -qx)
+    py2 = np.where(py >= 0, qy, -qy)
+    px = np.where(neg, px2, px)
+    py = np.where(neg, py2, py)
+    B = 1 << b
+    half = f32(0.5) * f32(B)
+    bmax = f32(B - 1)
+    u = np.fmin(np.fmax((px + f32(1)) * half, f32(0)), bmax).astype(np.uint32)
+    v = np.fmin(np.fmax((py + f32(1)) * half, f32(0)), bmax).astype(np.uint32)
+    dirb = (_spread(u, 2, 16) << np.uint32(1)) | _spread(v, 2, 16)
+    key = (np.uint32(tag) << np.uint32(3 * g + 2 * b)) | (cell << np.uint32(2 * b)) | dirb
+    valid = rays["tmax"] > rays["tmin"]
+    return np.where(valid, key, np.uint32(0xFFFFFFFF)).astype(np.uint32)
+
+
+@pytest.mark.parametrize("g,b", [(5, 4), (3, 6), (8, 2), (1, 1)])
+def test_hash_matches_numpy_restatement(g, b):
+    rng = np.random.default_rng(g * 7 + b)
+    n = 50_000
+    rays = np.zeros(n, oracle.RAY_DTYPE)
+    rays["o"] = rng.uniform(-3, 3, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[:6] = [[1, 0, 0], [0, -1, 0], [0, 0, -1], [0, 0, 1], [-0.6, 0, -0.8], [0.6, -0.8, 0]]
+    rays["d"] = d.astype(np.float32)
+    rays["tmin"] = 0.01
+    rays["tmax"] = np.inf
+    rays["tmax"][7] = -1
+    lo = np.array([-2, -2, -2], np.float32)
+    hi = np.array([2, 2, 2], np.float32)
+    scale = oracle.hash_scale(lo, hi, g)
+    assert np.array_equal(scale, np.float32(1 << g) / (hi - lo))
+    assert np.array_equal(oracle.hash_rays(rays, lo, scale, g, b, 0), np_hash(rays, lo, scale, g, b, 0))
+    assert np.array_equal(oracle.hash_rays(rays, lo, scale, g, b, 1), np_hash(rays, lo, scale, g, b, 1))
+
+
+def test_compress_sort_decompress_match_numpy():
+    rng = np.random.default_rng(1)
+    keys = np.repeat(rng.integers(0, 1000, 5000).astype(np.uint32), rng.integers(1, 9, 5000))
+    keys[rng.random(len(keys)) < 0.3] = 0xFFFFFFFF
+    tr, ck, cb, cs = oracle.compress(keys)
+    valid = np.nonzero(keys != 0xFFFFFFFF)[0]
+    assert np.array_equal(tr, valid)
+    tk = keys[valid]
+    heads = np.concatenate([[True], tk[1:] != tk[:-1]])
+    assert np.array_equal(ck, tk[heads])
+    assert np.array_equal(cb[:-1], np.nonzero(heads)[0])
+    assert cb[-1] == len(tr)
+    assert np.array_equal(cs, np.diff(cb))
+    sk, sv = oracle.sort_pairs(ck, None, 10)
+    order = np.argsort(ck, kind="stable")
+    assert np.array_equal(sv, order) and np.array_equal(sk, ck[order])
+    dk, di = oracle.decompress(sk, sv, cb, tr)
+    # decompressed order == stable sort of the trimmed rays by key
+    o2 = np.argsort(tk, kind="stable")
+    assert np.array_equal(di, tr[o2])
+    assert np.array_equal(dk, tk[o2])
+
+
+def test_hierarchy_path_equals_brute_force_cornell(cornell):
+    s = cornell
+    W = H = 48
+    cam = np.array([0, 0, 3.4, 0, 0, -3.4, 2 * 3.4 * np.tan(np.radians(30)), 0, 0, 0,
+                    2 * 3.4 * np.tan(np.radians(30)), 0], np.float32)
+    rays, pix = oracle.raygen_primary(cam, W, H)
+    lo = s.positions[..., :3].reshape(-1, 3).min(0)
+    hi = s.positions[..., :3].reshape(-1, 3).max(0)
+    oh = oracle.ObjH(s.positions, 8, lo, hi)
+    nodes, _ = oracle.build_rsh(rays, None, len(rays), 8)
+    cand, _ = oh.traverse(nodes, len(rays), 8)
+    got = oh.intersect(rays, None, len(rays), 8, cand, False, len(rays))
+    bf = oracle.brute(s.positions, rays, False)
+    assert np.array_equal(got, bf)
+    spos, snrm = oracle.resolve(s.positions, s.normals, s.material_ids, rays, bf, pix, W * H)
+    scale = oracle.hash_scale(lo, hi, 5)
+    for jitter in (0.0, 1.0):
+        rr, rk = oracle.raygen_reflect(spos, snrm, None, cam[:3], W, H, 0.01, jitter, 3, 0, lo, scale, 5, 4)
+        res, R, _, _ = oh.trace_keyed(rr, rk, 23, 8, False)
+        v = rk != oracle.KEY_NONE
+        assert np.array_equal(res[v], oracle.brute(s.positions, rr[v], False))
+    sr, sk = oracle.raygen_shadow(spos, snrm, W, H, np.array([[0, 0.95, 0]], np.float32), 0.01, lo, scale, 5, 4)
+    res, R, _, _ = oh.trace_keyed(sr, sk, 23, 8, True)
+    v = sk != oracle.KEY_NONE
+    assert R == int(v.sum()) > 0
+    assert np.array_equal(res[v], oracle.brute(s.positions, sr[v], True))
+
+
+@pytest.mark.parametrize("P", [8, 16, 32])
+def test_hierarchy_path_equals_brute_force_soup(P):
+    s = scenes.random_soup(8000, np.random.default_rng(4))
+    rays = scenes.surface_rays(s, 6000, np.random.default_rng(5))
+    lo = s.positions[..., :3].reshape(-1, 3).min(0)
+    hi = s.positions[..., :3].reshape(-1, 3).max(0)
+    oh = oracle.ObjH(s.positions, 8, lo, hi)
+    keys = oracle.hash_rays(rays, lo, oracle.hash_scale(lo, hi, 5), 5, 4)
+    res, R, _, ctr = oh.trace_keyed(rays, keys, 23, P, False)
+    assert np.array_equal(res, oracle.brute(s.positions, rays, False))
+    assert ctr[1] < len(rays) * s.tri_count  # the hierarchy culls
+    rays["tmax"] = 2.0
+    res, R, _, _ = oh.trace_keyed(rays, keys, 23, P, True)
+    assert np.array_equal(res, oracle.brute(s.positions, rays, True))
