@@ -382,7 +382,8 @@ def gpu_arm(args, s, rank, world, td):
         "secondary_ms_per_step": round(sec_ms / args.steps, 3),
         "fused": {"value": round(fused_value, 3), "unit": "Mrays/s", "ratio_vs_plain": round(fused_value / value, 3)
                   if value else None, "ms_per_step": round(f_ms / args.steps, 3),
-                  "secondary_ms_per_step": round(f_sec / args.steps, 3)},
+                  "secondary_ms_per_step": round(f_sec / args.steps, 3),
+                  "node_tests_per_frame": f_stats[-1]["node_tests"], "tri_tests_per_frame": f_stats[-1]["tri_tests"]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 48 + 32 * len(s.lights),
                 "d2h_bytes_per_step": npix * 4, "ms_per_step": round(e_ms / args.steps, 3)},
         "roofline": roof,

@@ -14,6 +14,8 @@
 // Nothing reads a count back to the host, so the whole sequence is captured in a CUDA graph.
 #include <chrono>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -204,37 +206,70 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     return RSH_OK;
 }
 
-// Host staging of the segment tables: pinned memory owned per context, which a captured graph reads
-// again on every replay.
-struct HostStage {
+// Host staging of the segment tables (pinned, read by asynchronous copies): a ring of slots per context,
+// each fenced by an event recorded after its copies, so a slot is never rewritten while a copy that reads
+// it may still be pending. A captured graph gets its own staging buffer, alive as long as the graph.
+struct StageSlot {
     void* ptr = nullptr;
     size_t bytes = 0;
+    cudaEvent_t done = nullptr;
+    bool used = false;
+};
+struct HostStage {
+    StageSlot slot[4];
+    uint32_t next = 0;
 };
 std::map<const rsh_ctx*, HostStage> g_stage;
+std::mutex g_stage_mu;
 
-rsh_status stage_tables(rsh_ctx* ctx, BatchPlan& pl, void** prep_h, void** fsegs_h) {
-    HostStage& hs = g_stage[ctx];
-    const size_t need = sizeof(PrepSeg) * pl.nseg + sizeof(FusedSeg) * pl.nseg + 256;
-    if (hs.bytes < need) {
-        if (hs.ptr) cudaFreeHost(hs.ptr);
-        hs.ptr = nullptr;
-        RSH_CUDA(cudaMallocHost(&hs.ptr, need));
-        hs.bytes = need;
-    }
-    char* b = static_cast<char*>(hs.ptr);
+size_t table_bytes(const BatchPlan& pl) { return sizeof(PrepSeg) * pl.nseg + sizeof(FusedSeg) * pl.nseg + 256; }
+
+void fill_tables(const BatchPlan& pl, char* b) {
     std::memcpy(b, pl.h_prep.data(), sizeof(PrepSeg) * pl.nseg);
     std::memcpy(b + sizeof(PrepSeg) * pl.nseg, pl.h_fsegs.data(), sizeof(FusedSeg) * pl.nseg);
-    *prep_h = b;
-    *fsegs_h = b + sizeof(PrepSeg) * pl.nseg;
+}
+
+// Returns pinned memory holding the tables. `own` != nullptr: a fresh buffer owned by the caller (graphs);
+// otherwise a ring slot whose fence the caller records with *fence after enqueuing the copies.
+rsh_status stage_tables(rsh_ctx* ctx, const BatchPlan& pl, char** out, void** own, cudaEvent_t* fence) {
+    const size_t need = table_bytes(pl);
+    if (own) {
+        void* p = nullptr;
+        RSH_CUDA(cudaMallocHost(&p, need));
+        fill_tables(pl, static_cast<char*>(p));
+        *own = p;
+        *out = static_cast<char*>(p);
+        *fence = nullptr;
+        return RSH_OK;
+    }
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    HostStage& hs = g_stage[ctx];
+    StageSlot& sl = hs.slot[hs.next];
+    hs.next = (hs.next + 1) % 4;
+    if (sl.used) RSH_CUDA(cudaEventSynchronize(sl.done));
+    if (!sl.done) RSH_CUDA(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+    if (sl.bytes < need) {
+        if (sl.ptr) cudaFreeHost(sl.ptr);
+        sl.ptr = nullptr;
+        RSH_CUDA(cudaMallocHost(&sl.ptr, need));
+        sl.bytes = need;
+    }
+    fill_tables(pl, static_cast<char*>(sl.ptr));
+    sl.used = true;
+    *out = static_cast<char*>(sl.ptr);
+    *fence = sl.done;
     return RSH_OK;
 }
 
-rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s) {
+rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, void** own_stage = nullptr) {
     if (pl.nseg == 0) return RSH_OK;
-    void *prep_h, *fsegs_h;
-    RSH_TRY(stage_tables(ctx, pl, &prep_h, &fsegs_h));
-    RSH_CUDA(cudaMemcpyAsync(pl.prep, prep_h, sizeof(PrepSeg) * pl.nseg, cudaMemcpyHostToDevice, s));
-    RSH_CUDA(cudaMemcpyAsync(pl.fsegs, fsegs_h, sizeof(FusedSeg) * pl.nseg, cudaMemcpyHostToDevice, s));
+    char* tables = nullptr;
+    cudaEvent_t fence = nullptr;
+    RSH_TRY(stage_tables(ctx, pl, &tables, own_stage, &fence));
+    RSH_CUDA(cudaMemcpyAsync(pl.prep, tables, sizeof(PrepSeg) * pl.nseg, cudaMemcpyHostToDevice, s));
+    RSH_CUDA(cudaMemcpyAsync(pl.fsegs, tables + sizeof(PrepSeg) * pl.nseg, sizeof(FusedSeg) * pl.nseg,
+                             cudaMemcpyHostToDevice, s));
+    if (fence) RSH_CUDA(cudaEventRecord(fence, s));
     RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
     if (pl.total == 0) return RSH_OK;
     uint32_t* cnt = static_cast<uint32_t*>(pl.counts);
@@ -292,9 +327,24 @@ struct GraphExec {
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     rsh_ctx* ctx = nullptr;
+    void* stage = nullptr;  // pinned segment tables read by every replay
 };
 
 }  // namespace
+
+namespace rsh {
+// Frees the context's staging ring (called by rsh_destroy).
+void batch_release_ctx(const rsh_ctx* ctx) {
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    auto it = g_stage.find(ctx);
+    if (it == g_stage.end()) return;
+    for (StageSlot& sl : it->second.slot) {
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.ptr) cudaFreeHost(sl.ptr);
+    }
+    g_stage.erase(it);
+}
+}  // namespace rsh
 
 extern "C" {
 
@@ -326,11 +376,12 @@ rsh_status rsh_batch_graph_create(rsh_ctx* ctx, const rsh_batch_segment* segment
         delete g;
         return cuda_status(e, "cudaStreamBeginCapture");
     }
-    rsh_status st = batch_enqueue(ctx, pl, stream);
+    rsh_status st = batch_enqueue(ctx, pl, stream, &g->stage);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(stream, &graph);
     if (st != RSH_OK || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
+        if (g->stage) cudaFreeHost(g->stage);
         delete g;
         return st != RSH_OK ? st : cuda_status(e, "cudaStreamEndCapture");
     }
@@ -338,6 +389,7 @@ rsh_status rsh_batch_graph_create(rsh_ctx* ctx, const rsh_batch_segment* segment
     e = cudaGraphInstantiate(&g->exec, graph, 0);
     if (e != cudaSuccess) {
         cudaGraphDestroy(graph);
+        if (g->stage) cudaFreeHost(g->stage);
         delete g;
         return cuda_status(e, "cudaGraphInstantiate");
     }
@@ -359,6 +411,7 @@ rsh_status rsh_batch_graph_destroy(void* graph_exec) {
     if (!g) return RSH_ERR_INVALID;
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->stage) cudaFreeHost(g->stage);
     delete g;
     return RSH_OK;
 }

@@ -315,6 +315,8 @@ rsh_status rsh_create(const rsh_config* cfg, rsh_ctx** out) {
 rsh_status rsh_destroy(rsh_ctx* ctx) {
     if (!ctx) return RSH_ERR_INVALID;
     cudaDeviceSynchronize();
+    batch_release_ctx(ctx);
+    for (const cudaEvent_t ev : ctx->tev) cudaEventDestroy(ev);
     for (auto& kv : ctx->bufs) release_buf(ctx, kv.second);
     for (auto& b : ctx->bounce) {
         release_buf(ctx, b.shadow_rays);

@@ -90,6 +90,7 @@ void stage_end(rsh_ctx* ctx, int handle, cudaStream_t s);
 rsh_status ensure_buf(rsh_ctx* ctx, DevBuf& b, size_t bytes);
 void release_buf(rsh_ctx* ctx, DevBuf& b);
 rsh_status make_hash_params(const rsh_scene* sc, const rsh_config& cfg, uint32_t tag_bits, HashP& out);
+void batch_release_ctx(const rsh_ctx* ctx);
 
 // One secondary batch through compress -> sort -> decompress -> build -> traverse -> intersect.
 // keys: per slot (RSH_KEY_NONE = no ray); rays indexed by slot. Output flags/hits indexed by slot
