@@ -299,6 +299,17 @@ rsh_status rsh_compress(rsh_ctx* ctx, const uint32_t* keys, uint32_t n_slots, ui
                         uint32_t* chunk_keys, uint32_t* chunk_bases, uint32_t* chunk_sizes,
                         uint32_t* counts, rsh_stream_t stream);
 
+/* rsh_compress without allocating: same outputs and semantics, no context, no cudaMalloc/cudaFree.
+ * For callers that may not allocate device memory themselves or let a library do it: hosts that own and
+ * pre-partition all device memory, and loops that allocate once at start-up and must not allocate while
+ * they run. No counterpart in the reference. The look-back scratch is a static device array of 196,684 bytes that every GPU loading the
+ * library keeps until the process exits; n_slots above 16,777,216 is rejected with RSH_ERR_INVALID. The
+ * first call on a device looks up the array's device address (call it once before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race, so serialise them on one stream. */
+rsh_status rsh_compress_noalloc(const uint32_t* keys, uint32_t n_slots, uint32_t* trimmed_ids,
+                                uint32_t* chunk_keys, uint32_t* chunk_bases, uint32_t* chunk_sizes,
+                                uint32_t* counts, rsh_stream_t stream);
+
 /* Stable LSD radix sort (onesweep) of (key, value) pairs by the low key_bits bits of the key.
  * n = *d_count if d_count != NULL (device), else n_max. vals_in == NULL means values 0..n-1.
  * Replaces RaySortingWrapper / cub::DeviceRadixSort::SortPairs (RayTracer.cu:2385-2409). */

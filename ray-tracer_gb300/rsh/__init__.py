@@ -163,6 +163,7 @@ SIGNATURES = {
     "rsh_raygen_reflect": (C.c_int, [_P, _P, _P, _P, _U32, _U32, _F, _F, _U32, _U32, _P, _P, _P, _P]),
     "rsh_hash": (C.c_int, [_P, _U32, _P, _U32, _P, _P]),
     "rsh_compress": (C.c_int, [_P, _P, _U32, _P, _P, _P, _P, _P, _P]),
+    "rsh_compress_noalloc": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P]),
     "rsh_sort_pairs": (C.c_int, [_P, _P, _P, _P, _P, _U32, _P, _U32, _P]),
     "rsh_decompress": (C.c_int, [_P, _P, _P, _P, _P, _P, _U32, _P, _P, _P]),
     "rsh_hierarchy_capacity": (_U32, [_U32, _U32, _P]),
