@@ -142,6 +142,8 @@ typedef struct rsh_config {
     uint32_t flags;            /* RSH_FLAG_* */
     float reflect_jitter;      /* 0: mirror reflections; >0: cosine-lobe perturbation weight */
     uint32_t seed;             /* seed of the reflection perturbation */
+    uint32_t ray_level;        /* batched form: object-tree level at and below which rays leave their packet
+                                  and descend one by one (0: packets down to the clusters; default 2) */
 } rsh_config;
 
 #define RSH_FLAG_STAGE_TIMERS 1u   /* record per-stage CUDA events (TestManager timers) */

@@ -707,30 +707,32 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
         s[2] = c.z;
         s[3] = std::sqrt(r2) * kRadSlack;
     }
-    for (uint32_t l = 1; l < levels && T; ++l)
+    // upper levels: the same formula over every vertex of the subtree (triangles [j span, (j+1) span))
+    uint64_t span = cluster;
+    for (uint32_t l = 1; l < levels && T; ++l) {
+        span *= 8;
         for (uint32_t j = 0; j < sizes[l]; ++j) {
-            const uint32_t c0 = 8 * j, c1 = std::min(c0 + 8, sizes[l - 1]);
+            const uint64_t t0 = (uint64_t)j * span, t1 = std::min<uint64_t>(t0 + span, T);
             float mn[3] = {INF, INF, INF}, mx[3] = {-INF, -INF, -INF};
-            for (uint32_t i = c0; i < c1; ++i) {
-                const float* q = &h.sph[4ull * (h.off[l - 1] + i)];
-                for (int k = 0; k < 3; ++k) {
-                    mn[k] = std::fmin(mn[k], q[k] - q[3]);
-                    mx[k] = std::fmax(mx[k], q[k] + q[3]);
+            for (uint64_t v = 3 * t0; v < 3 * t1; ++v)
+                for (int i = 0; i < 3; ++i) {
+                    mn[i] = std::fmin(mn[i], h.tris[4 * v + i]);
+                    mx[i] = std::fmax(mx[i], h.tris[4 * v + i]);
                 }
-            }
             const V3 c = V3{(mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f};
-            float r = 0.f;
-            for (uint32_t i = c0; i < c1; ++i) {
-                const float* q = &h.sph[4ull * (h.off[l - 1] + i)];
-                const V3 d = V3{q[0] - c.x, q[1] - c.y, q[2] - c.z};
-                r = std::fmax(r, length(d) + q[3]);
+            float r2 = 0.f;
+            for (uint64_t v = 3 * t0; v < 3 * t1; ++v) {
+                const float* p = &h.tris[4 * v];
+                const V3 d = V3{p[0] - c.x, p[1] - c.y, p[2] - c.z};
+                r2 = std::fmax(r2, dot(d, d));
             }
             float* s = &h.sph[4ull * (h.off[l] + j)];
             s[0] = c.x;
             s[1] = c.y;
             s[2] = c.z;
-            s[3] = r * kRadSlack;
+            s[3] = std::sqrt(r2) * kRadSlack;
         }
+    }
 }
 
 // Builds the object-sphere hierarchy; returns a handle used by the traversal / intersection calls.

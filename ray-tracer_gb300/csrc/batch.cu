@@ -229,19 +229,10 @@ void fill_tables(const BatchPlan& pl, char* b) {
     std::memcpy(b + sizeof(PrepSeg) * pl.nseg, pl.h_fsegs.data(), sizeof(FusedSeg) * pl.nseg);
 }
 
-// Returns pinned memory holding the tables. `own` != nullptr: a fresh buffer owned by the caller (graphs);
-// otherwise a ring slot whose fence the caller records with *fence after enqueuing the copies.
-rsh_status stage_tables(rsh_ctx* ctx, const BatchPlan& pl, char** out, void** own, cudaEvent_t* fence) {
+// Returns pinned memory holding the tables in a ring slot whose fence the caller records with *fence after
+// enqueuing the copies.
+rsh_status stage_tables(rsh_ctx* ctx, const BatchPlan& pl, char** out, cudaEvent_t* fence) {
     const size_t need = table_bytes(pl);
-    if (own) {
-        void* p = nullptr;
-        RSH_CUDA(cudaMallocHost(&p, need));
-        fill_tables(pl, static_cast<char*>(p));
-        *own = p;
-        *out = static_cast<char*>(p);
-        *fence = nullptr;
-        return RSH_OK;
-    }
     std::lock_guard<std::mutex> lk(g_stage_mu);
     HostStage& hs = g_stage[ctx];
     StageSlot& sl = hs.slot[hs.next];
@@ -261,11 +252,13 @@ rsh_status stage_tables(rsh_ctx* ctx, const BatchPlan& pl, char** out, void** ow
     return RSH_OK;
 }
 
-rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, void** own_stage = nullptr) {
+// pre_staged != nullptr: tables already in pinned memory owned by the caller (a captured graph, which must
+// not allocate while capturing); otherwise a fenced ring slot of the context.
+rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_staged = nullptr) {
     if (pl.nseg == 0) return RSH_OK;
-    char* tables = nullptr;
+    char* tables = pre_staged;
     cudaEvent_t fence = nullptr;
-    RSH_TRY(stage_tables(ctx, pl, &tables, own_stage, &fence));
+    if (!tables) RSH_TRY(stage_tables(ctx, pl, &tables, &fence));
     RSH_CUDA(cudaMemcpyAsync(pl.prep, tables, sizeof(PrepSeg) * pl.nseg, cudaMemcpyHostToDevice, s));
     RSH_CUDA(cudaMemcpyAsync(pl.fsegs, tables + sizeof(PrepSeg) * pl.nseg, sizeof(FusedSeg) * pl.nseg,
                              cudaMemcpyHostToDevice, s));
@@ -316,6 +309,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, void** own
     fa.units_max = pl.max_padded / pl.unit_rays;
     fa.d_units = totals + 1;
     fa.work = static_cast<uint32_t*>(pl.work);
+    fa.ray_level = ctx->cfg.ray_level;
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;
@@ -371,12 +365,19 @@ rsh_status rsh_batch_graph_create(rsh_ctx* ctx, const rsh_batch_segment* segment
     RSH_CUDA(cudaStreamSynchronize(stream));
     GraphExec* g = new GraphExec();
     g->ctx = ctx;
-    cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    cudaError_t e = cudaMallocHost(&g->stage, table_bytes(pl));
     if (e != cudaSuccess) {
+        delete g;
+        return cuda_status(e, "rsh_batch_graph_create: staging");
+    }
+    fill_tables(pl, static_cast<char*>(g->stage));
+    e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaFreeHost(g->stage);
         delete g;
         return cuda_status(e, "cudaStreamBeginCapture");
     }
-    rsh_status st = batch_enqueue(ctx, pl, stream, &g->stage);
+    rsh_status st = batch_enqueue(ctx, pl, stream, static_cast<char*>(g->stage));
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(stream, &graph);
     if (st != RSH_OK || e != cudaSuccess) {

@@ -269,6 +269,7 @@ void rsh_config_default(rsh_config* c) {
     c->flags = 0;
     c->reflect_jitter = 0.0f;
     c->seed = 0x5EED0000u;
+    c->ray_level = 2;
 }
 
 static rsh_status validate_config(const rsh_config* c) {
@@ -277,6 +278,7 @@ static rsh_status validate_config(const rsh_config* c) {
     if (c->packet_size != 8 && c->packet_size != 16 && c->packet_size != 32) return RSH_ERR_INVALID;
     if (c->cluster_size < 1 || c->cluster_size > 64) return RSH_ERR_INVALID;
     if (!(c->epsilon >= 0.0f)) return RSH_ERR_INVALID;
+    if (c->ray_level > 15) return RSH_ERR_INVALID;
     return RSH_OK;
 }
 
@@ -932,8 +934,10 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     uint32_t lbits = 0;
     while ((1u << lbits) < L) ++lbits;
     HashP hp_s, hp_r;
-    RSH_TRY(make_hash_params(sc, ctx->cfg, lbits, hp_s));
     RSH_TRY(make_hash_params(sc, ctx->cfg, 0, hp_r));
+    // the batched form re-keys every segment itself (segment tag instead of the light tag)
+    if (fused) hp_s = hp_r;
+    else RSH_TRY(make_hash_params(sc, ctx->cfg, lbits, hp_s));
     if (ctx->bounce.size() < depth) ctx->bounce.resize(depth);
 
     // primary rays (tile order) -> surface buffer 0

@@ -7,7 +7,9 @@
 // keeps the unit's rays in shared memory (watertight setup precomputed), walks the segment's
 // object-sphere tree depth-first with (node, packet-mask) stack entries, children pushed farthest-first
 // so that the nearest subtree is visited first, and at every triangle cluster immediately tests the
-// surviving packets' rays against the cluster's triangles staged in shared memory.
+// surviving packets' rays against the cluster's triangles staged in shared memory. At and below a
+// configurable object-tree level (and at once for packets whose cone is wider than a half-space) rays
+// leave their packet and descend the subtree one by one (the ray level of the ray hierarchy).
 //   closest hit: per-ray best (t bits << 32 | triangle id) kept in shared memory; after each cluster a
 //     packet's `reach` shrinks to max(|o - c| + best t), so later subtrees beyond every current hit are
 //     culled by the node test (early termination without changing any result);
@@ -47,6 +49,132 @@ RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
         if (__ldg(&segs[mid].unit_begin) <= u) lo = mid; else hi = mid;
     }
     return lo;
+}
+
+// Per-ray descent of one object-tree node's subtree: the ray leaves its packet and walks the subtree
+// alone, nearest child first, culling spheres against its own running closest-hit distance. Triangle
+// tests keep the ray's original interval and the key comparison, so ties still resolve to the smaller id.
+template <int P>
+RSH_DEV void ray_descend(FusedSmem<P>& S, uint32_t i, const FusedSeg& sg, uint32_t L0, uint32_t idx0, bool any,
+                         unsigned long long& ntests, unsigned long long& ttests) {
+    const float4 o = S.ro[i], d = S.rd[i], sh = S.rs[i];
+    const uint32_t meta = S.meta[i];
+    RayWT w;
+    w.ox = o.x;
+    w.oy = o.y;
+    w.oz = o.z;
+    w.tmin = o.w;
+    w.sx = sh.x;
+    w.sy = sh.y;
+    w.sz = sh.z;
+    w.tmax = sh.w;
+    w.kx = meta & 3u;
+    w.ky = (meta >> 2) & 3u;
+    w.kz = (meta >> 4) & 3u;
+    unsigned long long best = S.best[i];
+    float tcur = sh.w;
+    if (best != RSH_HIT_NONE) tcur = fminf(tcur, __uint_as_float((uint32_t)(best >> 32)));
+    uint32_t stk[72];
+    int sp = 0;
+    stk[sp++] = (L0 << 24) | idx0;
+    bool occl = false;
+    while (sp > 0 && !occl) {
+        const uint32_t e = stk[--sp];
+        const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
+        const uint32_t cl = L - 1u;
+        const uint32_t first = (L == sg.levels) ? 0u : 8u * idx;
+        const uint32_t size = sg.lvl_size[cl];
+        const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+        const float4* sb = sg.spheres + sg.lvl_off[cl] + first;
+        if (cl == 0) {
+            for (uint32_t c = 0; c < cnt && !occl; ++c) {
+                ++ntests;
+                if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, tcur, __ldg(sb + c))) continue;
+                const uint32_t t0 = (first + c) * sg.cluster;
+                const uint32_t t1 = (t0 + sg.cluster < sg.tri_count) ? t0 + sg.cluster : sg.tri_count;
+                for (uint32_t t = t0; t < t1; ++t) {
+                    const float4 v0 = __ldg(sg.tris + 3ull * t), v1 = __ldg(sg.tris + 3ull * t + 1),
+                                 v2 = __ldg(sg.tris + 3ull * t + 2);
+                    float th;
+                    ++ttests;
+                    if (wt_hit(w, v0, v1, v2, th)) {
+                        if (any) {
+                            occl = true;
+                            break;
+                        }
+                        const unsigned long long key = hit_key(th, __float_as_uint(v0.w));
+                        if (key < best) {
+                            best = key;
+                            tcur = fminf(tcur, th);
+                        }
+                    }
+                }
+            }
+        } else {
+            float te[8];
+            uint32_t ci[8];
+            uint32_t nh = 0;
+            for (uint32_t c = 0; c < cnt; ++c) {
+                const float4 q = __ldg(sb + c);
+                ++ntests;
+                if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, tcur, q)) continue;
+                const float tc = ((q.x - o.x) * d.x + (q.y - o.y) * d.y) + (q.z - o.z) * d.z - q.w;
+                uint32_t k = nh++;  // keep te[] sorted descending (farthest first)
+                while (k > 0 && te[k - 1] < tc) {
+                    te[k] = te[k - 1];
+                    ci[k] = ci[k - 1];
+                    --k;
+                }
+                te[k] = tc;
+                ci[k] = first + c;
+            }
+            for (uint32_t k = 0; k < nh && sp < 72; ++k) stk[sp++] = (cl << 24) | ci[k];
+        }
+    }
+    if (any) {
+        if (occl) atomicOr(&S.meta[i], 128u);
+    } else if (best < S.best[i]) {
+        S.best[i] = best;
+    }
+}
+
+// After rays were tested: retire fully occluded packets (any hit) or shrink each packet's reach to
+// max(|o - c| + best t) (closest hit). Lanes of group q hold packets 2q and 2q+1.
+template <int P>
+RSH_DEV void refresh_packets(FusedSmem<P>& S, bool any, uint32_t q, uint32_t ch, uint32_t& alive, NodeR& P0,
+                             NodeR& P1) {
+    if (any) {
+        bool all0 = true, all1 = true;
+        for (uint32_t jj = 0; jj < P; ++jj) {
+            const uint32_t m0 = S.meta[(2u * q) * P + jj], m1 = S.meta[(2u * q + 1u) * P + jj];
+            if ((m0 & 64u) && !(m0 & 128u)) all0 = false;
+            if ((m1 & 64u) && !(m1 & 128u)) all1 = false;
+        }
+        const uint32_t d0 = __ballot_sync(0xffffffffu, all0 && ch == 0);
+        const uint32_t d1 = __ballot_sync(0xffffffffu, all1 && ch == 0);
+        uint32_t dead = 0;
+#pragma unroll
+        for (uint32_t g = 0; g < 4; ++g)
+            dead |= (((d0 >> (8u * g)) & 1u) << (2u * g)) | (((d1 >> (8u * g)) & 1u) << (2u * g + 1u));
+        alive &= ~dead;
+    } else {
+        float r0m = 0.f, r1m = 0.f;
+        for (uint32_t jj = 0; jj < P; ++jj) {
+            const uint32_t i0 = (2u * q) * P + jj, i1 = (2u * q + 1u) * P + jj;
+            if (S.meta[i0] & 64u) {
+                const unsigned long long b = S.best[i0];
+                const float tb = (b == RSH_HIT_NONE) ? S.rs[i0].w : __uint_as_float((uint32_t)(b >> 32));
+                r0m = fmaxf(r0m, S.roc[i0] + tb);
+            }
+            if (S.meta[i1] & 64u) {
+                const unsigned long long b = S.best[i1];
+                const float tb = (b == RSH_HIT_NONE) ? S.rs[i1].w : __uint_as_float((uint32_t)(b >> 32));
+                r1m = fmaxf(r1m, S.roc[i1] + tb);
+            }
+        }
+        P0.reach = fminf(P0.reach, r0m * (1.0f + 1.0f / 1048576.0f));
+        P1.reach = fminf(P1.reach, r1m * (1.0f + 1.0f / 1048576.0f));
+    }
 }
 
 template <int P>
@@ -110,6 +238,12 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
         for (uint32_t g = 0; g < 4; ++g)
             mask |= (((b0 >> (8u * g)) & 1u) << (2u * g)) | (((b1 >> (8u * g)) & 1u) << (2u * g + 1u));
         uint32_t alive = mask;
+        const uint32_t f0 = __ballot_sync(0xffffffffu, v0 && !(P0.cs > 0.0f));
+        const uint32_t f1 = __ballot_sync(0xffffffffu, v1 && !(P1.cs > 0.0f));
+        uint32_t fullmask = 0;
+#pragma unroll
+        for (uint32_t g = 0; g < 4; ++g)
+            fullmask |= (((f0 >> (8u * g)) & 1u) << (2u * g)) | (((f1 >> (8u * g)) & 1u) << (2u * g + 1u));
         __syncwarp();
         if (mask != 0) {
             int sp = 1;
@@ -120,8 +254,27 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
                 __syncwarp();
                 --sp;
                 const uint32_t L = e >> 28, idx = (e >> 8) & 0xFFFFFu;
-                const uint32_t m = (e & 0xFFu) & alive;
+                uint32_t m = (e & 0xFFu) & alive;
                 if (m == 0) continue;
+                // rays of these packets leave the packet and descend this subtree one by one: below the
+                // switch level, and at once for packets whose cone is wider than a half-space
+                const uint32_t m_ray = (L <= a.ray_level) ? m : (m & fullmask);
+                if (m_ray) {
+                    const uint32_t nr = __popc(m_ray) * P;
+                    for (uint32_t ir = lane; ir < nr; ir += 32) {
+                        uint32_t pmm = m_ray;
+                        for (uint32_t s2 = 0; s2 < ir / P; ++s2) pmm &= pmm - 1u;
+                        const uint32_t i = (__ffs(pmm) - 1u) * P + (ir % P);
+                        const uint32_t mt = S.meta[i];
+                        if (!(mt & 64u) || (any && (mt & 128u))) continue;
+                        ray_descend<P>(S, i, sg, L, idx, any, ntests, ttests);
+                    }
+                    __syncwarp();
+                    refresh_packets<P>(S, any, q, ch, alive, P0, P1);
+                    m &= ~m_ray & alive;
+                    if (alive == 0) break;
+                    if (m == 0) continue;
+                }
                 const uint32_t cl = L - 1u;
                 const uint32_t first = (L == sg.levels) ? 0u : 8u * idx;
                 const uint32_t size = sg.lvl_size[cl];
@@ -217,41 +370,8 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
                         }
                         __syncwarp();
                         // refresh the packets' state: occlusion (any) or shrunken reach (closest)
-                        if (any) {
-                            bool all0 = true, all1 = true;
-                            for (uint32_t jj = 0; jj < P; ++jj) {
-                                const uint32_t m0 = S.meta[(2u * q) * P + jj], m1 = S.meta[(2u * q + 1u) * P + jj];
-                                if ((m0 & 64u) && !(m0 & 128u)) all0 = false;
-                                if ((m1 & 64u) && !(m1 & 128u)) all1 = false;
-                            }
-                            const uint32_t d0 = __ballot_sync(0xffffffffu, all0 && ch == 0);
-                            const uint32_t d1 = __ballot_sync(0xffffffffu, all1 && ch == 0);
-                            uint32_t dead = 0;
-#pragma unroll
-                            for (uint32_t g = 0; g < 4; ++g)
-                                dead |= (((d0 >> (8u * g)) & 1u) << (2u * g)) | (((d1 >> (8u * g)) & 1u) << (2u * g + 1u));
-                            alive &= ~dead;
-                            if (alive == 0) break;
-                        } else {
-                            float r0m = 0.f, r1m = 0.f;
-                            for (uint32_t jj = 0; jj < P; ++jj) {
-                                const uint32_t i0 = (2u * q) * P + jj, i1 = (2u * q + 1u) * P + jj;
-                                if (S.meta[i0] & 64u) {
-                                    const unsigned long long b = S.best[i0];
-                                    const float tb = (b == RSH_HIT_NONE) ? S.rs[i0].w : __uint_as_float((uint32_t)(b >> 32));
-                                    r0m = fmaxf(r0m, S.roc[i0] + tb);
-                                }
-                                if (S.meta[i1] & 64u) {
-                                    const unsigned long long b = S.best[i1];
-                                    const float tb = (b == RSH_HIT_NONE) ? S.rs[i1].w : __uint_as_float((uint32_t)(b >> 32));
-                                    r1m = fmaxf(r1m, S.roc[i1] + tb);
-                                }
-                            }
-                            const float k0 = r0m * (1.0f + 1.0f / 1048576.0f);
-                            const float k1 = r1m * (1.0f + 1.0f / 1048576.0f);
-                            P0.reach = fminf(P0.reach, k0);
-                            P1.reach = fminf(P1.reach, k1);
-                        }
+                        refresh_packets<P>(S, any, q, ch, alive, P0, P1);
+                        if (alive == 0) break;
                     }
                 } else {
                     if (sp + nlive > F_STACK) {

@@ -174,6 +174,7 @@ struct FusedArgs {
     uint32_t units_max;
     const uint32_t* d_units;       // device count of units
     uint32_t* work;
+    uint32_t ray_level;            // object-tree level at and below which rays descend individually
     unsigned long long* node_tests;
     unsigned long long* tri_tests;
     uint32_t* err;

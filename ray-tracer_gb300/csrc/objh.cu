@@ -10,8 +10,8 @@
 //   3. gather triangles into cluster order (original id kept in the first vertex's w);
 //   4. level 0: one sphere per cluster of `cluster` consecutive triangles: centre = midpoint of the
 //      vertex box, radius = max vertex distance (x (1 + 2^-20));
-//   5. levels 1..: fan-out 8 over consecutive nodes, centre = midpoint of the children's sphere box,
-//      radius = max(|c_i - c| + r_i), until a level has at most 8 nodes.
+//   5. levels 1..: fan-out 8 over consecutive nodes (until a level has at most 8 nodes); each node's
+//      sphere from all vertices of its subtree by the same formula as the clusters.
 // Every sphere encloses every vertex below it, so the hierarchy never culls a real hit.
 #include "common.cuh"
 #include "kernels.h"
@@ -76,30 +76,46 @@ __global__ void k_leaf_spheres(const float4* __restrict__ tris, uint32_t n, uint
     sph[j] = make_float4(c.x, c.y, c.z, sqrtf(r2) * kRadSlack);
 }
 
-__global__ void k_upper_spheres(float4* __restrict__ sph, uint32_t child_off, uint32_t nchild,
-                                uint32_t parent_off, uint32_t nparent) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nparent) return;
-    const uint32_t c0 = 8 * j, c1 = (8 * j + 8 < nchild) ? 8 * j + 8 : nchild;
+// Level >= 1: the same formula over every vertex of the node's subtree (one warp per node); tighter than
+// enclosing the children's spheres. Min/max and max reductions are exact in any order.
+__global__ void k_level_spheres(const float4* __restrict__ tris, uint32_t n, uint64_t span, uint32_t nnodes,
+                                float4* __restrict__ sph) {
+    const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (j >= nnodes) return;
+    const uint64_t t0 = (uint64_t)j * span;
+    const uint64_t t1 = (t0 + span < n) ? t0 + span : n;
+    const uint64_t v0 = 3 * t0, v1 = 3 * t1;
     const float inf = __int_as_float(0x7f800000);
     float mnx = inf, mny = inf, mnz = inf, mxx = -inf, mxy = -inf, mxz = -inf;
-    for (uint32_t i = c0; i < c1; ++i) {
-        const float4 q = sph[child_off + i];
-        mnx = fminf(mnx, q.x - q.w);
-        mny = fminf(mny, q.y - q.w);
-        mnz = fminf(mnz, q.z - q.w);
-        mxx = fmaxf(mxx, q.x + q.w);
-        mxy = fmaxf(mxy, q.y + q.w);
-        mxz = fmaxf(mxz, q.z + q.w);
+    for (uint64_t v = v0 + lane; v < v1; v += 32) {
+        const float4 p = __ldg(tris + v);
+        mnx = fminf(mnx, p.x);
+        mny = fminf(mny, p.y);
+        mnz = fminf(mnz, p.z);
+        mxx = fmaxf(mxx, p.x);
+        mxy = fmaxf(mxy, p.y);
+        mxz = fmaxf(mxz, p.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+        mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
     }
     const v3 c = v3{(mnx + mxx) * 0.5f, (mny + mxy) * 0.5f, (mnz + mxz) * 0.5f};
-    float r = 0.f;
-    for (uint32_t i = c0; i < c1; ++i) {
-        const float4 q = sph[child_off + i];
-        const v3 d = v3{q.x - c.x, q.y - c.y, q.z - c.z};
-        r = fmaxf(r, len3(d) + q.w);
+    float r2 = 0.f;
+    for (uint64_t v = v0 + lane; v < v1; v += 32) {
+        const float4 p = __ldg(tris + v);
+        const v3 d = v3{p.x - c.x, p.y - c.y, p.z - c.z};
+        r2 = fmaxf(r2, dot3(d, d));
     }
-    sph[parent_off + j] = make_float4(c.x, c.y, c.z, r * kRadSlack);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+    if (lane == 0) sph[j] = make_float4(c.x, c.y, c.z, sqrtf(r2) * kRadSlack);
 }
 
 size_t objh_scratch_bytes(uint32_t tri_count) {
@@ -165,10 +181,13 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     }
     k_leaf_spheres<<<(sizes[0] + 127) / 128, 128, 0, s>>>(h.tris, n, cluster, sizes[0], h.spheres);
     note_launch();
-    for (uint32_t l = 1; l < levels; ++l)
-        k_upper_spheres<<<(sizes[l] + 127) / 128, 128, 0, s>>>(h.spheres, h.level_off[l - 1],
-                                                               sizes[l - 1], h.level_off[l], sizes[l]);
+    uint64_t span = cluster;
+    for (uint32_t l = 1; l < levels; ++l) {
+        span *= 8;
+        k_level_spheres<<<(sizes[l] * 32 + 127) / 128, 128, 0, s>>>(h.tris, n, span, sizes[l],
+                                                                   h.spheres + h.level_off[l]);
         note_launch();
+    }
     e = cudaGetLastError();
     cudaStreamSynchronize(s);
     cudaFree(perm_tmp);

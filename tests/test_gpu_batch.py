@@ -19,10 +19,11 @@ def ctx():
     c.destroy()
 
 
+@pytest.mark.parametrize("ray_level", [0, 2, 15])
 @pytest.mark.parametrize("P", [8, 16, 32])
 @pytest.mark.parametrize("any_hit", [False, True])
-def test_fused_vs_brute(P, any_hit):
-    c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=P, cluster_size=8)
+def test_fused_vs_brute(P, any_hit, ray_level):
+    c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=P, cluster_size=8, ray_level=ray_level)
     s = scenes.random_soup(40_000, np.random.default_rng(P))
     sc = c.scene(s.positions, s.normals, s.material_ids, s.materials)
     rng = np.random.default_rng(100 + P)
