@@ -6,9 +6,11 @@ Workload (default): the procedural-architecture scene (40x40 tessellated pillars
 bounce), FP32, seeded synthetic input. One step = one frame through rsh_render_frame.
 
   value       secondary rays traced (after trimming) / GPU time from the first secondary ray generation to
-              the last secondary intersection of each frame (CUDA events on the frame's stream), plain path
-  fused       the same frames with the batched form (one segmented sort + one persistent fused
-              traversal/intersection launch per bounce)
+              the last secondary intersection of each frame (CUDA events on the frame's stream), through
+              rsh_render_frame in its batched form (RSH_FLAG_FUSED: per bounce one segmented hash/sort and
+              one persistent fused traversal + intersection launch)
+  plain       the same frames through the plain per-frame path (separate traversal -> candidates ->
+              intersection kernels, as the reference's wrappers); identical results
   e2e         the same metric through the C ABI with host buffers: camera + lights from host structs in,
               the RGBA8 frame copied to pinned host memory, both inside the timed region
   roofline    the dominant kernel's achieved rate against its roofline (per-stage CUDA events)
@@ -278,87 +280,107 @@ def gpu_arm(args, s, rank, world, td):
         barrier(td)
         return ms.value, stats
 
-    # warm-up (also sizes every buffer)
-    for _ in range(args.warmup):
-        frame(0)
-    lib.rsh_stream_synchronize(st)
+    def rays_of(stats):
+        return sum(x["shadow_rays"] + x["reflection_rays"] for x in stats)
+
+    def rate(stats):
+        ms = reduce_max(td, sum(x["secondary_ms"] for x in stats))
+        return reduce_sum(td, rays_of(stats)) / (ms * 1e3) if ms > 0 else 0.0
+
+    passes = {}
     clocks = ClockSampler()
     clocks.start()
-    launches_before = lib.rsh_kernel_launches()
-    wall_ms, stats = timed(0, args.steps)
-    launches = lib.rsh_kernel_launches() - launches_before
+    for name, flags in (("plain", 0), ("fused", 2)):
+        if args.mode not in ("all", name):
+            continue
+        for _ in range(args.warmup):  # warm-up (also sizes every buffer)
+            frame(flags)
+        lib.rsh_stream_synchronize(st)
+        l0 = lib.rsh_kernel_launches()
+        wall, stats = timed(flags, args.steps)
+        passes[name] = {"flags": flags, "wall_ms": reduce_max(td, wall), "stats": stats, "value": rate(stats),
+                        "launches": lib.rsh_kernel_launches() - l0}
     clk = clocks.stop()
-    sec_rays = sum(x["shadow_rays"] + x["reflection_rays"] for x in stats)
-    sec_ms = sum(x["secondary_ms"] for x in stats)
-    sec_ms_max = reduce_max(td, sec_ms)
-    total_rays = reduce_sum(td, sec_rays)
-    value = total_rays / (sec_ms_max * 1e3) if sec_ms_max > 0 else 0.0
-    ms_per_step = reduce_max(td, wall_ms) / args.steps
+    head = passes["fused"] if "fused" in passes else passes["plain"]
+    value = head["value"]
+    ms_per_step = head["wall_ms"] / args.steps
+    sec_rays = rays_of(head["stats"])
+    sec_ms = sum(x["secondary_ms"] for x in head["stats"])
+    launches = head["launches"]
 
-    # fused (batched) form on the same frames
-    for _ in range(max(1, args.warmup // 2)):
-        frame(2)
-    f_ms, f_stats = timed(2, args.steps)
-    f_rays = sum(x["shadow_rays"] + x["reflection_rays"] for x in f_stats)
-    f_sec = sum(x["secondary_ms"] for x in f_stats)
-    fused_value = reduce_sum(td, f_rays) / (reduce_max(td, f_sec) * 1e3) if f_sec > 0 else 0.0
+    def pass_summary(p):
+        last = p["stats"][-1]
+        return {"value": round(p["value"], 3), "unit": "Mrays/s", "ms_per_step": round(p["wall_ms"] / args.steps, 3),
+                "secondary_ms_per_step": round(sum(x["secondary_ms"] for x in p["stats"]) / args.steps, 3),
+                "node_tests_per_frame": last["node_tests"], "tri_tests_per_frame": last["tri_tests"],
+                "candidates_per_frame": last["candidates"], "gpu_launches": p["launches"]}
 
-    # e2e through the C ABI with host buffers
-    e_ms, e_stats = timed(0, args.steps, e2e=True)
-    e_rays = sum(x["shadow_rays"] + x["reflection_rays"] for x in e_stats)
-    e2e_value = reduce_sum(td, e_rays) / (reduce_max(td, e_ms) * 1e3)
-
-    # per-stage timers (separate frames: events between stages)
-    t_ms, t_stats = timed(1, max(1, min(args.steps, 3)))
-    stage_names = ["primary", "raygen", "compress", "sort", "decompress", "build", "traverse", "intersect", "shade"]
-    nst = len(t_stats)
-    stage_ms = {nm: sum(x["stage_ms"][i] for x in t_stats) / nst for i, nm in enumerate(stage_names)}
-    last = t_stats[-1]
-    chunks = last["chunks"]
-    R = last["shadow_rays"] + last["reflection_rays"]
-    slots = npix * (len(s.lights) + 1) * depth
-    key_bits = 3 * cfg.grid_bits + 2 * cfg.dir_log2 + 2
-    passes = (key_bits + 7) // 8
-    bytes_stage = {
-        "raygen": 64.0 * slots,
-        "compress": 4.0 * slots + 12.0 * chunks + 4.0 * R,
-        "sort": chunks * (4.0 + 16.0 * passes),
-        "decompress": 12.0 * chunks + 4.0 * R,
-        "build": 32.0 * R,
-    }
-    flops_stage = {"traverse": 24.0 * last["node_tests"], "intersect": 46.0 * last["tri_tests"]}
-    per_stage = {}
-    for nm in ("raygen", "compress", "sort", "decompress", "build"):
-        ms = stage_ms[nm]
-        gbs = bytes_stage[nm] / (ms * 1e6) if ms > 0 else 0.0
-        per_stage[nm] = {"ms": round(ms, 4), "GB/s": round(gbs, 1), "frac_hbm": round(gbs / peaks["hbm_gbs"], 4)}
-    sm_clock = clk.get("sm_mhz") or peaks["sm_max_mhz"]
-    n_sm = lib.rsh_sm_count()
-    fp32_peak = n_sm * 128 * 2 * sm_clock * 1e6 / 1e12   # TFLOP/s at the observed SM clock
-    for nm in ("traverse", "intersect"):
-        ms = stage_ms[nm]
-        tf = flops_stage[nm] / (ms * 1e9) if ms > 0 else 0.0
-        per_stage[nm] = {"ms": round(ms, 4), "TFLOP/s": round(tf, 3), "frac_fp32": round(tf / fp32_peak, 4)}
-    dom = max(("raygen", "compress", "sort", "decompress", "build", "traverse", "intersect"), key=lambda k: stage_ms[k])
-    if dom in flops_stage:
-        ach = per_stage[dom]["TFLOP/s"]
-        roof = {"bound": "fp32", "kernel": dom, "achieved": ach, "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
-                "frac": round(ach / fp32_peak, 4), "traffic": None,
-                "peak_note": f"FP32 issue: {n_sm} SMs x 128 lanes x 2 flops x {sm_clock:.0f} MHz (no measured FP32 peak)"}
-    else:
-        ach = per_stage[dom]["GB/s"]
-        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": None,
-                "peak_note": f"{peaks['source']} HBM copy bandwidth"}
-    prof = ROOT / "profiles" / "traffic.json"
-    if prof.exists():
-        try:
-            tr = json.loads(prof.read_text())
-            if dom in tr:
-                roof["traffic"] = tr[dom]
-        except Exception:
-            pass
-    ctx_err = lib.rsh_check_device_errors(ctx.handle, st)
+    e2e = None
+    per_stage, roof, last = {}, None, head["stats"][-1]
+    if args.mode == "all":
+        # e2e through the C ABI with host buffers, headline form
+        e_ms, e_stats = timed(head["flags"], args.steps, e2e=True)
+        e2e = {"value": round(reduce_sum(td, rays_of(e_stats)) / (reduce_max(td, e_ms) * 1e3), 3), "unit": "Mrays/s",
+               "h2d_bytes_per_step": 48 + 32 * len(s.lights), "d2h_bytes_per_step": npix * 4,
+               "ms_per_step": round(e_ms / args.steps, 3)}
+        # per-stage timers (separate frames: events between stages), headline form
+        t_ms, t_stats = timed(head["flags"] | 1, max(1, min(args.steps, 3)))
+        stage_names = ["primary", "raygen", "compress", "sort", "decompress", "build", "traverse", "intersect",
+                       "shade"]
+        nst = len(t_stats)
+        stage_ms = {nm: sum(x["stage_ms"][i] for x in t_stats) / nst for i, nm in enumerate(stage_names)}
+        last = t_stats[-1]
+        chunks = last["chunks"]
+        R = last["shadow_rays"] + last["reflection_rays"]
+        slots = npix * (len(s.lights) + 1) * depth
+        key_bits = 3 * cfg.grid_bits + 2 * cfg.dir_log2 + 2
+        passes_sort = (key_bits + 7) // 8
+        bytes_stage = {
+            "raygen": 64.0 * slots,
+            "compress": 4.0 * slots + 12.0 * chunks + 4.0 * R,
+            "sort": chunks * (4.0 + 16.0 * passes_sort),
+            "decompress": 12.0 * chunks + 4.0 * R,
+            "build": 32.0 * R,
+        }
+        fused_head = head["flags"] == 2
+        if fused_head:  # traversal and intersection run in one kernel: charge both to it
+            flops_stage = {"traverse": 24.0 * last["node_tests"] + 46.0 * last["tri_tests"], "intersect": 0.0}
+        else:
+            flops_stage = {"traverse": 24.0 * last["node_tests"], "intersect": 46.0 * last["tri_tests"]}
+        for nm in ("raygen", "compress", "sort", "decompress", "build"):
+            ms = stage_ms[nm]
+            gbs = bytes_stage[nm] / (ms * 1e6) if ms > 0 else 0.0
+            per_stage[nm] = {"ms": round(ms, 4), "GB/s": round(gbs, 1), "frac_hbm": round(gbs / peaks["hbm_gbs"], 4)}
+        sm_clock = clk.get("sm_mhz") or peaks["sm_max_mhz"]
+        n_sm = lib.rsh_sm_count()
+        fp32_peak = n_sm * 128 * 2 * sm_clock * 1e6 / 1e12   # TFLOP/s at the observed SM clock
+        for nm in ("traverse", "intersect"):
+            ms = stage_ms[nm]
+            tf = flops_stage[nm] / (ms * 1e9) if ms > 0 else 0.0
+            per_stage[nm] = {"ms": round(ms, 4), "TFLOP/s": round(tf, 3), "frac_fp32": round(tf / fp32_peak, 4)}
+        if fused_head:
+            per_stage["traverse"]["kernel"] = "k_fused (traversal + intersection)"
+        dom = max(("raygen", "compress", "sort", "decompress", "build", "traverse", "intersect"),
+                  key=lambda k: stage_ms[k])
+        if dom in flops_stage:
+            ach = per_stage[dom]["TFLOP/s"]
+            roof = {"bound": "fp32", "kernel": "k_fused" if (fused_head and dom == "traverse") else f"k_{dom}",
+                    "achieved": ach, "peak": round(fp32_peak, 2), "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4),
+                    "traffic": None,
+                    "peak_note": f"FP32 issue: {n_sm} SMs x 128 lanes x 2 flops x {sm_clock:.0f} MHz (no measured FP32 peak)"}
+        else:
+            ach = per_stage[dom]["GB/s"]
+            roof = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                    "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": None,
+                    "peak_note": f"{peaks['source']} HBM copy bandwidth"}
+        prof = ROOT / "profiles" / "traffic.json"
+        if prof.exists():
+            try:
+                tr = json.loads(prof.read_text())
+                if roof["kernel"] in tr:
+                    roof["traffic"] = tr[roof["kernel"]]
+            except Exception:
+                pass
     out = {
         "metric": METRIC,
         "value": round(value, 3),
@@ -374,27 +396,28 @@ def gpu_arm(args, s, rank, world, td):
         "data": "synthetic (seeded procedural architecture scene)",
         "config": {"workload": f"procedural architecture {s.tri_count} tris, {W}x{H}, {len(s.lights)} point lights, "
                                f"depth {depth}, cosine-lobe reflections",
+                   "path": "rsh_render_frame " + ("batched form (RSH_FLAG_FUSED)" if head["flags"] == 2 else "plain"),
                    "triangles": s.tri_count, "width": W, "height": H, "lights": len(s.lights), "depth": depth,
                    "grid_bits": cfg.grid_bits, "dir_log2": cfg.dir_log2, "packet_size": cfg.packet_size,
-                   "cluster_size": cfg.cluster_size, "l2": "inputs larger than L2 (scene + per-frame rays > 129 MB)",
-                   "parallelism": f"replicas x{world}"},
+                   "cluster_size": cfg.cluster_size, "ray_level": cfg.ray_level,
+                   "l2": "inputs larger than L2 (scene + per-frame rays > 129 MB)", "parallelism": f"replicas x{world}"},
         "secondary_rays_per_step": round(sec_rays / args.steps),
         "secondary_ms_per_step": round(sec_ms / args.steps, 3),
-        "fused": {"value": round(fused_value, 3), "unit": "Mrays/s", "ratio_vs_plain": round(fused_value / value, 3)
-                  if value else None, "ms_per_step": round(f_ms / args.steps, 3),
-                  "secondary_ms_per_step": round(f_sec / args.steps, 3),
-                  "node_tests_per_frame": f_stats[-1]["node_tests"], "tri_tests_per_frame": f_stats[-1]["tri_tests"]},
-        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 48 + 32 * len(s.lights),
-                "d2h_bytes_per_step": npix * 4, "ms_per_step": round(e_ms / args.steps, 3)},
+        "e2e": e2e,
         "roofline": roof,
         "stages": per_stage,
-        "counters_per_frame": {"chunks": chunks, "candidates": last["candidates"], "node_tests": last["node_tests"],
-                               "tri_tests": last["tri_tests"], "overflow_passes": last["overflow_passes"]},
+        "counters_per_frame": {"chunks": last["chunks"], "candidates": last["candidates"],
+                               "node_tests": last["node_tests"], "tri_tests": last["tri_tests"],
+                               "overflow_passes": last["overflow_passes"]},
         "gpu_launches": int(launches),
         "clocks": clk,
         "scene_upload_s": round(upload_s, 3),
-        "device_errors": int(ctx_err),
     }
+    for name, p in passes.items():
+        out[name] = pass_summary(p)
+    if "plain" in passes and "fused" in passes and passes["plain"]["value"] > 0:
+        out["fused"]["ratio_vs_plain"] = round(passes["fused"]["value"] / passes["plain"]["value"], 3)
+    out["device_errors"] = int(lib.rsh_check_device_errors(ctx.handle, st))
     lib.rsh_free_host(host_img)
     sc.destroy()
     ctx.destroy()
@@ -410,9 +433,17 @@ def main():
     ap.add_argument("--config", default="P", choices=["S", "O", "P"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-crop", default="240x136")
+    ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling runs)")
+    ap.add_argument("--height", type=int, default=0, help="override the frame height (profiling runs)")
+    ap.add_argument("--mode", default="all", choices=["all", "plain", "fused"],
+                    help="all: plain + fused + e2e + stage timers; plain/fused: only that timed pass")
     args = ap.parse_args()
     rank, world, td = dist_setup(args.gpus)
     s = make_workload(args.config)
+    if args.width:
+        s.width = args.width
+    if args.height:
+        s.height = args.height
     crop = tuple(int(x) for x in args.cpu_crop.split("x"))
     if args.impl == "reference":
         if rank != 0:

@@ -71,7 +71,7 @@ def lib():
             "orc_brute": (None, [P, U32, P, U32, I, P, P]),
             "orc_brute_second": (None, [P, U32, P, U32, P, P]),
             "orc_resolve": (None, [P, P, P, P, P, P, U32, P, P]),
-            "orc_trace_keyed": (U32, [P, P, P, U32, U32, U32, I, P, P, P, P]),
+            "orc_trace_keyed": (U32, [P, P, P, U32, U32, U32, I, P, P, P, P, U32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_lib, name)
@@ -212,7 +212,7 @@ class ObjH:
                             int(any_hit), _p(flags), _p(hits))
         return flags if any_hit else hits
 
-    def trace_keyed(self, rays, keys, key_bits, P, any_hit):
+    def trace_keyed(self, rays, keys, key_bits, P, any_hit, ray_level=3):
         rays = np.ascontiguousarray(rays, RAY_DTYPE)
         keys = _u32(keys)
         n = len(keys)
@@ -221,7 +221,7 @@ class ObjH:
         ms = np.zeros(8, np.float32)
         ctr = np.zeros(2, np.uint64)
         R = lib().orc_trace_keyed(self.h, _p(rays), _p(keys), n, key_bits, P, int(any_hit), _p(flags), _p(hits),
-                                  _p(ms), _p(ctr))
+                                  _p(ms), _p(ctr), ray_level)
         return (flags if any_hit else hits), int(R), ms, ctr
 
     def __del__(self):

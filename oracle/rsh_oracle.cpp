@@ -377,6 +377,68 @@ void traverse_packet(const Node& p, const ObjH& h, uint32_t L, uint32_t idx, std
     }
 }
 
+// Per-ray descent of the object subtree below (L0, idx0): nearest child first, spheres culled against
+// the ray's running closest-hit distance, triangle tests with the ray's own interval (the batched form's
+// per-ray phase). Returns true if occluded (any hit); updates best (closest hit).
+bool ray_descend(const ObjH& h, const Ray& r, const RayWT& w, uint32_t L0, uint32_t idx0, bool any, uint64_t& best,
+                 uint64_t& ntests, uint64_t& ttests) {
+    float tcur = r.tmax;
+    if (best != HIT_NONE) tcur = std::fmin(tcur, u2f((uint32_t)(best >> 32)));
+    Ray rc = r;
+    uint32_t stk[96];
+    int sp = 0;
+    stk[sp++] = (L0 << 24) | idx0;
+    while (sp > 0) {
+        const uint32_t e = stk[--sp];
+        const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
+        const uint32_t cl = L - 1;
+        const uint32_t first = (L == h.levels) ? 0 : 8 * idx;
+        const uint32_t cnt = std::min<uint32_t>(8, h.size[cl] - first);
+        rc.tmax = tcur;
+        if (cl == 0) {
+            for (uint32_t c = 0; c < cnt; ++c) {
+                ++ntests;
+                rc.tmax = tcur;
+                if (!ray_hits_sphere(rc, &h.sph[4ull * (h.off[0] + first + c)])) continue;
+                const uint32_t t0 = (first + c) * h.cluster, t1 = std::min(t0 + h.cluster, h.T);
+                for (uint32_t t = t0; t < t1; ++t) {
+                    const float* v = &h.tris[12ull * t];
+                    float th;
+                    ++ttests;
+                    if (wt_hit(w, v, v + 4, v + 8, th)) {
+                        if (any) return true;
+                        const uint64_t key = hit_key(th, f2u(v[3]));
+                        if (key < best) {
+                            best = key;
+                            tcur = std::fmin(tcur, th);
+                        }
+                    }
+                }
+            }
+        } else {
+            float te[8];
+            uint32_t ci[8];
+            uint32_t nh = 0;
+            for (uint32_t c = 0; c < cnt; ++c) {
+                const float* q = &h.sph[4ull * (h.off[cl] + first + c)];
+                ++ntests;
+                if (!ray_hits_sphere(rc, q)) continue;
+                const float tc = ((q[0] - r.o[0]) * r.d[0] + (q[1] - r.o[1]) * r.d[1]) + (q[2] - r.o[2]) * r.d[2] - q[3];
+                uint32_t k = nh++;
+                while (k > 0 && te[k - 1] < tc) {
+                    te[k] = te[k - 1];
+                    ci[k] = ci[k - 1];
+                    --k;
+                }
+                te[k] = tc;
+                ci[k] = first + c;
+            }
+            for (uint32_t k = 0; k < nh && sp < 96; ++k) stk[sp++] = (cl << 24) | ci[k];
+        }
+    }
+    return false;
+}
+
 }  // namespace
 
 extern "C" {
@@ -649,8 +711,11 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
     h.T = T;
     h.cluster = cluster;
     std::vector<uint32_t> codes(T);
-    float sc[3];
-    for (int i = 0; i < 3; ++i) sc[i] = (hi[i] > lo[i]) ? 1024.0f / (hi[i] - lo[i]) : 0.0f;
+    float ext = hi[0] - lo[0];
+    if (hi[1] - lo[1] > ext) ext = hi[1] - lo[1];
+    if (hi[2] - lo[2] > ext) ext = hi[2] - lo[2];
+    const float sc1 = (ext > 0.0f) ? 1024.0f / ext : 0.0f;
+    const float sc[3] = {sc1, sc1, sc1};
     for (uint32_t t = 0; t < T; ++t) {
         const float* a = pos + 12ull * t;
         uint32_t cc[3];
@@ -912,11 +977,12 @@ void orc_resolve(const float* pos, const float* nrm, const uint32_t* mat, const 
 
 // ---------------------------------------------------------------- the whole algorithm on the CPU
 // One keyed batch through compress -> sort -> decompress -> build -> traverse+intersect (per packet, all
-// host threads). Used as the CPU baseline; returns the number of traced rays. stage_ms (8 floats) gets
-// per-stage wall times: compress, sort, decompress, build, traverse+intersect.
+// host threads), with the same hybrid traversal as the GPU's batched form: packet tests above
+// `ray_level`, per-ray descent below. Used as the CPU baseline; returns the number of traced rays.
+// stage_ms (8 floats) gets per-stage wall times: compress, sort, decompress, build, traverse+intersect.
 uint32_t orc_trace_keyed(void* hp, const float* rays_in, const uint32_t* keys, uint32_t n_slots, uint32_t key_bits,
                          uint32_t P, int any, uint32_t* flags, uint64_t* hits, float* stage_ms,
-                         uint64_t* counters /* node tests, tri tests */) {
+                         uint64_t* counters /* node tests, tri tests */, uint32_t ray_level) {
     using clk = std::chrono::steady_clock;
     auto ms = [](clk::time_point a, clk::time_point b) {
         return std::chrono::duration<float, std::milli>(b - a).count();
@@ -943,45 +1009,113 @@ uint32_t orc_trace_keyed(void* hp, const float* rays_in, const uint32_t* keys, u
     const uint32_t n0 = (R + P - 1) / P;
     uint64_t ntests = 0, ttests = 0;
     if (h.levels) {
+        // per packet: packet tests above ray_level (and not at all for full cones), then each ray descends
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : ntests, ttests)
         for (int64_t p = 0; p < (int64_t)n0; ++p) {
-            const Node& nd = nodes[off[0] + p];
+            Node nd = nodes[off[0] + p];
             if (nd.count == 0) continue;
-            std::vector<uint32_t> cl;
-            uint64_t t = 0;
-            traverse_packet(nd, h, h.levels, 0, cl, t);
-            ntests += t;
+            uint32_t ids[64];
+            RayWT ws[64];
+            uint64_t best[64];
+            bool occl[64];
+            uint32_t nr = 0;
             for (uint32_t j = 0; j < P; ++j) {
                 const uint32_t k = (uint32_t)p * P + j;
                 if (k >= R) break;
                 const uint32_t id = sorted[k];
-                const Ray& r = rays[id];
-                if (!(r.tmax > r.tmin)) continue;
-                const RayWT w = wt_setup(r);
-                uint64_t best = HIT_NONE;
-                bool occl = false;
-                for (uint32_t c : cl) {
-                    if (!ray_hits_sphere(r, &h.sph[4ull * c])) continue;
-                    const uint32_t a0 = c * h.cluster, a1 = std::min(a0 + h.cluster, h.T);
-                    for (uint32_t t2i = a0; t2i < a1; ++t2i) {
-                        const float* v = &h.tris[12ull * t2i];
-                        float th;
-                        ++ttests;
-                        if (wt_hit(w, v, v + 4, v + 8, th)) {
-                            if (any) {
-                                occl = true;
-                                break;
-                            }
-                            const uint64_t key = hit_key(th, f2u(v[3]));
-                            if (key < best) best = key;
+                if (!(rays[id].tmax > rays[id].tmin)) continue;
+                ids[nr] = id;
+                ws[nr] = wt_setup(rays[id]);
+                best[nr] = HIT_NONE;
+                occl[nr] = false;
+                ++nr;
+            }
+            auto descend_all = [&](uint32_t L, uint32_t idx) {
+                for (uint32_t j = 0; j < nr; ++j)
+                    if (!occl[j]) occl[j] = ray_descend(h, rays[ids[j]], ws[j], L, idx, any != 0, best[j], ntests, ttests);
+            };
+            if (!(nd.cos_spread > 0.0f) || h.levels <= ray_level) {
+                descend_all(h.levels, 0);
+            } else {
+                uint32_t stk[96];
+                int sp = 0;
+                stk[sp++] = h.levels << 24;
+                while (sp > 0) {
+                    const uint32_t e = stk[--sp];
+                    const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
+                    if (L <= ray_level) {
+                        descend_all(L, idx);
+                        if (any) {
+                            bool all = true;
+                            for (uint32_t j = 0; j < nr; ++j) all = all && occl[j];
+                            if (all) break;
                         }
+                        continue;
                     }
-                    if (occl) break;
+                    const uint32_t cl = L - 1;
+                    const uint32_t first = (L == h.levels) ? 0 : 8 * idx;
+                    const uint32_t cnt = std::min<uint32_t>(8, h.size[cl] - first);
+                    float te[8];
+                    uint32_t ci[8];
+                    uint32_t nh = 0;
+                    for (uint32_t c = 0; c < cnt; ++c) {
+                        const float* q = &h.sph[4ull * (h.off[cl] + first + c)];
+                        ++ntests;
+                        if (!node_hits_sphere(nd, q)) continue;
+                        const V3 dc = V3{q[0] - nd.c[0], q[1] - nd.c[1], q[2] - nd.c[2]};
+                        const float tc = length(dc) - q[3];
+                        uint32_t k = nh++;
+                        while (k > 0 && te[k - 1] < tc) {
+                            te[k] = te[k - 1];
+                            ci[k] = ci[k - 1];
+                            --k;
+                        }
+                        te[k] = tc;
+                        ci[k] = first + c;
+                    }
+                    if (cl == 0) {  // ray_level 0: packets reach the clusters; rays filter and test them
+                        for (uint32_t k = nh; k-- > 0;) {
+                            const uint32_t c = ci[k];
+                            for (uint32_t j = 0; j < nr; ++j) {
+                                if (occl[j]) continue;
+                                const Ray& ry = rays[ids[j]];
+                                if (!ray_hits_sphere(ry, &h.sph[4ull * (h.off[0] + c)])) continue;
+                                const uint32_t a0 = c * h.cluster, a1 = std::min(a0 + h.cluster, h.T);
+                                for (uint32_t t2i = a0; t2i < a1; ++t2i) {
+                                    const float* v = &h.tris[12ull * t2i];
+                                    float th;
+                                    ++ttests;
+                                    if (wt_hit(ws[j], v, v + 4, v + 8, th)) {
+                                        if (any) {
+                                            occl[j] = true;
+                                            break;
+                                        }
+                                        const uint64_t key = hit_key(th, f2u(v[3]));
+                                        if (key < best[j]) best[j] = key;
+                                    }
+                                }
+                            }
+                        }
+                    } else {
+                        for (uint32_t k = 0; k < nh && sp < 96; ++k) stk[sp++] = (cl << 24) | ci[k];
+                    }
+                    if (!any) {  // shrink the packet's reach to its rays' current closest hits
+                        float rm = 0.0f;
+                        for (uint32_t j = 0; j < nr; ++j) {
+                            const Ray& ry = rays[ids[j]];
+                            const float tb = best[j] == HIT_NONE ? ry.tmax : u2f((uint32_t)(best[j] >> 32));
+                            const V3 oc = V3{ry.o[0] - nd.c[0], ry.o[1] - nd.c[1], ry.o[2] - nd.c[2]};
+                            rm = std::fmax(rm, length(oc) + tb);
+                        }
+                        nd.reach = std::fmin(nd.reach, rm * kRadSlack);
+                    }
                 }
+            }
+            for (uint32_t j = 0; j < nr; ++j) {
                 if (any) {
-                    if (occl) flags[id] = OCCLUDED;
-                } else if (best < hits[id]) {
-                    hits[id] = best;
+                    if (occl[j]) flags[ids[j]] = OCCLUDED;
+                } else if (best[j] < hits[ids[j]]) {
+                    hits[ids[j]] = best[j];
                 }
             }
         }

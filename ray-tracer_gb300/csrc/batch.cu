@@ -271,16 +271,23 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
                                                        static_cast<uint32_t*>(pl.keys));
     note_launch();
     RSH_CUDA(cudaGetLastError());
+    int th = stage_begin(ctx, RSH_STAGE_COMPRESS, s);
     RSH_CUDA(launch_compress(static_cast<uint32_t*>(pl.keys), pl.total, static_cast<uint32_t*>(pl.trimmed),
                              static_cast<uint32_t*>(pl.ckeys), static_cast<uint32_t*>(pl.cbases), cnt, pl.scr,
                              ctx->d_err, s));
+    stage_end(ctx, th, s);
+    th = stage_begin(ctx, RSH_STAGE_SORT, s);
     RSH_CUDA(launch_sort_pairs(static_cast<uint32_t*>(pl.ckeys), nullptr, static_cast<uint32_t*>(pl.skeys),
                                static_cast<uint32_t*>(pl.svals), pl.total, cnt + 1, pl.key_bits, pl.scr, ctx->d_err,
                                s));
+    stage_end(ctx, th, s);
+    th = stage_begin(ctx, RSH_STAGE_DECOMPRESS, s);
     RSH_CUDA(launch_decompress(static_cast<uint32_t*>(pl.skeys), static_cast<uint32_t*>(pl.svals),
                                static_cast<uint32_t*>(pl.cbases), static_cast<uint32_t*>(pl.trimmed), cnt, pl.total,
                                static_cast<uint32_t*>(pl.sorted_keys), static_cast<uint32_t*>(pl.sorted_ids), pl.scr,
                                ctx->d_err, s));
+    stage_end(ctx, th, s);
+    th = stage_begin(ctx, RSH_STAGE_BUILD, s);
     uint32_t* totals = static_cast<uint32_t*>(pl.totals);
     k_batch_bounds<<<1, 1024, 0, s>>>(static_cast<uint32_t*>(pl.sorted_keys), cnt, pl.nseg, pl.tag_shift,
                                       pl.unit_rays, static_cast<uint32_t*>(pl.seg_begin),
@@ -296,6 +303,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     RSH_CUDA(cudaGetLastError());
     RSH_CUDA(launch_build_rsh(static_cast<rsh_ray*>(pl.rays_all), static_cast<uint32_t*>(pl.padded), pl.max_padded,
                               totals, pl.P, static_cast<rsh_node*>(pl.nodes), s));
+    stage_end(ctx, th, s);
     RSH_CUDA(cudaMemsetAsync(pl.work, 0, 16, s));
     FusedArgs fa{};
     fa.nodes = static_cast<rsh_node*>(pl.nodes);
@@ -313,7 +321,9 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;
+    th = stage_begin(ctx, RSH_STAGE_TRAVERSE, s);  // traversal and intersection in one kernel
     RSH_CUDA(launch_fused(fa, s));
+    stage_end(ctx, th, s);
     return RSH_OK;
 }
 

@@ -259,17 +259,17 @@ const char* rsh_last_error_string(void) { return g_last_error.c_str(); }
 void rsh_config_default(rsh_config* c) {
     if (!c) return;
     std::memset(c, 0, sizeof(*c));
-    c->grid_bits = 5;
-    c->dir_log2 = 4;
+    c->grid_bits = 4;
+    c->dir_log2 = 6;
     c->packet_size = 8;
-    c->cluster_size = 8;
+    c->cluster_size = 4;
     c->epsilon = 0.01f;
     c->hbm_budget = 0;
     c->candidate_capacity = 0;
     c->flags = 0;
     c->reflect_jitter = 0.0f;
     c->seed = 0x5EED0000u;
-    c->ray_level = 2;
+    c->ray_level = 3;
 }
 
 static rsh_status validate_config(const rsh_config* c) {
@@ -1016,9 +1016,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
             rsh_batch_segment segs[2] = {
                 {sc, srays, npix * L, 1, nullptr, sflags},
                 {sc, rrays, npix, 0, reinterpret_cast<uint64_t*>(rhits), nullptr}};
-            th = stage_begin(ctx, RSH_STAGE_TRAVERSE, s);
             RSH_TRY(rsh_batch_trace(ctx, segs, 2, s));
-            stage_end(ctx, th, s);
             const uint32_t* seg_cnt = static_cast<const uint32_t*>(ctx->bufs["b_seg_cnt"].ptr);
             const uint32_t* bcnt = static_cast<const uint32_t*>(ctx->bufs["b_counts"].ptr);
             RSH_CUDA(cudaMemcpyAsync(fc + 4 * b, seg_cnt, 4, cudaMemcpyDeviceToDevice, s));

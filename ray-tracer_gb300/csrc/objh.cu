@@ -5,7 +5,7 @@
 // nodes (CalculateBoundingSpheresIntersections, RayTracer.cu:1152-1280); triangles then get a bounding
 // sphere each (CreateTriangleBoundingSphere, :301-376) inside the descent. Here the object spheres
 // become a full sphere tree built on the GPU:
-//   1. Morton code (10 bits per axis) of every triangle centroid over the scene box;
+//   1. Morton code (10 bits per axis) of every triangle centroid over the cube around the scene box;
 //   2. stable onesweep sort of (code, triangle id) -> cluster order;
 //   3. gather triangles into cluster order (original id kept in the first vertex's w);
 //   4. level 0: one sphere per cluster of `cluster` consecutive triangles: centre = midpoint of the
@@ -160,9 +160,15 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     void* sort_scratch = b + ((8ull * n + 255) & ~255ull);
     v3 vlo = v3{lo[0], lo[1], lo[2]};
     v3 vsc;
-    vsc.x = (hi[0] > lo[0]) ? 1024.0f / (hi[0] - lo[0]) : 0.0f;
-    vsc.y = (hi[1] > lo[1]) ? 1024.0f / (hi[1] - lo[1]) : 0.0f;
-    vsc.z = (hi[2] > lo[2]) ? 1024.0f / (hi[2] - lo[2]) : 0.0f;
+    // one scale for all axes (the cube over the largest extent): Morton bits follow physical size, so a
+    // flat scene does not spend its high-order splits on its thin axis
+    float ext = hi[0] - lo[0];
+    if (hi[1] - lo[1] > ext) ext = hi[1] - lo[1];
+    if (hi[2] - lo[2] > ext) ext = hi[2] - lo[2];
+    const float sc1 = (ext > 0.0f) ? 1024.0f / ext : 0.0f;
+    vsc.x = sc1;
+    vsc.y = sc1;
+    vsc.z = sc1;
     k_morton<<<(n + 255) / 256, 256, 0, s>>>(positions_dev, n, vlo, vsc, codes);
     note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
