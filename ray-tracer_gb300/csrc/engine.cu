@@ -97,7 +97,7 @@ rsh_status make_hash_params(const rsh_scene* sc, const rsh_config& cfg, uint32_t
 }
 
 static uint64_t cand_capacity(const rsh_ctx* ctx) {
-    return ctx->cfg.candidate_capacity ? ctx->cfg.candidate_capacity : (1ull << 26);
+    return ctx->cfg.candidate_capacity ? ctx->cfg.candidate_capacity : (1ull << 28);  // 2 GiB of candidates
 }
 
 // Traverse + intersect with the overflow/resume protocol: the traversal stops at the first work unit
@@ -131,6 +131,9 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ta.capacity = cap;
     ta.cand_count = cc;
     ta.work = w;
+    ta.ray_level = ctx->cfg.ray_level;
+    ta.rays = rays;
+    ta.sorted_ids = sorted_ids;
     ta.node_tests = ctx->d_stats + 0;
     ta.err = ctx->d_err;
     IsectArgs ia{};
@@ -149,6 +152,7 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ia.flags = flags;
     ia.hits = hits;
     ia.tri_tests = ctx->d_stats + 1;
+    ia.per_ray = ctx->cfg.ray_level > 0 ? 1u : 0u;
     // Passes over a window of work units [start, start + window). Without overflow the first pass covers
     // every unit. After an overflow the window restarts at the first unfinished unit; if a pass made no
     // progress the window shrinks (units of one pass race for the buffer), down to a single unit, which

@@ -66,13 +66,73 @@ __global__ void __launch_bounds__(256) k_intersect(IsectArgs a) {
     if ((threadIdx.x & 31u) == 0 && a.tri_tests) atomicAdd(a.tri_tests, tests);
 }
 
+// Per-ray candidates: one thread per (ray, cluster). A closest-hit ray skips a cluster whose sphere lies
+// beyond its current best hit.
+template <bool ANY>
+__global__ void __launch_bounds__(256) k_intersect_rays(IsectArgs a) {
+    const unsigned long long cc = *a.cand_count;
+    const unsigned long long count = cc < a.capacity ? cc : a.capacity;
+    const uint32_t n = dev_count(a.d_count, a.max_rays);
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long tests = 0;
+    for (unsigned long long c = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; c < count; c += stride) {
+        const unsigned long long cand = __ldg(a.cand + c);
+        const uint32_t k = (uint32_t)(cand >> 32), cluster = (uint32_t)cand & 0x7FFFFFFFu;
+        if (k >= n) continue;
+        const uint32_t id = a.sorted_ids ? __ldg(a.sorted_ids + k) : k;
+        if (id >= a.max_rays) continue;
+        float4 o, d;
+        load_ray(a.rays, id, o, d);
+        if (!(d.w > o.w)) continue;
+        if (ANY && *(volatile uint32_t*)(a.flags + id) == RSH_OCCLUDED) continue;
+        if (!ANY) {
+            const unsigned long long cur = *(volatile unsigned long long*)(a.hits + id);
+            if (cur != RSH_HIT_NONE) {
+                const float tb = __uint_as_float((uint32_t)(cur >> 32));
+                if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, fminf(d.w, tb), __ldg(a.spheres + cluster)))
+                    continue;
+            }
+        }
+        const RayWT r = wt_setup(o, d);
+        const uint32_t t0 = cluster * a.cluster;
+        const uint32_t t1 = (t0 + a.cluster < a.tri_count) ? t0 + a.cluster : a.tri_count;
+        unsigned long long best = RSH_HIT_NONE;
+        for (uint32_t t = t0; t < t1; ++t) {
+            const float4 v0 = __ldg(a.tris + 3ull * t);
+            const float4 v1 = __ldg(a.tris + 3ull * t + 1);
+            const float4 v2 = __ldg(a.tris + 3ull * t + 2);
+            float th;
+            ++tests;
+            if (wt_hit(r, v0, v1, v2, th)) {
+                if (ANY) {
+                    a.flags[id] = RSH_OCCLUDED;
+                    break;
+                }
+                const unsigned long long key = hit_key(th, __float_as_uint(v0.w));
+                best = key < best ? key : best;
+            }
+        }
+        if (!ANY && best != RSH_HIT_NONE) {
+            if (best < *(volatile unsigned long long*)(a.hits + id)) atomicMin(a.hits + id, best);
+        }
+    }
+#pragma unroll
+    for (int dd = 16; dd > 0; dd >>= 1) tests += __shfl_xor_sync(0xffffffffu, tests, dd);
+    if ((threadIdx.x & 31u) == 0 && a.tri_tests) atomicAdd(a.tri_tests, tests);
+}
+
 cudaError_t launch_intersect(const IsectArgs& a, bool any_hit, cudaStream_t s) {
     int sms = 152, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t grid = (uint32_t)sms * 8u;
-    if (any_hit) k_intersect<true><<<grid, 256, 0, s>>>(a);
-    else k_intersect<false><<<grid, 256, 0, s>>>(a);
+    if (a.per_ray) {
+        if (any_hit) k_intersect_rays<true><<<grid, 256, 0, s>>>(a);
+        else k_intersect_rays<false><<<grid, 256, 0, s>>>(a);
+    } else {
+        if (any_hit) k_intersect<true><<<grid, 256, 0, s>>>(a);
+        else k_intersect<false><<<grid, 256, 0, s>>>(a);
+    }
     note_launch();
     return cudaGetLastError();
 }

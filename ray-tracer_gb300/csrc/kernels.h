@@ -121,6 +121,10 @@ struct TravArgs {
     unsigned long long* cand_count;
     uint32_t* work;              // [0] = next unit, [1] = resume unit (min failed)
     uint32_t unit_end;           // units >= unit_end are left for a later pass
+    uint32_t ray_level;          // >= 1: rays descend individually at and below this object-tree level and
+                                 // emit per-ray candidates (sorted ray index << 32 | 1 << 31 | cluster)
+    const rsh_ray* rays;         // per-ray mode: the rays (by slot) and the sorted order
+    const uint32_t* sorted_ids;
     unsigned long long* node_tests;
     uint32_t* err;
 };
@@ -143,6 +147,7 @@ struct IsectArgs {
     uint32_t* flags;
     unsigned long long* hits;
     unsigned long long* tri_tests;
+    uint32_t per_ray;            // candidates are per ray (sorted ray index << 32 | 1 << 31 | cluster)
 };
 cudaError_t launch_intersect(const IsectArgs& a, bool any_hit, cudaStream_t s);
 

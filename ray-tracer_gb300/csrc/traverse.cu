@@ -13,15 +13,62 @@
 // compacted with a warp scan and one atomicAdd per warp; inner children are pushed. No dense
 // node x triangle matrix, no per-level host sync. If the candidate buffer fills, the warp records the
 // first unfinished work unit (atomicMin) and stops; the host drains the buffer and resumes there.
+// With ray_level >= 1, rays leave their packet at and below that object-tree level (and at once when the
+// packet's cone is wider than a half-space) and emit per-ray (ray, cluster) candidates instead.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "tests.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace rsh {
 
 namespace {
 constexpr int TV_WARPS = 4;
 constexpr int TV_STACK = 96;
+}
+
+// Appends one candidate with one atomic per group of lanes that reach this point together.
+RSH_DEV bool emit_candidate(const TravArgs& a, unsigned long long val) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(a.cand_count, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    const unsigned long long pos = base + g.thread_rank();
+    if (pos >= a.capacity) return false;
+    a.cand[pos] = val;
+    return true;
+}
+
+// A ray leaves its packet and descends the subtree of (L0, idx0) alone, testing every child sphere
+// against itself, and emits one candidate per cluster whose sphere it pierces. False: buffer full.
+RSH_DEV bool ray_emit(const TravArgs& a, uint32_t k, float4 o, float4 d, uint32_t L0, uint32_t idx0,
+                      unsigned long long& tests) {
+    uint32_t stk[72];
+    int sp = 0;
+    stk[sp++] = (L0 << 24) | idx0;
+    bool ok = true;
+    while (sp > 0) {
+        const uint32_t e = stk[--sp];
+        const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
+        const uint32_t cl = L - 1u;
+        const uint32_t first = (L == a.levels) ? 0u : 8u * idx;
+        const uint32_t size = a.lvl_size[cl];
+        const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+        const float4* sb = a.spheres + a.lvl_off[cl] + first;
+        for (uint32_t c = 0; c < cnt; ++c) {
+            ++tests;
+            if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, __ldg(sb + c))) continue;
+            if (cl == 0) {
+                ok = emit_candidate(a, ((unsigned long long)k << 32) | 0x80000000ull | (first + c)) && ok;
+            } else if (sp < 72) {
+                stk[sp++] = (cl << 24) | (first + c);
+            }
+        }
+    }
+    return ok;
 }
 
 __global__ void __launch_bounds__(TV_WARPS * 32) k_traverse(TravArgs a) {
@@ -60,6 +107,12 @@ __global__ void __launch_bounds__(TV_WARPS * 32) k_traverse(TravArgs a) {
         for (uint32_t g = 0; g < 4; ++g)
             mask |= (((b0 >> (8u * g)) & 1u) << (2u * g)) | (((b1 >> (8u * g)) & 1u) << (2u * g + 1u));
         if (mask == 0) continue;
+        const uint32_t f0 = __ballot_sync(0xffffffffu, v0 && !(P0.cs > 0.0f));
+        const uint32_t f1 = __ballot_sync(0xffffffffu, v1 && !(P1.cs > 0.0f));
+        uint32_t fullmask = 0;
+#pragma unroll
+        for (uint32_t g = 0; g < 4; ++g)
+            fullmask |= (((f0 >> (8u * g)) & 1u) << (2u * g)) | (((f1 >> (8u * g)) & 1u) << (2u * g + 1u));
         int sp = 0;
         if (lane == 0) stack[0] = (levels << 28) | mask;  // virtual root above the top level
         sp = 1;
@@ -69,7 +122,37 @@ __global__ void __launch_bounds__(TV_WARPS * 32) k_traverse(TravArgs a) {
             const uint32_t e = stack[sp - 1];
             __syncwarp();
             --sp;
-            const uint32_t L = e >> 28, idx = (e >> 8) & 0xFFFFFu, m = e & 0xFFu;
+            const uint32_t L = e >> 28, idx = (e >> 8) & 0xFFFFFu;
+            uint32_t m = e & 0xFFu;
+            if (a.ray_level > 0) {
+                // rays leave their packet below the switch level (at once for full cones) and emit
+                // per-ray candidates
+                const uint32_t m_ray = (L <= a.ray_level) ? m : (m & fullmask);
+                if (m_ray) {
+                    const uint32_t nr = __popc(m_ray) * P;
+                    bool ok = true;
+                    for (uint32_t ir = lane; ir < nr; ir += 32) {
+                        uint32_t pmm = m_ray;
+                        for (uint32_t s2 = 0; s2 < ir / P; ++s2) pmm &= pmm - 1u;
+                        const uint32_t k = 8u * u * P + (__ffs(pmm) - 1u) * P + (ir % P);
+                        if (k >= n) continue;
+                        const uint32_t id = a.sorted_ids ? __ldg(a.sorted_ids + k) : k;
+                        if (id >= a.max_rays) continue;
+                        float4 o, d;
+                        load_ray(a.rays, id, o, d);
+                        if (!(d.w > o.w)) continue;
+                        ok = ray_emit(a, k, o, d, L, idx, tests) && ok;
+                    }
+                    __syncwarp();
+                    if (__any_sync(0xffffffffu, !ok)) {
+                        failed = true;
+                        if (lane == 0) atomicMin(&a.work[1], u);
+                        break;
+                    }
+                    m &= ~m_ray;
+                    if (m == 0) continue;
+                }
+            }
             const uint32_t cl = L - 1u;
             const uint32_t first = (L == levels) ? 0u : 8u * idx;
             const uint32_t size = a.lvl_size[cl];

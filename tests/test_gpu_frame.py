@@ -68,9 +68,11 @@ def _check_frame(ctx, s, sc, W, H, depth, jitter):
     return st
 
 
+@pytest.mark.parametrize("ray_level", [0, 3])
 @pytest.mark.parametrize("jitter", [0.0, 1.0])
-def test_frame_cornell(cornell, jitter):
-    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, reflect_jitter=jitter)
+def test_frame_cornell(cornell, jitter, ray_level):
+    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, reflect_jitter=jitter,
+                      ray_level=ray_level)
     sc = ctx.scene(cornell.positions, cornell.normals, cornell.material_ids, cornell.materials)
     st = _check_frame(ctx, cornell, sc, 128, 96, 2, jitter)
     assert st["secondary_ms"] > 0
