@@ -424,6 +424,89 @@ def gpu_arm(args, s, rank, world, td):
     return out
 
 
+# ---------------------------------------------------------------- serving (continuous batching)
+def serving_bench(args):
+    """Poisson request arrivals over resident scenes through rsh_server_*: p50/p99 latency and Mrays/s,
+    next to the same requests rendered one by one through rsh_render_frame (a serial per-frame loop)."""
+    import ctypes as C
+
+    import rsh
+    from rsh import scenes
+
+    lib = rsh.load()
+    rng = np.random.default_rng([scenes.SEED_BASE + 4, 0])
+    n_scenes = args.serve_scenes
+    tris = np.exp(rng.uniform(np.log(50_000), np.log(1_000_000), n_scenes)).astype(int)
+    sd = [scenes.random_soup(int(t), np.random.default_rng([scenes.SEED_BASE + 4, 100 + i])) for i, t in enumerate(tris)]
+    ctx = rsh.Context(rsh.default_config(reflect_jitter=1.0))
+    scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]
+    res_choices = [(256, 256), (512, 512), (1920, 1080)][: args.serve_max_res]
+    reqs = []
+    for k in range(args.serve_requests):
+        si = int(rng.integers(0, n_scenes))
+        s = sd[si]
+        W, H = res_choices[int(rng.integers(0, len(res_choices)))]
+        ang = rng.uniform(0, 2 * np.pi)
+        eye = (60.0 * np.cos(ang), rng.uniform(-10, 30), 60.0 * np.sin(ang))
+        cam = rsh.camera_look_at(eye, (0, 0, 0), (0, 1, 0), 60.0, W, H)
+        nl = int(rng.integers(1, 5))
+        lights = [{"position": tuple(rng.uniform(-30, 30, 3))} for _ in range(nl)]
+        r = rsh.Request()
+        r.scene_index, r.camera, r.width, r.height = si, cam, W, H
+        r.depth, r.light_count = int(rng.integers(1, 4)), nl
+        arr = rsh.make_lights(lights)
+        for i in range(nl):
+            r.lights[i] = arr[i]
+        reqs.append(r)
+    gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
+    # serial per-frame loop (same requests, back to back)
+    t0 = time.perf_counter()
+    serial_rays = 0
+    for r in reqs:
+        ctx.set_camera(r.camera)
+        lib.rsh_lights_set(ctx.handle, r.lights, r.light_count)
+        rsh.check(lib.rsh_render_frame(ctx.handle, scs[r.scene_index].handle, r.width, r.height, r.depth, None, None),
+                  "render")
+        fs = rsh.FrameStats()
+        lib.rsh_frame_stats_get(ctx.handle, C.byref(fs))
+        serial_rays += fs.shadow_rays + fs.reflection_rays
+    serial_s = time.perf_counter() - t0
+    # the server: submit with Poisson gaps, then wait for all
+    arrs = (C.c_void_p * n_scenes)(*[s.handle for s in scs])
+    srv = C.c_void_p()
+    rsh.check(lib.rsh_server_create(ctx.handle, arrs, n_scenes, args.serve_budget_gb << 30, 64, C.byref(srv)), "srv")
+    ids = []
+    t0 = time.perf_counter()
+    for r, g in zip(reqs, gaps):
+        time.sleep(g)
+        i = C.c_uint64()
+        rsh.check(lib.rsh_server_submit(srv, C.byref(r), C.byref(i)), "submit")
+        ids.append(i.value)
+    lat, rays = [], 0
+    for i in ids:
+        rr = rsh.RequestResult()
+        st = lib.rsh_server_wait(srv, i, 600_000, C.byref(rr), None, None)
+        if st == rsh.RSH_OK:
+            lat.append(rr.finish_ms - rr.submit_ms)
+            rays += rr.rays
+    wall = time.perf_counter() - t0
+    stats = [C.c_uint64() for _ in range(4)]
+    lib.rsh_server_stats(srv, *[C.byref(x) for x in stats])
+    lib.rsh_server_destroy(srv)
+    for s in scs:
+        s.destroy()
+    ctx.destroy()
+    lat = np.array(lat)
+    return {"metric": "serving p50/p99 latency", "requests": len(reqs), "completed": int(len(lat)),
+            "arrival_rate_req_s": args.serve_rate, "p50_ms": round(float(np.percentile(lat, 50)), 2),
+            "p99_ms": round(float(np.percentile(lat, 99)), 2), "server_wall_s": round(wall, 3),
+            "server_mrays_s": round(rays / wall / 1e6, 3), "serial_wall_s": round(serial_s, 3),
+            "serial_mrays_s": round(serial_rays / serial_s / 1e6, 3),
+            "steps": stats[1].value, "peak_inflight": stats[2].value, "peak_bytes": stats[3].value,
+            "scenes_tris": [int(t) for t in tris]}
+
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -437,7 +520,16 @@ def main():
     ap.add_argument("--height", type=int, default=0, help="override the frame height (profiling runs)")
     ap.add_argument("--mode", default="all", choices=["all", "plain", "fused"],
                     help="all: plain + fused + e2e + stage timers; plain/fused: only that timed pass")
+    ap.add_argument("--serving", action="store_true", help="run the serving benchmark instead")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-scenes", type=int, default=8)
+    ap.add_argument("--serve-max-res", type=int, default=3)
+    ap.add_argument("--serve-budget-gb", type=int, default=32)
     args = ap.parse_args()
+    if args.serving:
+        print(json.dumps(serving_bench(args)))
+        return 0
     rank, world, td = dist_setup(args.gpus)
     s = make_workload(args.config)
     if args.width:

@@ -434,7 +434,7 @@ typedef struct rsh_request_result {
     uint64_t id;
     int32_t status;           /* rsh_status */
     double submit_ms, start_ms, finish_ms;   /* server clock */
-    uint64_t rays;            /* secondary rays traced */
+    uint64_t rays;            /* secondary (shadow + reflection) rays traced, after trimming */
 } rsh_request_result;
 
 /* A continuous-batching request loop on its own host thread: requests are admitted while their

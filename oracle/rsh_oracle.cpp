@@ -181,18 +181,18 @@ inline uint32_t f2u(float f) {
     return u;
 }
 
-// Per-ray filter against a cluster sphere before its triangle tests (same arithmetic as the GPU).
+// Per-ray test of a sphere (same arithmetic as the GPU): squared line distance against the squared radius
+// inflated by 1e-5 of the L1 distance plus radius, and the sphere's interval along the ray.
 inline bool ray_hits_sphere(const Ray& r, const float* s) {
     const float vx = s[0] - r.o[0], vy = s[1] - r.o[1], vz = s[2] - r.o[2];
     const float t = (vx * r.d[0] + vy * r.d[1]) + vz * r.d[2];
     const float wx = vy * r.d[2] - vz * r.d[1];
     const float wy = vz * r.d[0] - vx * r.d[2];
     const float wz = vx * r.d[1] - vy * r.d[0];
-    const float perp = std::sqrt((wx * wx + wy * wy) + wz * wz);
-    const float dist = std::sqrt((vx * vx + vy * vy) + vz * vz);
-    const float slack = (dist + s[3]) * 1e-5f;
+    const float perp2 = (wx * wx + wy * wy) + wz * wz;
+    const float slack = (((std::fabs(vx) + std::fabs(vy)) + std::fabs(vz)) + s[3]) * 1e-5f;
     const float rr = s[3] + slack;
-    if (perp > rr) return false;
+    if (perp2 > rr * rr) return false;
     if (t + rr < r.tmin) return false;
     if (t - rr > r.tmax) return false;
     return true;

@@ -143,11 +143,10 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
                                              nullptr});
         } else {
             const uint32_t b = q->stage - 1;
-            uint32_t lbits = 0;
-            while ((1u << lbits) < L) ++lbits;
-            HashP hp_s, hp_r;
-            RSH_TRY(make_hash_params(sc, s->ctx->cfg, lbits, hp_s));
+            // the batched call re-keys every segment itself, so the ray generators' keys are not used
+            HashP hp_r;
             RSH_TRY(make_hash_params(sc, s->ctx->cfg, 0, hp_r));
+            const HashP& hp_s = hp_r;
             LightsP lp{};
             lp.count = L;
             for (uint32_t l = 0; l < L; ++l)
@@ -163,6 +162,10 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
         }
     }
     RSH_TRY(rsh_batch_trace(s->ctx, segs.data(), (uint32_t)segs.size(), st));
+    // rays traced per segment (after trimming), read back with the step's synchronisation below
+    std::vector<uint32_t> seg_cnt(segs.size());
+    RSH_CUDA(cudaMemcpyAsync(seg_cnt.data(), s->ctx->bufs["b_seg_cnt"].ptr, 4 * segs.size(), cudaMemcpyDeviceToHost,
+                             st));
     // advance: resolve hits into the next surface
     for (Req* q : act) {
         const rsh_request& r = q->r;
@@ -176,10 +179,18 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
             const uint32_t b = q->stage - 1;
             RSH_CUDA(launch_resolve(sc->pos, sc->nrm, sc->mat, q->rrays[b & 1], q->hits + (size_t)b * npix, nullptr,
                                     npix, q->spos, q->snrm, st));
-            q->rays += (uint64_t)npix * (r.light_count + 1);
         }
     }
     RSH_CUDA(cudaStreamSynchronize(st));
+    size_t si = 0;
+    for (Req* q : act) {
+        if (q->stage == 0) {
+            si += 1;  // primary rays are not counted as secondary rays
+        } else {
+            q->rays += (uint64_t)seg_cnt[si] + seg_cnt[si + 1];
+            si += 2;
+        }
+    }
     return rsh_check_device_errors(s->ctx, st);
 }
 

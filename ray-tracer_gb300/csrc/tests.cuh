@@ -55,10 +55,11 @@ RSH_DEV bool node_hits_sphere(const NodeR& p, float4 s) {
     return true;
 }
 
-// Can ray (o, d, [tmin, tmax]) touch sphere s? Conservative per-ray filter applied before a cluster's
-// triangle tests: the distance from the sphere centre to the ray line (through a cross product) and the
-// parameter interval of the sphere along the ray, each with a 1e-5 relative slack for FP32 rounding
-// and |d| = 1 +- 1e-7. A miss here implies every triangle inside the sphere is missed.
+// Can ray (o, d, [tmin, tmax]) touch sphere s? Conservative per-ray test: the squared distance from the
+// sphere centre to the ray line (through a cross product) against the squared inflated radius, and the
+// sphere's parameter interval along the ray against [tmin, tmax]. The inflation is 1e-5 of the L1 distance
+// plus radius (an upper bound of the Euclidean one), which absorbs FP32 rounding and |d| = 1 +- 1e-7.
+// No square roots. A miss here implies every triangle inside the sphere is missed.
 RSH_DEV bool ray_hits_sphere(float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
                              float4 s) {
     const float vx = s.x - ox, vy = s.y - oy, vz = s.z - oz;
@@ -66,11 +67,10 @@ RSH_DEV bool ray_hits_sphere(float ox, float oy, float oz, float dx, float dy, f
     const float wx = vy * dz - vz * dy;
     const float wy = vz * dx - vx * dz;
     const float wz = vx * dy - vy * dx;
-    const float perp = sqrtf((wx * wx + wy * wy) + wz * wz);
-    const float dist = sqrtf((vx * vx + vy * vy) + vz * vz);
-    const float slack = (dist + s.w) * 1e-5f;
+    const float perp2 = (wx * wx + wy * wy) + wz * wz;
+    const float slack = (((fabsf(vx) + fabsf(vy)) + fabsf(vz)) + s.w) * 1e-5f;
     const float r = s.w + slack;
-    if (perp > r) return false;
+    if (perp2 > r * r) return false;
     if (t + r < tmin) return false;
     if (t - r > tmax) return false;
     return true;
