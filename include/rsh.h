@@ -148,6 +148,9 @@ typedef struct rsh_config {
 
 #define RSH_FLAG_STAGE_TIMERS 1u   /* record per-stage CUDA events (TestManager timers) */
 #define RSH_FLAG_FUSED 2u          /* rsh_render_frame traces each bounce through the batched form */
+#define RSH_FLAG_RAH 4u            /* plain path: ray-hierarchy ablation without hashing/sorting: packets
+                                      of consecutive trimmed rays (the reference's algorithm 1 "RAH",
+                                      main.cpp:1016-1037) */
 
 /* Per-frame statistics (TestManager::dump, TestManager.cpp:229-313, as a struct). */
 typedef struct rsh_frame_stats {

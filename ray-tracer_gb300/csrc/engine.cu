@@ -220,6 +220,15 @@ rsh_status trace_keyed(rsh_ctx* ctx, const rsh_scene* sc, const rsh_ray* rays, c
     RSH_CUDA(launch_compress(keys, n_slots, static_cast<uint32_t*>(trimmed), static_cast<uint32_t*>(ckeys),
                              static_cast<uint32_t*>(cbases), cnt, scr, ctx->d_err, s));
     stage_end(ctx, th, s);
+    if (ctx->cfg.flags & RSH_FLAG_RAH) {
+        // ablation: no sort, packets of consecutive trimmed rays (the reference's RAH path)
+        th = stage_begin(ctx, RSH_STAGE_BUILD, s);
+        RSH_CUDA(launch_build_rsh(rays, static_cast<uint32_t*>(trimmed), n_slots, cnt, P,
+                                  static_cast<rsh_node*>(nodes), s));
+        stage_end(ctx, th, s);
+        return traverse_and_intersect(ctx, sc, static_cast<rsh_node*>(nodes), rays,
+                                      static_cast<uint32_t*>(trimmed), n_slots, cnt, any_hit, flags, hits, s);
+    }
     th = stage_begin(ctx, RSH_STAGE_SORT, s);
     RSH_CUDA(launch_sort_pairs(static_cast<uint32_t*>(ckeys), nullptr, static_cast<uint32_t*>(skeys),
                                static_cast<uint32_t*>(svals), n_slots, cnt + 1, key_bits, scr, ctx->d_err, s));

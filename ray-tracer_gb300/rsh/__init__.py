@@ -25,6 +25,7 @@ HIT_NONE = 0xFFFFFFFFFFFFFFFF
 OCCLUDED = 0xFFFFFFFF
 FLAG_STAGE_TIMERS = 1
 FLAG_FUSED = 2
+FLAG_RAH = 4
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 NODE_DTYPE = np.dtype([("c", "<f4", 3), ("radius", "<f4"), ("axis", "<f4", 3), ("cos_spread", "<f4"),

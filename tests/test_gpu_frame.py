@@ -114,3 +114,26 @@ def test_fused_frame_equals_plain_frame():
         assert np.array_equal(a, b)
     assert outs[0][1]["shadow_rays"] == outs[1][1]["shadow_rays"]
     assert outs[0][1]["reflection_rays"] == outs[1][1]["reflection_rays"]
+
+
+@pytest.mark.parametrize("ray_level", [0, 3])
+def test_rah_ablation_same_results_more_work(cornell, ray_level):
+    """RAH (no hashing/sorting, main.cpp:1016-1037) gives the same hits and flags as CRSH; with packets the
+    unsorted rays make wider cones, so the traversal does more node tests (the thesis' CRSH vs RAH
+    comparison, Thesis_Evaluation.tex:217-219)."""
+    W, H = 128, 128
+    res = {}
+    for flags in (0, rsh.FLAG_RAH):
+        ctx = rsh.Context(grid_bits=5, dir_log2=5, packet_size=8, cluster_size=8, flags=flags, ray_level=ray_level)
+        sc = ctx.scene(cornell.positions, cornell.normals, cornell.material_ids, cornell.materials)
+        ctx.set_camera(rsh.camera_look_at(cornell.eye, cornell.target, cornell.up, cornell.fov, W, H))
+        ctx.set_lights(cornell.lights)
+        ctx.render(sc, W, H, 2)
+        st = ctx.stats()
+        res[flags] = ([ctx.frame_hits(b, W * H) for b in range(2)] + [ctx.frame_shadow(b, W * H) for b in range(2)], st)
+        sc.destroy()
+        ctx.destroy()
+    for a, b in zip(res[0][0], res[rsh.FLAG_RAH][0]):
+        assert np.array_equal(a, b)
+    if ray_level == 0:
+        assert res[rsh.FLAG_RAH][1]["node_tests"] > res[0][1]["node_tests"]
