@@ -378,7 +378,9 @@ def gpu_arm(args, s, rank, world, td):
             try:
                 tr = json.loads(prof.read_text())
                 if roof["kernel"] in tr:
-                    roof["traffic"] = tr[roof["kernel"]]
+                    ent = tr[roof["kernel"]]
+                    roof["traffic"] = ent["bytes_per_launch"]
+                    roof["traffic_note"] = f"ncu dram read+write bytes of one launch, {ent['workload']}"
             except Exception:
                 pass
     out = {
