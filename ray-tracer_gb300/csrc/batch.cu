@@ -186,6 +186,10 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         p.flags = g.flags;
         p.hits = reinterpret_cast<unsigned long long*>(g.hits);
         RSH_TRY(make_hash_params(sc, ctx->cfg, 0, p.hp));
+        if (sc->h.level_size[0] > (1u << 23)) {  // per-ray job words hold a level-1 node index in 20 bits
+            set_error("batched traversal supports at most 8,388,608 triangle clusters per scene");
+            return RSH_ERR_INVALID;
+        }
         FusedSeg& f = pl.h_fsegs[s];
         std::memset(&f, 0, sizeof(f));
         f.spheres = sc->h.spheres;

@@ -82,6 +82,11 @@ RSH_DEV uint32_t ld_relaxed_u32(const uint32_t* p) {
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+RSH_DEV unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 
 RSH_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
 RSH_DEV uint32_t lanemask_lt() {

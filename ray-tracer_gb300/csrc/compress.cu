@@ -32,6 +32,22 @@ RSH_DEV Summ combine(const Summ& a, const Summ& b) {
     r.last = b.n > 0u ? b.last : a.last;
     return r;
 }
+RSH_DEV Summ shfl_down(const Summ& s, int d) {
+    Summ r;
+    r.n = __shfl_down_sync(0xffffffffu, s.n, d);
+    r.h = __shfl_down_sync(0xffffffffu, s.h, d);
+    r.first = __shfl_down_sync(0xffffffffu, s.first, d);
+    r.last = __shfl_down_sync(0xffffffffu, s.last, d);
+    return r;
+}
+RSH_DEV Summ shfl_idx0(const Summ& s) {
+    Summ r;
+    r.n = __shfl_sync(0xffffffffu, s.n, 0);
+    r.h = __shfl_sync(0xffffffffu, s.h, 0);
+    r.first = __shfl_sync(0xffffffffu, s.first, 0);
+    r.last = __shfl_sync(0xffffffffu, s.last, 0);
+    return r;
+}
 RSH_DEV Summ shfl_up(const Summ& s, int d) {
     Summ r;
     r.n = __shfl_up_sync(0xffffffffu, s.n, d);
@@ -75,7 +91,7 @@ k_compress(const uint32_t* __restrict__ keys, uint32_t n_slots, uint32_t num_til
     __shared__ uint32_t s_ckey[CT_TILE];
     __shared__ uint32_t s_cbase[CT_TILE];
     __shared__ Summ s_warp[CT_THREADS / 32];
-    __shared__ Summ s_prefix;
+    __shared__ Summ s_prefix, s_run;
     __shared__ uint32_t s_tile, s_tn, s_th;
 
     if (threadIdx.x == 0) s_tile = atomicAdd(sc.ticket, 1u);
@@ -134,37 +150,56 @@ k_compress(const uint32_t* __restrict__ keys, uint32_t n_slots, uint32_t num_til
             s_warp[w] = run;
             run = combine(run, wv);
         }
-        // decoupled look-back
+        s_run = run;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // decoupled look-back, 32 predecessors per step: lane l reads tile j - l; the window is folded
+        // (oldest first) up to the newest predecessor that already holds its inclusive prefix
+        const Summ run = s_run;
         Summ excl{0u, 0u, 0u, 0u};
         if (tile == 0) {
-            publish(sc.inc, sc.flags, 2u, run);
+            if (lane == 0) publish(sc.inc, sc.flags, 2u, run);
         } else {
-            publish(sc.agg + 4ull * tile, sc.flags + tile, 1u, run);
+            if (lane == 0) publish(sc.agg + 4ull * tile, sc.flags + tile, 1u, run);
             int64_t j = (int64_t)tile - 1;
             uint32_t spins = 0;
             while (j >= 0) {
-                uint32_t f = ld_acquire_u32(sc.flags + j);
-                if (f == 0u) {
+                const int64_t idx = j - (int64_t)lane;
+                const uint32_t f = idx >= 0 ? ld_acquire_u32(sc.flags + idx) : 2u;
+                const uint32_t incl = __ballot_sync(0xffffffffu, f == 2u);
+                const uint32_t lim = incl ? (uint32_t)(__ffs(incl) - 1) : 31u;
+                const uint32_t upto = lim == 31u ? 0xffffffffu : ((2u << lim) - 1u);
+                if (__ballot_sync(0xffffffffu, f == 0u) & upto) {
                     if (++spins > RSH_SPIN_LIMIT) {
                         raise_device_error(err, RSH_DEVERR_TIMEOUT);
                         break;
                     }
-                    if (spins > 64) __nanosleep(64);
+                    if (spins > 16) __nanosleep(32);
                     continue;
                 }
-                Summ p = read4((f == 2u ? sc.inc : sc.agg) + 4ull * j);
-                excl = combine(p, excl);
-                if (f == 2u) break;
-                --j;
+                Summ v{0u, 0u, 0u, 0u};
+                if (lane <= lim && idx >= 0) v = read4((f == 2u ? sc.inc : sc.agg) + 4ull * idx);
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const Summ o = shfl_down(v, d);
+                    if ((lane & (2u * d - 1u)) == 0u) v = combine(o, v);
+                }
+                v = shfl_idx0(v);
+                excl = combine(v, excl);
+                if (incl) break;
+                j -= 32;
             }
-            publish(sc.inc + 4ull * tile, sc.flags + tile, 2u, combine(excl, run));
+            if (lane == 0) publish(sc.inc + 4ull * tile, sc.flags + tile, 2u, combine(excl, run));
         }
-        s_prefix = excl;
-        if (tile == num_tiles - 1) {
-            const Summ tot = combine(excl, run);
-            counts[0] = tot.n < n_slots ? tot.n : n_slots;
-            counts[1] = tot.h < n_slots ? tot.h : n_slots;
-            chunk_bases[counts[1]] = counts[0];
+        if (lane == 0) {
+            s_prefix = excl;
+            if (tile == num_tiles - 1) {
+                const Summ tot = combine(excl, run);
+                counts[0] = tot.n < n_slots ? tot.n : n_slots;
+                counts[1] = tot.h < n_slots ? tot.h : n_slots;
+                chunk_bases[counts[1]] = counts[0];
+            }
         }
     }
     __syncthreads();

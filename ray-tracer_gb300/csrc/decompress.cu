@@ -31,7 +31,7 @@ k_dc_scan(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
           const uint32_t* __restrict__ counts, uint32_t max_chunks, uint32_t* __restrict__ off,
           unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* err) {
     __shared__ uint32_t s_warp[DS_THREADS / 32];
-    __shared__ uint32_t s_tile, s_excl;
+    __shared__ uint32_t s_tile, s_excl, s_tot;
     const uint32_t C = counts[1] < max_chunks ? counts[1] : max_chunks;
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
@@ -68,32 +68,47 @@ k_dc_scan(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
             s_warp[w] = r;
             r += t;
         }
+        s_tot = r;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // decoupled look-back, 32 predecessors per step (lane l reads tile j - l), summing up to the
+        // newest predecessor that already holds its inclusive prefix
+        const uint32_t r = s_tot;
         unsigned long long* st = status + tile;
         uint32_t excl = 0;
         if (tile == 0) {
-            st_release_u64(st, F_PRE | r);
+            if (lane == 0) st_release_u64(st, F_PRE | r);
         } else {
-            st_release_u64(st, F_AGG | r);
+            if (lane == 0) st_release_u64(st, F_AGG | r);
             int64_t j = (int64_t)tile - 1;
             uint32_t spins = 0;
             while (j >= 0) {
-                const unsigned long long s = ld_acquire_u64(status + j);
+                const int64_t idx = j - (int64_t)lane;
+                // flag and value share one word, so a relaxed load suffices
+                const unsigned long long s = idx >= 0 ? ld_relaxed_u64(status + idx) : F_PRE;
                 const unsigned long long f = s & ~V_MASK;
-                if (f == 0ull) {
+                const uint32_t pre = __ballot_sync(0xffffffffu, f == F_PRE);
+                const uint32_t lim = pre ? (uint32_t)(__ffs(pre) - 1) : 31u;
+                const uint32_t upto = lim == 31u ? 0xffffffffu : ((2u << lim) - 1u);
+                if (__ballot_sync(0xffffffffu, f == 0ull) & upto) {
                     if (++spins > RSH_SPIN_LIMIT) {
                         raise_device_error(err, RSH_DEVERR_TIMEOUT);
                         break;
                     }
-                    if (spins > 64) __nanosleep(32);
+                    if (spins > 16) __nanosleep(32);
                     continue;
                 }
-                excl += (uint32_t)(s & V_MASK);
-                if (f == F_PRE) break;
-                --j;
+                uint32_t v = lane <= lim ? (uint32_t)(s & V_MASK) : 0u;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+                excl += v;
+                if (pre) break;
+                j -= 32;
             }
-            st_release_u64(st, F_PRE | (unsigned long long)(excl + r));
+            if (lane == 0) st_release_u64(st, F_PRE | (unsigned long long)(excl + r));
         }
-        s_excl = excl;
+        if (lane == 0) s_excl = excl;
     }
     __syncthreads();
     uint32_t run = s_excl + s_warp[warp] + inc - tsum;

@@ -26,6 +26,9 @@ constexpr int FW = 4;            // warps per block
 constexpr int F_STACK = 96;
 constexpr int F_MAXK = 32;       // max cluster size staged in shared memory
 constexpr uint32_t INVALID_ID = 0xFFFFFFFFu;
+constexpr int J_STACK = 96;                // per-lane node stack of a job
+constexpr uint32_t J_CAP = 512;            // job queue entries per warp
+constexpr uint32_t J_DRAIN = 128;          // queue length at which the packet walk stops to run the jobs
 }
 
 template <int P>
@@ -40,6 +43,8 @@ struct FusedSmem {
     unsigned long long best[8 * P];
     float4 tri[F_MAXK * 3];
     uint32_t stack[F_STACK];
+    uint32_t jobs[J_CAP];
+    uint32_t qn;                  // jobs queued
 };
 
 RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
@@ -51,91 +56,141 @@ RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
     return lo;
 }
 
-// Per-ray descent of one object-tree node's subtree: the ray leaves its packet and walks the subtree
-// alone, nearest child first, culling spheres against its own running closest-hit distance. Triangle
-// tests keep the ray's original interval and the key comparison, so ties still resolve to the smaller id.
+// Per-ray jobs. A job is one ray and one object-tree node whose subtree the ray walks alone, nearest
+// child first (job word: ray index | level << 8 | node index << 12). The warp keeps a queue of jobs in
+// shared memory and runs it with all 32 lanes: a lane without a job takes the next one from the queue,
+// and every iteration each busy lane makes ONE bounded step -- pop a node and test its (up to 8)
+// children's spheres, pushing the hits farthest first, or pop a triangle cluster and test its
+// triangles. Lanes never wait for another lane's whole ray, only for one step.
+//   closest hit: a hit updates the ray's shared best (atomicMin) at once, and every step re-reads it, so
+//     jobs of the same ray running on other lanes cull with it too; triangle tests keep the ray's
+//     original interval and the key comparison, so ties still resolve to the smaller triangle id;
+//   any hit: an occluding hit sets the ray's occluded bit, which ends its other jobs at their next step.
+
+RSH_DEV uint32_t job_word(uint32_t i, uint32_t L, uint32_t idx) { return i | (L << 8) | (idx << 12); }
+
 template <int P>
-RSH_DEV void ray_descend(FusedSmem<P>& S, uint32_t i, const FusedSeg& sg, uint32_t L0, uint32_t idx0, bool any,
-                         unsigned long long& ntests, unsigned long long& ttests) {
-    const float4 o = S.ro[i], d = S.rd[i], sh = S.rs[i];
-    const uint32_t meta = S.meta[i];
-    RayWT w;
-    w.ox = o.x;
-    w.oy = o.y;
-    w.oz = o.z;
-    w.tmin = o.w;
-    w.sx = sh.x;
-    w.sy = sh.y;
-    w.sz = sh.z;
-    w.tmax = sh.w;
-    w.kx = meta & 3u;
-    w.ky = (meta >> 2) & 3u;
-    w.kz = (meta >> 4) & 3u;
-    unsigned long long best = S.best[i];
-    float tcur = sh.w;
-    if (best != RSH_HIT_NONE) tcur = fminf(tcur, __uint_as_float((uint32_t)(best >> 32)));
-    uint32_t stk[72];
+RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t lane, unsigned long long& ntests,
+                      unsigned long long& ttests, uint32_t* err) {
+    const uint32_t qn = S.qn;
+    uint32_t qh = 0;
+    bool has = false;
+    uint32_t i = 0;
     int sp = 0;
-    stk[sp++] = (L0 << 24) | idx0;
-    bool occl = false;
-    while (sp > 0 && !occl) {
-        const uint32_t e = stk[--sp];
-        const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
-        const uint32_t cl = L - 1u;
-        const uint32_t first = (L == sg.levels) ? 0u : 8u * idx;
-        const uint32_t size = sg.lvl_size[cl];
-        const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
-        const float4* sb = sg.spheres + sg.lvl_off[cl] + first;
-        if (cl == 0) {
-            for (uint32_t c = 0; c < cnt && !occl; ++c) {
-                ++ntests;
-                if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, tcur, __ldg(sb + c))) continue;
-                const uint32_t t0 = (first + c) * sg.cluster;
+    uint32_t stk[J_STACK];
+    float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f, tmin = 0.f, tcur = 0.f;
+    RayWT w;
+    unsigned long long best = RSH_HIT_NONE;
+    for (;;) {
+        // lanes without a job take the next ones in queue order
+        const uint32_t need = __ballot_sync(0xffffffffu, !has);
+        if (need) {
+            const uint32_t my = qh + __popc(need & lanemask_lt());
+            qh += __popc(need);
+            if (!has && my < qn) {
+                const uint32_t job = S.jobs[my];
+                i = job & 255u;
+                const uint32_t mt = S.meta[i];
+                if (!(any && (mt & 128u))) {
+                    const float4 o = S.ro[i], d = S.rd[i], sh = S.rs[i];
+                    ox = o.x;
+                    oy = o.y;
+                    oz = o.z;
+                    tmin = o.w;
+                    dx = d.x;
+                    dy = d.y;
+                    dz = d.z;
+                    w.ox = o.x;
+                    w.oy = o.y;
+                    w.oz = o.z;
+                    w.tmin = o.w;
+                    w.sx = sh.x;
+                    w.sy = sh.y;
+                    w.sz = sh.z;
+                    w.tmax = sh.w;
+                    w.kx = mt & 3u;
+                    w.ky = (mt >> 2) & 3u;
+                    w.kz = (mt >> 4) & 3u;
+                    tcur = sh.w;
+                    best = RSH_HIT_NONE;
+                    stk[0] = (((job >> 8) & 15u) << 24) | (job >> 12);
+                    sp = 1;
+                    has = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, has)) break;
+        if (!has) continue;
+        // what other jobs of this ray found so far
+        if (any) {
+            if (*(volatile uint32_t*)&S.meta[i] & 128u) sp = 0;
+        } else {
+            const unsigned long long b = *(volatile unsigned long long*)&S.best[i];
+            if (b < best) {
+                best = b;
+                tcur = fminf(tcur, __uint_as_float((uint32_t)(b >> 32)));
+            }
+        }
+        if (sp > 0) {
+            const uint32_t e = stk[--sp];
+            const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
+            if (L == 0u) {
+                const uint32_t t0 = idx * sg.cluster;
                 const uint32_t t1 = (t0 + sg.cluster < sg.tri_count) ? t0 + sg.cluster : sg.tri_count;
-                for (uint32_t t = t0; t < t1; ++t) {
-                    const float4 v0 = __ldg(sg.tris + 3ull * t), v1 = __ldg(sg.tris + 3ull * t + 1),
-                                 v2 = __ldg(sg.tris + 3ull * t + 2);
+                for (uint32_t tt = t0; tt < t1; ++tt) {
+                    const float4 v0 = __ldg(sg.tris + 3ull * tt), v1 = __ldg(sg.tris + 3ull * tt + 1),
+                                 v2 = __ldg(sg.tris + 3ull * tt + 2);
                     float th;
                     ++ttests;
                     if (wt_hit(w, v0, v1, v2, th)) {
                         if (any) {
-                            occl = true;
+                            atomicOr(&S.meta[i], 128u);
+                            sp = 0;
                             break;
                         }
                         const unsigned long long key = hit_key(th, __float_as_uint(v0.w));
                         if (key < best) {
                             best = key;
                             tcur = fminf(tcur, th);
+                            atomicMin(&S.best[i], key);
                         }
                     }
                 }
-            }
-        } else {
-            float te[8];
-            uint32_t ci[8];
-            uint32_t nh = 0;
-            for (uint32_t c = 0; c < cnt; ++c) {
-                const float4 q = __ldg(sb + c);
-                ++ntests;
-                if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, tcur, q)) continue;
-                const float tc = ((q.x - o.x) * d.x + (q.y - o.y) * d.y) + (q.z - o.z) * d.z - q.w;
-                uint32_t k = nh++;  // keep te[] sorted descending (farthest first)
-                while (k > 0 && te[k - 1] < tc) {
-                    te[k] = te[k - 1];
-                    ci[k] = ci[k - 1];
-                    --k;
+            } else {
+                const uint32_t cl = L - 1u;
+                const uint32_t first = (L == sg.levels) ? 0u : 8u * idx;
+                const uint32_t size = sg.lvl_size[cl];
+                const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+                const float4* sb = sg.spheres + sg.lvl_off[cl] + first;
+                float te[8];
+                uint32_t ci[8];
+                uint32_t nh = 0;
+                for (uint32_t c = 0; c < cnt; ++c) {
+                    const float4 q = __ldg(sb + c);
+                    ++ntests;
+                    if (!ray_hits_sphere(ox, oy, oz, dx, dy, dz, tmin, tcur, q)) continue;
+                    const float tc = ((q.x - ox) * dx + (q.y - oy) * dy) + (q.z - oz) * dz - q.w;
+                    uint32_t k = nh++;  // keep te[] sorted descending (farthest first)
+                    while (k > 0 && te[k - 1] < tc) {
+                        te[k] = te[k - 1];
+                        ci[k] = ci[k - 1];
+                        --k;
+                    }
+                    te[k] = tc;
+                    ci[k] = first + c;
                 }
-                te[k] = tc;
-                ci[k] = first + c;
+                if (sp + (int)nh > J_STACK) {
+                    raise_device_error(err, RSH_DEVERR_OVERFLOW);
+                    nh = 0;
+                }
+                for (uint32_t k = 0; k < nh; ++k) stk[sp++] = (cl << 24) | ci[k];
             }
-            for (uint32_t k = 0; k < nh && sp < 72; ++k) stk[sp++] = (cl << 24) | ci[k];
         }
+        if (sp == 0) has = false;
     }
-    if (any) {
-        if (occl) atomicOr(&S.meta[i], 128u);
-    } else if (best < S.best[i]) {
-        S.best[i] = best;
-    }
+    __syncwarp();
+    if (lane == 0) S.qn = 0;
+    __syncwarp();
 }
 
 // After rays were tested: retire fully occluded packets (any hit) or shrink each packet's reach to
@@ -186,6 +241,8 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
     const uint32_t units = dev_count(a.d_units, a.units_max);
     unsigned long long ntests = 0, ttests = 0;
     constexpr uint32_t R = 8 * P;
+    if (lane == 0) S.qn = 0;
+    __syncwarp();
 
     for (;;) {
         uint32_t u = 0;
@@ -260,17 +317,37 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
                 // switch level, and at once for packets whose cone is wider than a half-space
                 const uint32_t m_ray = (L <= a.ray_level) ? m : (m & fullmask);
                 if (m_ray) {
+                    // queue one job per live ray of these packets; run the queue once it is long enough
+                    // to keep every lane busy (or would overflow)
                     const uint32_t nr = __popc(m_ray) * P;
-                    for (uint32_t ir = lane; ir < nr; ir += 32) {
-                        uint32_t pmm = m_ray;
-                        for (uint32_t s2 = 0; s2 < ir / P; ++s2) pmm &= pmm - 1u;
-                        const uint32_t i = (__ffs(pmm) - 1u) * P + (ir % P);
-                        const uint32_t mt = S.meta[i];
-                        if (!(mt & 64u) || (any && (mt & 128u))) continue;
-                        ray_descend<P>(S, i, sg, L, idx, any, ntests, ttests);
+                    if (S.qn + nr > J_CAP) {
+                        run_jobs<P>(S, sg, any, lane, ntests, ttests, a.err);
+                        refresh_packets<P>(S, any, q, ch, alive, P0, P1);
+                    }
+                    uint32_t qn = S.qn;
+                    __syncwarp();
+                    for (uint32_t base = 0; base < nr; base += 32) {
+                        const uint32_t ir = base + lane;
+                        bool push = false;
+                        uint32_t i = 0;
+                        if (ir < nr) {
+                            uint32_t pmm = m_ray;
+                            for (uint32_t s2 = 0; s2 < ir / P; ++s2) pmm &= pmm - 1u;
+                            i = (__ffs(pmm) - 1u) * P + (ir % P);
+                            const uint32_t mt = S.meta[i];
+                            push = (mt & 64u) && !(any && (mt & 128u)) && ((alive >> (i / P)) & 1u);
+                        }
+                        const uint32_t bl = __ballot_sync(0xffffffffu, push);
+                        if (push) S.jobs[qn + __popc(bl & lanemask_lt())] = job_word(i, L, idx);
+                        qn += __popc(bl);
                     }
                     __syncwarp();
-                    refresh_packets<P>(S, any, q, ch, alive, P0, P1);
+                    if (lane == 0) S.qn = qn;
+                    __syncwarp();
+                    if (qn >= J_DRAIN) {
+                        run_jobs<P>(S, sg, any, lane, ntests, ttests, a.err);
+                        refresh_packets<P>(S, any, q, ch, alive, P0, P1);
+                    }
                     m &= ~m_ray & alive;
                     if (alive == 0) break;
                     if (m == 0) continue;
@@ -384,6 +461,7 @@ __global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
                 }
                 if (alive == 0) break;
             }
+            if (S.qn) run_jobs<P>(S, sg, any, lane, ntests, ttests, a.err);
         }
         __syncwarp();
         // ---- results (each ray belongs to exactly one unit)

@@ -26,14 +26,23 @@ constexpr uint32_t VAL_MASK = (1u << 30) - 1u;
 inline uint32_t num_passes(uint32_t key_bits) { return key_bits == 0 ? 1u : (key_bits + 7u) / 8u; }
 }  // namespace
 
-// --- histograms of every pass in one read
+// --- histograms of every pass in one read; also clears the look-back status rows of the tiles that
+// the passes will use (ceil(n / SR_TILE) rows of 256 words per pass, pass stride `stride` words)
 __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
                             const uint32_t* __restrict__ d_count, uint32_t passes,
-                            uint32_t* __restrict__ hist) {
+                            uint32_t* __restrict__ hist, uint32_t* __restrict__ status, size_t stride) {
     __shared__ uint32_t sh[4][256];
     for (uint32_t i = threadIdx.x; i < 4u * 256u; i += blockDim.x) (&sh[0][0])[i] = 0u;
     __syncthreads();
     const uint32_t n = dev_count(d_count, n_max);
+    {
+        const size_t words = (size_t)((n + SR_TILE - 1) / SR_TILE) * 256u;  // multiple of 4
+        const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
+        for (uint32_t p = 0; p < passes; ++p) {
+            uint4* row = reinterpret_cast<uint4*>(status + p * stride);
+            for (size_t i = tid; i < words / 4; i += nth) row[i] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t k = __ldg(keys + i);
         for (uint32_t p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8u * p)) & 255u], 1u);
@@ -155,25 +164,42 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
         __syncthreads();
         gex = s_scan[warp] + x - hv;
     }
-    // decoupled look-back for this digit
+    // decoupled look-back for this digit, LB predecessors per step: their status words are loaded
+    // together (flag and count share one word, so relaxed loads suffice) and folded newest first up to
+    // the first one holding an inclusive prefix; a not-yet-published word restarts the step there
     uint32_t excl = 0u;
     if (tile > 0) {
+        constexpr int LB = 8;
         int64_t j = (int64_t)tile - 1;
         uint32_t spins = 0;
         while (j >= 0) {
-            const uint32_t s = ld_acquire_u32(status + (size_t)j * 256u + dg);
-            const uint32_t f = s & ~VAL_MASK;
-            if (f == 0u) {
+            uint32_t sv[LB];
+#pragma unroll
+            for (int q = 0; q < LB; ++q)
+                sv[q] = (j - q >= 0) ? ld_relaxed_u32(status + (size_t)(j - q) * 256u + dg) : FLAG_PRE;
+            int used = 0;
+            bool done = false, stall = false;
+#pragma unroll
+            for (int q = 0; q < LB; ++q) {
+                if (done || stall) continue;
+                const uint32_t f = sv[q] & ~VAL_MASK;
+                if (f == 0u) {
+                    stall = true;
+                    continue;
+                }
+                excl += sv[q] & VAL_MASK;
+                ++used;
+                if (f == FLAG_PRE) done = true;
+            }
+            if (done) break;
+            j -= used;
+            if (stall) {
                 if (++spins > RSH_SPIN_LIMIT) {
                     raise_device_error(err, RSH_DEVERR_TIMEOUT);
                     break;
                 }
-                if (spins > 64) __nanosleep(32);
-                continue;
+                if (spins > 16) __nanosleep(32);
             }
-            excl += s & VAL_MASK;
-            if (f == FLAG_PRE) break;
-            --j;
         }
         st_release_u32(st, FLAG_PRE | (excl + tcount));
     }
@@ -223,9 +249,9 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
     uint32_t* alt_keys = status + passes * tiles * 256;
     alt_keys = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(alt_keys) + 255) & ~uintptr_t(255));
     uint32_t* alt_vals = alt_keys + n_max;
-    cudaError_t e = cudaMemsetAsync(w, 0, (4 * 256 + 8 + passes * tiles * 256) * sizeof(uint32_t), s);
+    cudaError_t e = cudaMemsetAsync(w, 0, (4 * 256 + 8) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    k_sort_hist<<<152 * 2, 256, 0, s>>>(keys_in, n_max, d_count, passes, hist);
+    k_sort_hist<<<152 * 2, 256, 0, s>>>(keys_in, n_max, d_count, passes, hist, status, tiles * 256);
     note_launch();
     // ping-pong so that the last pass lands in the output
     const uint32_t* ki = keys_in;
