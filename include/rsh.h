@@ -294,7 +294,7 @@ rsh_status rsh_raygen_reflect(const float* surface_pos, const float* surface_nrm
 rsh_status rsh_hash(const rsh_ray* rays, uint32_t n, const rsh_hash_params* hp, uint32_t tag,
                     uint32_t* keys, rsh_stream_t stream);
 
-/* Trim + compress in one pass (decoupled look-back): keeps slots whose key != RSH_KEY_NONE in slot
+/* Trim + compress (reduce-then-scan over 4096-slot tiles): keeps slots whose key != RSH_KEY_NONE in slot
  * order (trimmed_ids = their slot indices), and cuts the trimmed keys into runs of equal keys.
  * Outputs chunk_keys[c], chunk_bases[c] (trimmed index of the run head; chunk_bases[C] = R) and, if
  * non-NULL, chunk_sizes[c]; counts[0] = R (rays), counts[1] = C (chunks), device memory.
@@ -307,7 +307,7 @@ rsh_status rsh_compress(rsh_ctx* ctx, const uint32_t* keys, uint32_t n_slots, ui
 /* rsh_compress without allocating: same outputs and semantics, no context, no cudaMalloc/cudaFree.
  * For callers that may not allocate device memory themselves or let a library do it: hosts that own and
  * pre-partition all device memory, and loops that allocate once at start-up and must not allocate while
- * they run. No counterpart in the reference. The look-back scratch is a static device array of 196,684 bytes that every GPU loading the
+ * they run. No counterpart in the reference. The scratch (per-tile summaries and prefixes) is a static device array of 196,684 bytes that every GPU loading the
  * library keeps until the process exits; n_slots above 16,777,216 is rejected with RSH_ERR_INVALID. The
  * first call on a device looks up the array's device address (call it once before any stream capture).
  * All calls share the array: calls that overlap on the GPU race, so serialise them on one stream. */

@@ -7,11 +7,14 @@
 //   compress / sort / decompress over all keys at once (the segment tag is the top key digit, so the
 //                    sorted order is segment-major: a segmented sort for free);
 //   k_batch_bounds   per-segment ray ranges of the sorted order (binary search on the tag), padded so
-//                    that no level-1 ray node straddles two segments;
+//                    that no level-1 ray node straddles two segments, laid out in schedule order:
+//                    closest-hit segments before any-hit ones, larger before smaller, so the work
+//                    units handed out last (the launch's tail) are the cheap ones;
 //   k_batch_pad      padded ray order (empty slots = inactive rays);
 //   build            ray-space hierarchy over the padded order;
 //   fused            ONE persistent traversal + intersection launch over every segment's work units.
 // Nothing reads a count back to the host, so the whole sequence is captured in a CUDA graph.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <map>
@@ -64,7 +67,8 @@ __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, ui
 __global__ void k_batch_bounds(const uint32_t* __restrict__ sorted_keys, const uint32_t* __restrict__ counts,
                                uint32_t nseg, uint32_t tag_shift, uint32_t unit_rays, uint32_t* __restrict__ seg_begin,
                                uint32_t* __restrict__ seg_cnt, uint32_t* __restrict__ pstart,
-                               FusedSeg* __restrict__ fsegs, uint32_t* __restrict__ totals) {
+                               const uint32_t* __restrict__ sched, FusedSeg* __restrict__ fsegs,
+                               uint32_t* __restrict__ totals) {
     const uint32_t R = counts[0];
     for (uint32_t s = threadIdx.x; s < nseg; s += blockDim.x) {
         auto lower = [&](uint32_t key) {
@@ -82,10 +86,11 @@ __global__ void k_batch_bounds(const uint32_t* __restrict__ sorted_keys, const u
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (uint32_t s = 0; s < nseg; ++s) {
-            pstart[s] = acc;
-            fsegs[s].unit_begin = acc / unit_rays;
+        uint32_t acc = 0;  // padded layout in schedule order: position k holds segment sched[k]
+        for (uint32_t k = 0; k < nseg; ++k) {
+            const uint32_t s = sched[k];
+            pstart[k] = acc;
+            fsegs[k].unit_begin = acc / unit_rays;
             acc += ((seg_cnt[s] + unit_rays - 1) / unit_rays) * unit_rays;
         }
         pstart[nseg] = acc;
@@ -95,17 +100,19 @@ __global__ void k_batch_bounds(const uint32_t* __restrict__ sorted_keys, const u
 }
 
 __global__ void k_batch_pad(const uint32_t* __restrict__ sorted_ids, const uint32_t* __restrict__ seg_begin,
-                            const uint32_t* __restrict__ seg_cnt, const uint32_t* __restrict__ pstart, uint32_t nseg,
-                            uint32_t max_padded, const uint32_t* __restrict__ totals, uint32_t* __restrict__ padded) {
+                            const uint32_t* __restrict__ seg_cnt, const uint32_t* __restrict__ pstart,
+                            const uint32_t* __restrict__ sched, uint32_t nseg, uint32_t max_padded,
+                            const uint32_t* __restrict__ totals, uint32_t* __restrict__ padded) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= max_padded || q >= totals[0]) return;
-    uint32_t lo = 0, hi = nseg;
+    uint32_t lo = 0, hi = nseg;  // schedule position k of q
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (__ldg(pstart + mid) <= q) lo = mid; else hi = mid;
     }
+    const uint32_t s = __ldg(sched + lo);
     const uint32_t j = q - pstart[lo];
-    padded[q] = (j < seg_cnt[lo]) ? sorted_ids[seg_begin[lo] + j] : INVALID_ID;
+    padded[q] = (j < seg_cnt[s]) ? sorted_ids[seg_begin[s] + j] : INVALID_ID;
 }
 
 }  // namespace rsh
@@ -117,9 +124,10 @@ namespace {
 struct BatchPlan {
     uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0;
     void *rays_all, *keys, *trimmed, *ckeys, *cbases, *counts, *skeys, *svals, *sorted_keys, *sorted_ids, *scr;
-    void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work;
+    void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work, *sched;
     std::vector<PrepSeg> h_prep;
-    std::vector<FusedSeg> h_fsegs;
+    std::vector<FusedSeg> h_fsegs;  // in schedule order
+    std::vector<uint32_t> h_sched;  // schedule position -> segment index
 };
 
 rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count, BatchPlan& pl) {
@@ -173,6 +181,7 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     RSH_TRY(ensure(ctx, "b_pstart", 4ull * (count + 1), &pl.pstart));
     RSH_TRY(ensure(ctx, "b_totals", 64, &pl.totals));
     RSH_TRY(ensure(ctx, "b_work", 64, &pl.work));
+    RSH_TRY(ensure(ctx, "b_sched", 4ull * (count + 1), &pl.sched));
     pl.h_prep.resize(count);
     pl.h_fsegs.resize(count);
     uint32_t start = 0;
@@ -207,6 +216,15 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         f.slot_base = start;
         start += g.n;
     }
+    // schedule: closest-hit segments first (incoherent, long rays), then by size, descending
+    pl.h_sched.resize(count);
+    for (uint32_t s = 0; s < count; ++s) pl.h_sched[s] = s;
+    std::stable_sort(pl.h_sched.begin(), pl.h_sched.end(), [&](uint32_t a, uint32_t b) {
+        if (segs[a].any_hit != segs[b].any_hit) return segs[a].any_hit == 0;
+        return segs[a].n > segs[b].n;
+    });
+    std::vector<FusedSeg> by_seg(pl.h_fsegs);
+    for (uint32_t k = 0; k < count; ++k) pl.h_fsegs[k] = by_seg[pl.h_sched[k]];
     return RSH_OK;
 }
 
@@ -226,11 +244,14 @@ struct HostStage {
 std::map<const rsh_ctx*, HostStage> g_stage;
 std::mutex g_stage_mu;
 
-size_t table_bytes(const BatchPlan& pl) { return sizeof(PrepSeg) * pl.nseg + sizeof(FusedSeg) * pl.nseg + 256; }
+size_t table_bytes(const BatchPlan& pl) {
+    return sizeof(PrepSeg) * pl.nseg + sizeof(FusedSeg) * pl.nseg + 4ull * pl.nseg + 256;
+}
 
 void fill_tables(const BatchPlan& pl, char* b) {
     std::memcpy(b, pl.h_prep.data(), sizeof(PrepSeg) * pl.nseg);
     std::memcpy(b + sizeof(PrepSeg) * pl.nseg, pl.h_fsegs.data(), sizeof(FusedSeg) * pl.nseg);
+    std::memcpy(b + (sizeof(PrepSeg) + sizeof(FusedSeg)) * pl.nseg, pl.h_sched.data(), 4ull * pl.nseg);
 }
 
 // Returns pinned memory holding the tables in a ring slot whose fence the caller records with *fence after
@@ -266,6 +287,8 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     RSH_CUDA(cudaMemcpyAsync(pl.prep, tables, sizeof(PrepSeg) * pl.nseg, cudaMemcpyHostToDevice, s));
     RSH_CUDA(cudaMemcpyAsync(pl.fsegs, tables + sizeof(PrepSeg) * pl.nseg, sizeof(FusedSeg) * pl.nseg,
                              cudaMemcpyHostToDevice, s));
+    RSH_CUDA(cudaMemcpyAsync(pl.sched, tables + (sizeof(PrepSeg) + sizeof(FusedSeg)) * pl.nseg, 4ull * pl.nseg,
+                             cudaMemcpyHostToDevice, s));
     if (fence) RSH_CUDA(cudaEventRecord(fence, s));
     RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
     if (pl.total == 0) return RSH_OK;
@@ -296,12 +319,13 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     k_batch_bounds<<<1, 1024, 0, s>>>(static_cast<uint32_t*>(pl.sorted_keys), cnt, pl.nseg, pl.tag_shift,
                                       pl.unit_rays, static_cast<uint32_t*>(pl.seg_begin),
                                       static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart),
-                                      static_cast<FusedSeg*>(pl.fsegs), totals);
+                                      static_cast<uint32_t*>(pl.sched), static_cast<FusedSeg*>(pl.fsegs), totals);
     note_launch();
     RSH_CUDA(cudaGetLastError());
     k_batch_pad<<<(pl.max_padded + 255) / 256, 256, 0, s>>>(
         static_cast<uint32_t*>(pl.sorted_ids), static_cast<uint32_t*>(pl.seg_begin),
-        static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart), pl.nseg, pl.max_padded, totals,
+        static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart), static_cast<uint32_t*>(pl.sched),
+        pl.nseg, pl.max_padded, totals,
         static_cast<uint32_t*>(pl.padded));
     note_launch();
     RSH_CUDA(cudaGetLastError());

@@ -4,11 +4,13 @@
 // skeleton[x] = size[sortedValue[x]]) -> cub ExclusiveSum -> CreateSortedRays (:1012-1059), where one
 // thread copies a whole chunk serially (load-imbalanced; the largest sort-stage cost in the thesis
 // timings). Here:
-//  1. k_dc_scan: single-pass exclusive scan of the sorted chunk sizes (decoupled look-back on 64-bit
-//     flag|value words) -> off[x];
-//  2. k_dc_expand: every CTA owns 2048 consecutive OUTPUT rays, locates its chunk range by binary
-//     search, stages those chunks' offsets/bases/keys in shared memory, and each thread binary-searches
-//     its ray's chunk there: work per CTA is fixed whatever the chunk sizes.
+//  1. exclusive scan of the sorted chunk sizes -> off[x], reduce-then-scan (k_dc_reduce: one sum per
+//     2048-chunk tile; k_dc_tscan: one CTA scans the tile sums; k_dc_write: per tile, the chunk
+//     offsets); every chunk also records itself as the first chunk of each 2048-output expand tile
+//     that starts inside it (tile_chunk[m]);
+//  2. k_dc_expand: every CTA owns 2048 consecutive OUTPUT rays, reads its chunk range from tile_chunk,
+//     stages those chunks' offsets/bases/keys in shared memory, and each thread binary-searches its
+//     ray's chunk there: work per CTA is fixed whatever the chunk sizes.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -20,27 +22,12 @@ constexpr int DS_ITEMS = 8;
 constexpr int DS_TILE = DS_THREADS * DS_ITEMS;  // chunks per scan tile
 constexpr int DE_THREADS = 256;
 constexpr int DE_ITEMS = 8;
-constexpr int DE_TILE = DE_THREADS * DE_ITEMS;  // output rays per expand CTA
-constexpr unsigned long long F_AGG = 1ull << 62;
-constexpr unsigned long long F_PRE = 2ull << 62;
-constexpr unsigned long long V_MASK = (1ull << 62) - 1ull;
+constexpr uint32_t DE_TILE = DE_THREADS * DE_ITEMS;  // output rays per expand CTA
 }  // namespace
 
-__global__ void __launch_bounds__(DS_THREADS)
-k_dc_scan(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
-          const uint32_t* __restrict__ counts, uint32_t max_chunks, uint32_t* __restrict__ off,
-          unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* err) {
-    __shared__ uint32_t s_warp[DS_THREADS / 32];
-    __shared__ uint32_t s_tile, s_excl, s_tot;
-    const uint32_t C = counts[1] < max_chunks ? counts[1] : max_chunks;
-    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    const uint32_t num_tiles = (C + DS_TILE - 1) / DS_TILE;
-    if (tile >= num_tiles) return;
-    const uint32_t x0 = tile * DS_TILE + tid * DS_ITEMS;
-    uint32_t sz[DS_ITEMS];
+// sizes of the tile's sorted chunks (8 consecutive per thread) and their sum
+RSH_DEV uint32_t chunk_sizes(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases, uint32_t C,
+                             uint32_t x0, uint32_t (&sz)[DS_ITEMS]) {
     uint32_t tsum = 0;
 #pragma unroll
     for (int i = 0; i < DS_ITEMS; ++i) {
@@ -48,11 +35,17 @@ k_dc_scan(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
         uint32_t v = 0;
         if (x < C) {
             const uint32_t c = __ldg(vals + x);
-            v = __ldg(bases + c + 1) - __ldg(bases + c);
+            if (c < C) v = __ldg(bases + c + 1) - __ldg(bases + c);
         }
         sz[i] = v;
         tsum += v;
     }
+    return tsum;
+}
+
+// block-wide exclusive prefix of each thread's sum; *total (all threads) = the tile's sum
+RSH_DEV uint32_t block_excl(uint32_t tsum, uint32_t* s_warp, uint32_t* total) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     uint32_t inc = tsum;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -61,61 +54,72 @@ k_dc_scan(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
     }
     if (lane == 31) s_warp[warp] = inc;
     __syncthreads();
-    if (tid == 0) {
+    if (threadIdx.x == 0) {
         uint32_t r = 0;
-        for (int w = 0; w < DS_THREADS / 32; ++w) {
-            const uint32_t t = s_warp[w];
+        for (uint32_t w = 0; w < blockDim.x / 32; ++w) {
+            const uint32_t v = s_warp[w];
             s_warp[w] = r;
-            r += t;
+            r += v;
         }
-        s_tot = r;
+        s_warp[32] = r;
     }
     __syncthreads();
-    if (warp == 0) {
-        // decoupled look-back, 32 predecessors per step (lane l reads tile j - l), summing up to the
-        // newest predecessor that already holds its inclusive prefix
-        const uint32_t r = s_tot;
-        unsigned long long* st = status + tile;
-        uint32_t excl = 0;
-        if (tile == 0) {
-            if (lane == 0) st_release_u64(st, F_PRE | r);
-        } else {
-            if (lane == 0) st_release_u64(st, F_AGG | r);
-            int64_t j = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            while (j >= 0) {
-                const int64_t idx = j - (int64_t)lane;
-                // flag and value share one word, so a relaxed load suffices
-                const unsigned long long s = idx >= 0 ? ld_relaxed_u64(status + idx) : F_PRE;
-                const unsigned long long f = s & ~V_MASK;
-                const uint32_t pre = __ballot_sync(0xffffffffu, f == F_PRE);
-                const uint32_t lim = pre ? (uint32_t)(__ffs(pre) - 1) : 31u;
-                const uint32_t upto = lim == 31u ? 0xffffffffu : ((2u << lim) - 1u);
-                if (__ballot_sync(0xffffffffu, f == 0ull) & upto) {
-                    if (++spins > RSH_SPIN_LIMIT) {
-                        raise_device_error(err, RSH_DEVERR_TIMEOUT);
-                        break;
-                    }
-                    if (spins > 16) __nanosleep(32);
-                    continue;
-                }
-                uint32_t v = lane <= lim ? (uint32_t)(s & V_MASK) : 0u;
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-                excl += v;
-                if (pre) break;
-                j -= 32;
-            }
-            if (lane == 0) st_release_u64(st, F_PRE | (unsigned long long)(excl + r));
-        }
-        if (lane == 0) s_excl = excl;
+    *total = s_warp[32];
+    return s_warp[warp] + inc - tsum;
+}
+
+__global__ void __launch_bounds__(DS_THREADS)
+k_dc_reduce(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
+            const uint32_t* __restrict__ counts, uint32_t max_chunks, uint32_t* __restrict__ tsum) {
+    __shared__ uint32_t s_warp[33];
+    const uint32_t C = counts[1] < max_chunks ? counts[1] : max_chunks;
+    const uint32_t x0 = blockIdx.x * DS_TILE + threadIdx.x * DS_ITEMS;
+    if (blockIdx.x * DS_TILE >= C) return;  // whole CTA: tiles past the chunk count are never read
+    uint32_t sz[DS_ITEMS];
+    uint32_t tot;
+    block_excl(chunk_sizes(vals, bases, C, x0, sz), s_warp, &tot);
+    if (threadIdx.x == 0) tsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024)
+k_dc_tscan(const uint32_t* __restrict__ tsum, const uint32_t* __restrict__ counts, uint32_t max_chunks,
+           uint32_t* __restrict__ tpre) {
+    __shared__ uint32_t s_warp[33];
+    const uint32_t C = counts[1] < max_chunks ? counts[1] : max_chunks;
+    const uint32_t tiles = (C + DS_TILE - 1) / DS_TILE;
+    const uint32_t per = (tiles + 1023) / 1024;
+    const uint32_t b = threadIdx.x * per, e = min(b + per, tiles);
+    uint32_t s = 0;
+    for (uint32_t i = b; i < e; ++i) s += __ldg(tsum + i);
+    uint32_t tot;
+    uint32_t run = block_excl(s, s_warp, &tot);
+    for (uint32_t i = b; i < e; ++i) {
+        tpre[i] = run;
+        run += __ldg(tsum + i);
     }
-    __syncthreads();
-    uint32_t run = s_excl + s_warp[warp] + inc - tsum;
+}
+
+__global__ void __launch_bounds__(DS_THREADS)
+k_dc_write(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
+           const uint32_t* __restrict__ counts, uint32_t max_chunks, const uint32_t* __restrict__ tpre,
+           uint32_t* __restrict__ off, uint32_t* __restrict__ tile_chunk, uint32_t mcap) {
+    __shared__ uint32_t s_warp[33];
+    const uint32_t C = counts[1] < max_chunks ? counts[1] : max_chunks;
+    const uint32_t x0 = blockIdx.x * DS_TILE + threadIdx.x * DS_ITEMS;
+    if (blockIdx.x * DS_TILE >= C) return;
+    uint32_t sz[DS_ITEMS];
+    uint32_t tot;
+    uint32_t run = __ldg(tpre + blockIdx.x) + block_excl(chunk_sizes(vals, bases, C, x0, sz), s_warp, &tot);
 #pragma unroll
     for (int i = 0; i < DS_ITEMS; ++i) {
         const uint32_t x = x0 + i;
-        if (x < C) off[x] = run;
+        if (x < C) {
+            off[x] = run;
+            // expand tiles whose first output lies in this chunk (sizes are >= 1)
+            if (sz[i] > 0u)
+                for (uint32_t m = (run + DE_TILE - 1u) / DE_TILE; m <= (run + sz[i] - 1u) / DE_TILE && m < mcap; ++m)
+                    tile_chunk[m] = x;
+        }
         run += sz[i];
     }
 }
@@ -124,36 +128,24 @@ __global__ void __launch_bounds__(DE_THREADS)
 k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ vals,
             const uint32_t* __restrict__ bases, const uint32_t* __restrict__ trimmed,
             const uint32_t* __restrict__ counts, uint32_t max_rays, const uint32_t* __restrict__ off,
-            uint32_t* __restrict__ sorted_keys, uint32_t* __restrict__ sorted_ids) {
+            const uint32_t* __restrict__ tile_chunk, uint32_t* __restrict__ sorted_keys,
+            uint32_t* __restrict__ sorted_ids) {
     __shared__ uint32_t s_off[DE_TILE + 1];
     __shared__ uint32_t s_base[DE_TILE + 1];
     __shared__ uint32_t s_key[DE_TILE + 1];
-    __shared__ uint32_t s_x0, s_m;
     const uint32_t R = counts[0] < max_rays ? counts[0] : max_rays;
     const uint32_t C = counts[1];
     const uint32_t k0 = blockIdx.x * DE_TILE;
     if (k0 >= R || C == 0) return;
     const uint32_t k1 = (k0 + DE_TILE < R ? k0 + DE_TILE : R) - 1;  // last output of the tile
-    if (threadIdx.x == 0) {
-        // chunk of k: the last x with off[x] <= k
-        uint32_t lo = 0, hi = C;
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (__ldg(off + mid) <= k0) lo = mid; else hi = mid;
-        }
-        const uint32_t xa = lo;
-        lo = xa;
-        hi = C;
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (__ldg(off + mid) <= k1) lo = mid; else hi = mid;
-        }
-        s_x0 = xa;
-        const uint32_t m = lo - xa + 1;  // <= DE_TILE: every chunk in range covers >= 1 output of the tile
-        s_m = m < (uint32_t)DE_TILE ? m : (uint32_t)DE_TILE;
-    }
-    __syncthreads();
-    const uint32_t x0 = s_x0, m = s_m;
+    // chunks x0..x1 cover outputs k0..k1: x0 holds k0, and the chunk holding the next tile's first
+    // output is at or after the one holding k1 (one extra chunk may be staged)
+    const uint32_t ntiles = (R + DE_TILE - 1) / DE_TILE;
+    const uint32_t x0 = __ldg(tile_chunk + blockIdx.x);
+    uint32_t x1 = (blockIdx.x + 1 < ntiles) ? __ldg(tile_chunk + blockIdx.x + 1) : C - 1;
+    if (x1 >= C) x1 = C - 1;
+    if (x1 < x0) x1 = x0;
+    const uint32_t m = (x1 - x0 + 1 < DE_TILE + 1) ? x1 - x0 + 1 : DE_TILE + 1;
     for (uint32_t i = threadIdx.x; i < m; i += DE_THREADS) {
         const uint32_t x = x0 + i;
         s_off[i] = __ldg(off + x);
@@ -165,7 +157,7 @@ k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ val
     for (int it = 0; it < DE_ITEMS; ++it) {
         const uint32_t k = k0 + it * DE_THREADS + threadIdx.x;
         if (k > k1) break;
-        uint32_t lo = 0, hi = m;
+        uint32_t lo = 0, hi = m;  // last staged chunk with off <= k
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
             if (s_off[mid] <= k) lo = mid; else hi = mid;
@@ -178,29 +170,34 @@ k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ val
 
 size_t decompress_scratch_bytes(uint32_t max_chunks) {
     const size_t tiles = (max_chunks + DS_TILE - 1) / DS_TILE + 1;
-    return 64 + tiles * 8 + (size_t)max_chunks * 4 + 512;
+    const size_t etiles = (max_chunks + DE_TILE - 1) / DE_TILE + 1;
+    return 64 + tiles * 8 + (size_t)max_chunks * 4 + etiles * 4 + 512;
 }
 
 cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t* sorted_chunk_vals,
                               const uint32_t* chunk_bases, const uint32_t* trimmed_ids,
                               const uint32_t* counts, uint32_t max_rays, uint32_t* sorted_keys,
                               uint32_t* sorted_ids, void* scratch, uint32_t* err, cudaStream_t s) {
+    (void)err;  // no step of this form waits on another CTA
     if (max_rays == 0) return cudaSuccess;
     const uint32_t max_chunks = max_rays;
     const size_t tiles = (max_chunks + DS_TILE - 1) / DS_TILE + 1;
     char* b = static_cast<char*>(scratch);
-    uint32_t* ticket = reinterpret_cast<uint32_t*>(b);
-    unsigned long long* status = reinterpret_cast<unsigned long long*>(b + 64);
+    uint32_t* tsum = reinterpret_cast<uint32_t*>(b + 64);
+    uint32_t* tpre = tsum + tiles;
     uint32_t* off = reinterpret_cast<uint32_t*>(b + 64 + tiles * 8);
-    cudaError_t e = cudaMemsetAsync(b, 0, 64 + tiles * 8, s);
-    if (e != cudaSuccess) return e;
-    k_dc_scan<<<(unsigned)(tiles - 1 > 0 ? tiles - 1 : 1), DS_THREADS, 0, s>>>(
-        sorted_chunk_vals, chunk_bases, counts, max_chunks, off, status, ticket, err);
+    uint32_t* tile_chunk = off + max_chunks;
+    const uint32_t mcap = (uint32_t)((max_chunks + DE_TILE - 1) / DE_TILE + 1);
+    const uint32_t grid = (uint32_t)(tiles - 1 > 0 ? tiles - 1 : 1);
+    k_dc_reduce<<<grid, DS_THREADS, 0, s>>>(sorted_chunk_vals, chunk_bases, counts, max_chunks, tsum);
     note_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    k_dc_tscan<<<1, 1024, 0, s>>>(tsum, counts, max_chunks, tpre);
+    note_launch();
+    k_dc_write<<<grid, DS_THREADS, 0, s>>>(sorted_chunk_vals, chunk_bases, counts, max_chunks, tpre, off,
+                                           tile_chunk, mcap);
+    note_launch();
     k_dc_expand<<<(max_rays + DE_TILE - 1) / DE_TILE, DE_THREADS, 0, s>>>(
-        sorted_chunk_keys, sorted_chunk_vals, chunk_bases, trimmed_ids, counts, max_rays, off,
+        sorted_chunk_keys, sorted_chunk_vals, chunk_bases, trimmed_ids, counts, max_rays, off, tile_chunk,
         sorted_keys, sorted_ids);
     note_launch();
     return cudaGetLastError();

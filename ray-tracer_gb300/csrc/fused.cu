@@ -28,7 +28,10 @@ constexpr int F_MAXK = 32;       // max cluster size staged in shared memory
 constexpr uint32_t INVALID_ID = 0xFFFFFFFFu;
 constexpr int J_STACK = 96;                // per-lane node stack of a job
 constexpr uint32_t J_CAP = 512;            // job queue entries per warp
-constexpr uint32_t J_DRAIN = 128;          // queue length at which the packet walk stops to run the jobs
+#ifndef RSH_J_DRAIN
+#define RSH_J_DRAIN 256
+#endif
+constexpr uint32_t J_DRAIN = RSH_J_DRAIN;  // queue length at which the packet walk stops to run the jobs
 }
 
 template <int P>
@@ -232,8 +235,11 @@ RSH_DEV void refresh_packets(FusedSmem<P>& S, bool any, uint32_t q, uint32_t ch,
     }
 }
 
+#ifndef RSH_FUSED_MIN_BLOCKS
+#define RSH_FUSED_MIN_BLOCKS 5
+#endif
 template <int P>
-__global__ void __launch_bounds__(FW * 32) k_fused(FusedArgs a) {
+__global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FusedSmem<P>& S = reinterpret_cast<FusedSmem<P>*>(smem_raw)[threadIdx.x >> 5];
     const uint32_t lane = lane_id();

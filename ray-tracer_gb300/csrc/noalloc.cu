@@ -1,6 +1,6 @@
-// Trim + compress without any allocation: the decoupled look-back scratch of k_compress (tile ticket,
-// tile status flags and the two 4-word summaries per tile) lives in a fixed static device array, so the
-// call needs no context and never calls cudaMalloc/cudaFree.
+// Trim + compress without any allocation: the scratch of the compress kernels (a 4-word summary and a
+// 4-word prefix per tile) lives in a fixed static device array, so the call needs no context and never
+// calls cudaMalloc/cudaFree.
 //
 // Who needs this: host applications that own every byte of device memory and forbid a plug-in from
 // allocating (pre-partitioned memory on a shared or real-time device), and loops that allocate once at
@@ -15,7 +15,8 @@ namespace {
 
 // Largest slot count one call accepts (16,777,216 = e.g. 1920 x 1080 pixels x 8 lights).
 constexpr uint32_t kMaxSlots = 1u << 24;
-// k_compress tiles hold 3072 slots; scratch = 4 words + per tile (1 flag + 4 + 4 summary words).
+// Room for compress tiles of 3072 slots or more at 9 words per tile; the current kernels use 4096-slot
+// tiles at 8 words per tile (compress_scratch_bytes), checked against the array below on every call.
 constexpr uint32_t kTileSlots = 3072u;
 constexpr uint32_t kMaxTiles = (kMaxSlots + kTileSlots - 1) / kTileSlots + 1;
 constexpr uint32_t kScratchWords = 4u + 9u * kMaxTiles;   // 49,171 words = 196,684 bytes
@@ -38,6 +39,10 @@ extern "C" rsh_status rsh_compress_noalloc(const uint32_t* keys, uint32_t n_slot
         rsh::set_error("rsh_compress_noalloc: n_slots exceeds the static scratch limit of 16777216 slots");
         return RSH_ERR_INVALID;
     }
+    if (rsh::compress_scratch_bytes(n_slots) > sizeof(g_compress_scratch)) {
+        rsh::set_error("rsh_compress_noalloc: static scratch too small for n_slots");
+        return RSH_ERR_INVALID;
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return rsh::cuda_status(e, "rsh_compress_noalloc: cudaGetDevice");
@@ -55,8 +60,9 @@ extern "C" rsh_status rsh_compress_noalloc(const uint32_t* keys, uint32_t n_slot
         }
         scratch = g_scratch_addr[dev];
     }
-    // launch_compress clears the ticket and the tile flags (the part of the scratch that must start at
-    // zero) with a memset on `stream` before the kernel; no device error word is attached here.
+    // nothing in the scratch has to start at zero: every word is written before it is read, within the
+    // call, on `stream`
+
     e = rsh::launch_compress(keys, n_slots, trimmed_ids, chunk_keys, chunk_bases, counts, scratch, nullptr,
                              stream);
     if (e != cudaSuccess) return rsh::cuda_status(e, "rsh_compress_noalloc");

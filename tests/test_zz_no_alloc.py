@@ -1,5 +1,5 @@
 """rsh_compress_noalloc: the trim + compress entry point for callers that cannot allocate device memory
-(it keeps its look-back scratch in a static device array). Its outputs must equal rsh_compress's exactly,
+(it keeps its compress scratch in a static device array). Its outputs must equal rsh_compress's exactly,
 on two calls in a row (the second smaller than the first, so stale scratch from the first call would
 show). This file is collected last on purpose."""
 import numpy as np
