@@ -317,7 +317,7 @@ def gpu_arm(args, s, rank, world, td):
 
     e2e = None
     per_stage, roof, last = {}, None, head["stats"][-1]
-    if args.mode == "all":
+    if args.mode in ("all", "fused"):
         # e2e through the C ABI with host buffers, headline form
         e_ms, e_stats = timed(head["flags"], args.steps, e2e=True)
         e2e = {"value": round(reduce_sum(td, rays_of(e_stats)) / (reduce_max(td, e_ms) * 1e3), 3), "unit": "Mrays/s",

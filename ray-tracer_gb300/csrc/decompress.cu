@@ -25,24 +25,6 @@ constexpr int DE_ITEMS = 8;
 constexpr uint32_t DE_TILE = DE_THREADS * DE_ITEMS;  // output rays per expand CTA
 }  // namespace
 
-// sizes of the tile's sorted chunks (8 consecutive per thread) and their sum
-RSH_DEV uint32_t chunk_sizes(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases, uint32_t C,
-                             uint32_t x0, uint32_t (&sz)[DS_ITEMS]) {
-    uint32_t tsum = 0;
-#pragma unroll
-    for (int i = 0; i < DS_ITEMS; ++i) {
-        const uint32_t x = x0 + i;
-        uint32_t v = 0;
-        if (x < C) {
-            const uint32_t c = __ldg(vals + x);
-            if (c < C) v = __ldg(bases + c + 1) - __ldg(bases + c);
-        }
-        sz[i] = v;
-        tsum += v;
-    }
-    return tsum;
-}
-
 // block-wide exclusive prefix of each thread's sum; *total (all threads) = the tile's sum
 RSH_DEV uint32_t block_excl(uint32_t tsum, uint32_t* s_warp, uint32_t* total) {
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
@@ -68,16 +50,32 @@ RSH_DEV uint32_t block_excl(uint32_t tsum, uint32_t* s_warp, uint32_t* total) {
     return s_warp[warp] + inc - tsum;
 }
 
+// Gathers each sorted chunk's base and size once (the only random reads of the chunk table) into
+// sorted order, and sums the tile's sizes.
 __global__ void __launch_bounds__(DS_THREADS)
 k_dc_reduce(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
-            const uint32_t* __restrict__ counts, uint32_t max_chunks, uint32_t* __restrict__ tsum) {
+            const uint32_t* __restrict__ counts, uint32_t max_chunks, uint32_t* __restrict__ tsum,
+            uint32_t* __restrict__ sbase, uint32_t* __restrict__ ssize) {
     __shared__ uint32_t s_warp[33];
     const uint32_t C = counts[1] < max_chunks ? counts[1] : max_chunks;
-    const uint32_t x0 = blockIdx.x * DS_TILE + threadIdx.x * DS_ITEMS;
     if (blockIdx.x * DS_TILE >= C) return;  // whole CTA: tiles past the chunk count are never read
-    uint32_t sz[DS_ITEMS];
+    uint32_t tsum_t = 0;
+    for (uint32_t i = 0; i < DS_ITEMS; ++i) {  // x strided by the block: coalesced
+        const uint32_t x = blockIdx.x * DS_TILE + i * DS_THREADS + threadIdx.x;
+        if (x < C) {
+            const uint32_t c = __ldg(vals + x);
+            uint32_t b = 0, v = 0;
+            if (c < C) {
+                b = __ldg(bases + c);
+                v = __ldg(bases + c + 1) - b;
+            }
+            sbase[x] = b;
+            ssize[x] = v;
+            tsum_t += v;
+        }
+    }
     uint32_t tot;
-    block_excl(chunk_sizes(vals, bases, C, x0, sz), s_warp, &tot);
+    block_excl(tsum_t, s_warp, &tot);
     if (threadIdx.x == 0) tsum[blockIdx.x] = tot;
 }
 
@@ -100,16 +98,22 @@ k_dc_tscan(const uint32_t* __restrict__ tsum, const uint32_t* __restrict__ count
 }
 
 __global__ void __launch_bounds__(DS_THREADS)
-k_dc_write(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases,
-           const uint32_t* __restrict__ counts, uint32_t max_chunks, const uint32_t* __restrict__ tpre,
-           uint32_t* __restrict__ off, uint32_t* __restrict__ tile_chunk, uint32_t mcap) {
+k_dc_write(const uint32_t* __restrict__ ssize, const uint32_t* __restrict__ counts, uint32_t max_chunks,
+           const uint32_t* __restrict__ tpre, uint32_t* __restrict__ off, uint32_t* __restrict__ tile_chunk,
+           uint32_t mcap) {
     __shared__ uint32_t s_warp[33];
     const uint32_t C = counts[1] < max_chunks ? counts[1] : max_chunks;
     const uint32_t x0 = blockIdx.x * DS_TILE + threadIdx.x * DS_ITEMS;
     if (blockIdx.x * DS_TILE >= C) return;
     uint32_t sz[DS_ITEMS];
+    uint32_t ts = 0;
+#pragma unroll
+    for (int i = 0; i < DS_ITEMS; ++i) {
+        sz[i] = (x0 + i < C) ? __ldg(ssize + x0 + i) : 0u;
+        ts += sz[i];
+    }
     uint32_t tot;
-    uint32_t run = __ldg(tpre + blockIdx.x) + block_excl(chunk_sizes(vals, bases, C, x0, sz), s_warp, &tot);
+    uint32_t run = __ldg(tpre + blockIdx.x) + block_excl(ts, s_warp, &tot);
 #pragma unroll
     for (int i = 0; i < DS_ITEMS; ++i) {
         const uint32_t x = x0 + i;
@@ -125,8 +129,8 @@ k_dc_write(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ bases
 }
 
 __global__ void __launch_bounds__(DE_THREADS)
-k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ vals,
-            const uint32_t* __restrict__ bases, const uint32_t* __restrict__ trimmed,
+k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ sbase,
+            const uint32_t* __restrict__ trimmed,
             const uint32_t* __restrict__ counts, uint32_t max_rays, const uint32_t* __restrict__ off,
             const uint32_t* __restrict__ tile_chunk, uint32_t* __restrict__ sorted_keys,
             uint32_t* __restrict__ sorted_ids) {
@@ -149,7 +153,7 @@ k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ val
     for (uint32_t i = threadIdx.x; i < m; i += DE_THREADS) {
         const uint32_t x = x0 + i;
         s_off[i] = __ldg(off + x);
-        s_base[i] = __ldg(bases + __ldg(vals + x));
+        s_base[i] = __ldg(sbase + x);
         s_key[i] = skeys ? __ldg(skeys + x) : 0u;
     }
     __syncthreads();
@@ -171,7 +175,7 @@ k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ val
 size_t decompress_scratch_bytes(uint32_t max_chunks) {
     const size_t tiles = (max_chunks + DS_TILE - 1) / DS_TILE + 1;
     const size_t etiles = (max_chunks + DE_TILE - 1) / DE_TILE + 1;
-    return 64 + tiles * 8 + (size_t)max_chunks * 4 + etiles * 4 + 512;
+    return 64 + tiles * 8 + (size_t)max_chunks * 12 + etiles * 4 + 512;
 }
 
 cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t* sorted_chunk_vals,
@@ -186,19 +190,19 @@ cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t*
     uint32_t* tsum = reinterpret_cast<uint32_t*>(b + 64);
     uint32_t* tpre = tsum + tiles;
     uint32_t* off = reinterpret_cast<uint32_t*>(b + 64 + tiles * 8);
-    uint32_t* tile_chunk = off + max_chunks;
+    uint32_t* sbase = off + max_chunks;   // sorted chunk bases and sizes
+    uint32_t* ssize = sbase + max_chunks;
+    uint32_t* tile_chunk = ssize + max_chunks;
     const uint32_t mcap = (uint32_t)((max_chunks + DE_TILE - 1) / DE_TILE + 1);
     const uint32_t grid = (uint32_t)(tiles - 1 > 0 ? tiles - 1 : 1);
-    k_dc_reduce<<<grid, DS_THREADS, 0, s>>>(sorted_chunk_vals, chunk_bases, counts, max_chunks, tsum);
+    k_dc_reduce<<<grid, DS_THREADS, 0, s>>>(sorted_chunk_vals, chunk_bases, counts, max_chunks, tsum, sbase, ssize);
     note_launch();
     k_dc_tscan<<<1, 1024, 0, s>>>(tsum, counts, max_chunks, tpre);
     note_launch();
-    k_dc_write<<<grid, DS_THREADS, 0, s>>>(sorted_chunk_vals, chunk_bases, counts, max_chunks, tpre, off,
-                                           tile_chunk, mcap);
+    k_dc_write<<<grid, DS_THREADS, 0, s>>>(ssize, counts, max_chunks, tpre, off, tile_chunk, mcap);
     note_launch();
     k_dc_expand<<<(max_rays + DE_TILE - 1) / DE_TILE, DE_THREADS, 0, s>>>(
-        sorted_chunk_keys, sorted_chunk_vals, chunk_bases, trimmed_ids, counts, max_rays, off, tile_chunk,
-        sorted_keys, sorted_ids);
+        sorted_chunk_keys, sbase, trimmed_ids, counts, max_rays, off, tile_chunk, sorted_keys, sorted_ids);
     note_launch();
     return cudaGetLastError();
 }

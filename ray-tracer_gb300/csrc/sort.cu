@@ -9,6 +9,8 @@
 //     stably (warp match_any + per-warp digit counters), publishes its per-digit counts, resolves the
 //     per-digit exclusive prefix over earlier tiles by decoupled look-back (bounded spin), then
 //     scatters through shared memory so that global writes are runs of one digit.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -54,7 +56,7 @@ __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
     }
 }
 
-__global__ void __launch_bounds__(SR_THREADS)
+__global__ void __launch_bounds__(SR_THREADS, 3)
 k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n_max,
            const uint32_t* __restrict__ d_count, uint32_t shift, const uint32_t* __restrict__ hist,
@@ -69,12 +71,14 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
 
     const uint32_t n = dev_count(d_count, n_max);
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    const uint32_t num_tiles = (n + SR_TILE - 1) / SR_TILE;
+  for (;;) {  // tiles by ticket until none is left (the grid is capped at the resident CTAs)
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
-    for (uint32_t i = tid; i < SR_WARPS * 256u; i += SR_THREADS) (&s_wc[0][0])[i] = 0u;
     __syncthreads();
     const uint32_t tile = s_tile;
-    const uint32_t num_tiles = (n + SR_TILE - 1) / SR_TILE;
     if (tile >= num_tiles) return;
+    for (uint32_t i = tid; i < SR_WARPS * 256u; i += SR_THREADS) (&s_wc[0][0])[i] = 0u;
+    __syncthreads();
     const uint32_t base = tile * SR_TILE;
     const uint32_t wbase = base + warp * (SR_ITEMS * 32u);
 
@@ -227,6 +231,8 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
             vals_out[g] = s_vals[i];
         }
     }
+    __syncthreads();  // shared state is reused by the next tile
+  }
 }
 
 size_t sort_scratch_bytes(uint32_t n_max, uint32_t key_bits) {
@@ -252,6 +258,14 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
     cudaError_t e = cudaMemsetAsync(w, 0, (4 * 256 + 8) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     k_sort_hist<<<152 * 2, 256, 0, s>>>(keys_in, n_max, d_count, passes, hist, status, tiles * 256);
+    // at most the CTAs resident at once: tiles beyond the device count cost nothing, and every ticket
+    // below a CTA's tile is held by a running CTA (forward progress of the look-back)
+    int dev = 0, sms = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep, SR_THREADS, 0);
+    if (per_sm < 1) per_sm = 1;
+    const uint32_t resident = (uint32_t)(sms * per_sm);
     note_launch();
     // ping-pong so that the last pass lands in the output
     const uint32_t* ki = keys_in;
@@ -263,7 +277,7 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
         uint32_t* ko = to_out ? keys_out : alt_keys;
         uint32_t* vo = to_out ? vals_out : alt_vals;
         (void)last;
-        const uint32_t grid = (uint32_t)(tiles - 1 > 0 ? tiles - 1 : 1);
+        const uint32_t grid = std::min<uint32_t>((uint32_t)(tiles - 1 > 0 ? tiles - 1 : 1), resident);
         k_onesweep<<<grid, SR_THREADS, 0, s>>>(ki, vi, ko, vo, n_max, d_count, 8u * p, hist + 256u * p,
                                                status + p * tiles * 256, tickets + p, err);
         note_launch();
