@@ -3,14 +3,15 @@
 // The reference has no batched path: every batch is a host loop of wrappers with a blocking count
 // readback after each stage (main.cpp:951-1054, RayTracer.cu:2316-2832). Here, for S segments:
 //   k_batch_prep     one pass over all rays: gather into one array, key = segment << shift | hash
-//                    (per-segment scene box), pre-fill each segment's output;
-//   compress / sort / decompress over all keys at once (the segment tag is the top key digit, so the
-//                    sorted order is segment-major: a segmented sort for free);
-//   k_batch_bounds   per-segment ray ranges of the sorted order (binary search on the tag), padded so
-//                    that no level-1 ray node straddles two segments, laid out in schedule order:
-//                    closest-hit segments before any-hit ones, larger before smaller, so the work
-//                    units handed out last (the launch's tail) are the cheap ones;
-//   k_batch_pad      padded ray order (empty slots = inactive rays);
+//                    (per-segment scene box), pre-fill each segment's output, count each segment's rays;
+//   k_batch_bounds   from those counts (one block): each segment's range of the sorted order (the
+//                    segment tag is the top key digit, so the sorted order is segment-major: a segmented
+//                    sort for free) and of the padded layout, padded so that no level-1 ray node straddles
+//                    two segments, laid out in schedule order -- closest-hit segments before any-hit
+//                    ones, larger before smaller, so the work units handed out last (the launch's tail)
+//                    are the cheap ones; the padding slots are marked empty;
+//   compress / sort / decompress over all keys at once; decompress writes each ray straight to its
+//                    padded position;
 //   build            ray-space hierarchy over the padded order;
 //   fused            ONE persistent traversal + intersection launch over every segment's work units.
 // Nothing reads a count back to the host, so the whole sequence is captured in a CUDA graph.
@@ -41,78 +42,67 @@ struct PrepSeg {  // per-segment table of k_batch_prep
 }  // namespace
 
 __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, uint32_t total, uint32_t tag_shift,
-                             rsh_ray* __restrict__ rays_all, uint32_t* __restrict__ keys) {
+                             rsh_ray* __restrict__ rays_all, uint32_t* __restrict__ keys,
+                             uint32_t* __restrict__ seg_cnt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) return;
-    uint32_t lo = 0, hi = nseg;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&segs[mid].start) <= i) lo = mid; else hi = mid;
+    bool valid = false;
+    uint32_t lo = 0;
+    if (i < total) {
+        uint32_t hi = nseg;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(&segs[mid].start) <= i) lo = mid; else hi = mid;
+        }
+        const PrepSeg& sg = segs[lo];
+        const uint32_t j = i - sg.start;
+        float4 o, d;
+        load_ray(sg.rays, j, o, d);
+        store_ray(rays_all, i, o, d);
+        uint32_t key = RSH_KEY_NONE;
+        valid = d.w > o.w;
+        if (valid) key = (lo << tag_shift) | ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, sg.hp, 0u);
+        keys[i] = key;
+        if (sg.any_hit) sg.flags[j] = 0u;
+        else sg.hits[j] = RSH_HIT_NONE;
     }
-    const PrepSeg& sg = segs[lo];
-    const uint32_t j = i - sg.start;
-    float4 o, d;
-    load_ray(sg.rays, j, o, d);
-    store_ray(rays_all, i, o, d);
-    uint32_t key = RSH_KEY_NONE;
-    if (d.w > o.w) {
-        key = (lo << tag_shift) | ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, sg.hp, 0u);
-    }
-    keys[i] = key;
-    if (sg.any_hit) sg.flags[j] = 0u;
-    else sg.hits[j] = RSH_HIT_NONE;
+    // rays per segment: one atomic per segment present in the warp
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? lo : 0xFFFFFFFFu);
+    if (valid && (peers & lanemask_lt()) == 0u) atomicAdd(seg_cnt + lo, (uint32_t)__popc(peers));
 }
 
-// Per-segment ranges in the sorted (segment-major) order and the padded layout; one block.
-__global__ void k_batch_bounds(const uint32_t* __restrict__ sorted_keys, const uint32_t* __restrict__ counts,
-                               uint32_t nseg, uint32_t tag_shift, uint32_t unit_rays, uint32_t* __restrict__ seg_begin,
-                               uint32_t* __restrict__ seg_cnt, uint32_t* __restrict__ pstart,
-                               const uint32_t* __restrict__ sched, FusedSeg* __restrict__ fsegs,
-                               uint32_t* __restrict__ totals) {
-    const uint32_t R = counts[0];
-    for (uint32_t s = threadIdx.x; s < nseg; s += blockDim.x) {
-        auto lower = [&](uint32_t key) {
-            uint32_t lo = 0, hi = R;  // first index with sorted_keys >= key
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (sorted_keys[mid] < key) lo = mid + 1; else hi = mid;
-            }
-            return lo;
-        };
-        const uint32_t b = lower(s << tag_shift);
-        const uint32_t e = lower((s + 1) << tag_shift);
-        seg_begin[s] = b;
-        seg_cnt[s] = e - b;
-    }
-    __syncthreads();
+// Per-segment ranges in the sorted (segment-major) order and the padded layout, from the per-segment ray
+// counts; one block. seg_delta[s] = padded position - sorted position for segment s's rays.
+__global__ void k_batch_bounds(const uint32_t* __restrict__ seg_cnt, uint32_t nseg, uint32_t unit_rays,
+                               uint32_t* __restrict__ seg_begin, uint32_t* __restrict__ pstart,
+                               uint32_t* __restrict__ seg_delta, const uint32_t* __restrict__ sched,
+                               FusedSeg* __restrict__ fsegs, uint32_t* __restrict__ totals,
+                               uint32_t* __restrict__ padded, uint32_t max_padded) {
+    __shared__ uint32_t s_pad_end[1025], s_pad_begin[1025];
     if (threadIdx.x == 0) {
-        uint32_t acc = 0;  // padded layout in schedule order: position k holds segment sched[k]
+        uint32_t acc = 0;  // sorted order: segment index order
+        for (uint32_t s = 0; s < nseg; ++s) {
+            seg_begin[s] = acc;
+            acc += seg_cnt[s];
+        }
+        acc = 0;  // padded layout in schedule order: position k holds segment sched[k]
         for (uint32_t k = 0; k < nseg; ++k) {
             const uint32_t s = sched[k];
             pstart[k] = acc;
             fsegs[k].unit_begin = acc / unit_rays;
+            seg_delta[s] = acc - seg_begin[s];
+            s_pad_begin[k] = acc + seg_cnt[s];
             acc += ((seg_cnt[s] + unit_rays - 1) / unit_rays) * unit_rays;
+            s_pad_end[k] = acc;
         }
         pstart[nseg] = acc;
         totals[0] = acc;              // padded ray count
         totals[1] = acc / unit_rays;  // work units
     }
-}
-
-__global__ void k_batch_pad(const uint32_t* __restrict__ sorted_ids, const uint32_t* __restrict__ seg_begin,
-                            const uint32_t* __restrict__ seg_cnt, const uint32_t* __restrict__ pstart,
-                            const uint32_t* __restrict__ sched, uint32_t nseg, uint32_t max_padded,
-                            const uint32_t* __restrict__ totals, uint32_t* __restrict__ padded) {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= max_padded || q >= totals[0]) return;
-    uint32_t lo = 0, hi = nseg;  // schedule position k of q
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(pstart + mid) <= q) lo = mid; else hi = mid;
-    }
-    const uint32_t s = __ldg(sched + lo);
-    const uint32_t j = q - pstart[lo];
-    padded[q] = (j < seg_cnt[s]) ? sorted_ids[seg_begin[s] + j] : INVALID_ID;
+    __syncthreads();
+    // empty slots at the end of each segment's last work unit
+    for (uint32_t k = 0; k < nseg; ++k)
+        for (uint32_t q = s_pad_begin[k] + threadIdx.x; q < s_pad_end[k] && q < max_padded; q += blockDim.x)
+            padded[q] = INVALID_ID;
 }
 
 }  // namespace rsh
@@ -124,7 +114,7 @@ namespace {
 struct BatchPlan {
     uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0;
     void *rays_all, *keys, *trimmed, *ckeys, *cbases, *counts, *skeys, *svals, *sorted_keys, *sorted_ids, *scr;
-    void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work, *sched;
+    void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work, *sched, *seg_delta;
     std::vector<PrepSeg> h_prep;
     std::vector<FusedSeg> h_fsegs;  // in schedule order
     std::vector<uint32_t> h_sched;  // schedule position -> segment index
@@ -182,6 +172,7 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     RSH_TRY(ensure(ctx, "b_totals", 64, &pl.totals));
     RSH_TRY(ensure(ctx, "b_work", 64, &pl.work));
     RSH_TRY(ensure(ctx, "b_sched", 4ull * (count + 1), &pl.sched));
+    RSH_TRY(ensure(ctx, "b_seg_delta", 4ull * (count + 1), &pl.seg_delta));
     pl.h_prep.resize(count);
     pl.h_fsegs.resize(count);
     uint32_t start = 0;
@@ -293,9 +284,18 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
     if (pl.total == 0) return RSH_OK;
     uint32_t* cnt = static_cast<uint32_t*>(pl.counts);
+    uint32_t* totals = static_cast<uint32_t*>(pl.totals);
+    RSH_CUDA(cudaMemsetAsync(pl.seg_cnt, 0, 4ull * pl.nseg, s));
     k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
                                                        pl.tag_shift, static_cast<rsh_ray*>(pl.rays_all),
-                                                       static_cast<uint32_t*>(pl.keys));
+                                                       static_cast<uint32_t*>(pl.keys), static_cast<uint32_t*>(pl.seg_cnt));
+    note_launch();
+    RSH_CUDA(cudaGetLastError());
+    k_batch_bounds<<<1, 1024, 0, s>>>(static_cast<uint32_t*>(pl.seg_cnt), pl.nseg, pl.unit_rays,
+                                      static_cast<uint32_t*>(pl.seg_begin), static_cast<uint32_t*>(pl.pstart),
+                                      static_cast<uint32_t*>(pl.seg_delta), static_cast<uint32_t*>(pl.sched),
+                                      static_cast<FusedSeg*>(pl.fsegs), totals, static_cast<uint32_t*>(pl.padded),
+                                      pl.max_padded);
     note_launch();
     RSH_CUDA(cudaGetLastError());
     int th = stage_begin(ctx, RSH_STAGE_COMPRESS, s);
@@ -309,26 +309,14 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
                                s));
     stage_end(ctx, th, s);
     th = stage_begin(ctx, RSH_STAGE_DECOMPRESS, s);
+    // straight into the padded layout: ray k of the sorted order goes to k + seg_delta[its segment]
+    PaddedOut po{static_cast<const uint32_t*>(pl.seg_delta), pl.tag_shift, pl.max_padded,
+                 static_cast<uint32_t*>(pl.padded)};
     RSH_CUDA(launch_decompress(static_cast<uint32_t*>(pl.skeys), static_cast<uint32_t*>(pl.svals),
                                static_cast<uint32_t*>(pl.cbases), static_cast<uint32_t*>(pl.trimmed), cnt, pl.total,
-                               static_cast<uint32_t*>(pl.sorted_keys), static_cast<uint32_t*>(pl.sorted_ids), pl.scr,
-                               ctx->d_err, s));
+                               nullptr, nullptr, pl.scr, ctx->d_err, s, &po));
     stage_end(ctx, th, s);
     th = stage_begin(ctx, RSH_STAGE_BUILD, s);
-    uint32_t* totals = static_cast<uint32_t*>(pl.totals);
-    k_batch_bounds<<<1, 1024, 0, s>>>(static_cast<uint32_t*>(pl.sorted_keys), cnt, pl.nseg, pl.tag_shift,
-                                      pl.unit_rays, static_cast<uint32_t*>(pl.seg_begin),
-                                      static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart),
-                                      static_cast<uint32_t*>(pl.sched), static_cast<FusedSeg*>(pl.fsegs), totals);
-    note_launch();
-    RSH_CUDA(cudaGetLastError());
-    k_batch_pad<<<(pl.max_padded + 255) / 256, 256, 0, s>>>(
-        static_cast<uint32_t*>(pl.sorted_ids), static_cast<uint32_t*>(pl.seg_begin),
-        static_cast<uint32_t*>(pl.seg_cnt), static_cast<uint32_t*>(pl.pstart), static_cast<uint32_t*>(pl.sched),
-        pl.nseg, pl.max_padded, totals,
-        static_cast<uint32_t*>(pl.padded));
-    note_launch();
-    RSH_CUDA(cudaGetLastError());
     RSH_CUDA(launch_build_rsh(static_cast<rsh_ray*>(pl.rays_all), static_cast<uint32_t*>(pl.padded), pl.max_padded,
                               totals, pl.P, static_cast<rsh_node*>(pl.nodes), s));
     stage_end(ctx, th, s);

@@ -133,7 +133,7 @@ k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ sba
             const uint32_t* __restrict__ trimmed,
             const uint32_t* __restrict__ counts, uint32_t max_rays, const uint32_t* __restrict__ off,
             const uint32_t* __restrict__ tile_chunk, uint32_t* __restrict__ sorted_keys,
-            uint32_t* __restrict__ sorted_ids) {
+            uint32_t* __restrict__ sorted_ids, PaddedOut po) {
     __shared__ uint32_t s_off[DE_TILE + 1];
     __shared__ uint32_t s_base[DE_TILE + 1];
     __shared__ uint32_t s_key[DE_TILE + 1];
@@ -167,7 +167,13 @@ k_dc_expand(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ sba
             if (s_off[mid] <= k) lo = mid; else hi = mid;
         }
         const uint32_t src = s_base[lo] + (k - s_off[lo]);
-        sorted_ids[k] = src < R ? __ldg(trimmed + src) : 0u;
+        const uint32_t id = src < R ? __ldg(trimmed + src) : 0u;
+        if (po.padded) {
+            const uint32_t q = k + __ldg(po.seg_delta + (s_key[lo] >> po.tag_shift));
+            if (q < po.max_padded) po.padded[q] = id;
+        } else {
+            sorted_ids[k] = id;
+        }
         if (sorted_keys) sorted_keys[k] = s_key[lo];
     }
 }
@@ -181,7 +187,8 @@ size_t decompress_scratch_bytes(uint32_t max_chunks) {
 cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t* sorted_chunk_vals,
                               const uint32_t* chunk_bases, const uint32_t* trimmed_ids,
                               const uint32_t* counts, uint32_t max_rays, uint32_t* sorted_keys,
-                              uint32_t* sorted_ids, void* scratch, uint32_t* err, cudaStream_t s) {
+                              uint32_t* sorted_ids, void* scratch, uint32_t* err, cudaStream_t s,
+                              const PaddedOut* padded_out) {
     (void)err;  // no step of this form waits on another CTA
     if (max_rays == 0) return cudaSuccess;
     const uint32_t max_chunks = max_rays;
@@ -202,7 +209,8 @@ cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t*
     k_dc_write<<<grid, DS_THREADS, 0, s>>>(ssize, counts, max_chunks, tpre, off, tile_chunk, mcap);
     note_launch();
     k_dc_expand<<<(max_rays + DE_TILE - 1) / DE_TILE, DE_THREADS, 0, s>>>(
-        sorted_chunk_keys, sbase, trimmed_ids, counts, max_rays, off, tile_chunk, sorted_keys, sorted_ids);
+        sorted_chunk_keys, sbase, trimmed_ids, counts, max_rays, off, tile_chunk, sorted_keys, sorted_ids,
+        padded_out ? *padded_out : PaddedOut{nullptr, 0u, 0u, nullptr});
     note_launch();
     return cudaGetLastError();
 }

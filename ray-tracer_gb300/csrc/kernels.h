@@ -78,10 +78,19 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
 
 // ---- decompress (decompress.cu)
 size_t decompress_scratch_bytes(uint32_t max_chunks);
+// Batched layout target of decompression: ray k of the sorted order (segment tag = key >> tag_shift)
+// is written to padded[k + seg_delta[tag]] instead of sorted_ids[k].
+struct PaddedOut {
+    const uint32_t* seg_delta;
+    uint32_t tag_shift;
+    uint32_t max_padded;
+    uint32_t* padded;
+};
 cudaError_t launch_decompress(const uint32_t* sorted_chunk_keys, const uint32_t* sorted_chunk_vals,
                               const uint32_t* chunk_bases, const uint32_t* trimmed_ids,
                               const uint32_t* counts, uint32_t max_rays, uint32_t* sorted_keys,
-                              uint32_t* sorted_ids, void* scratch, uint32_t* err, cudaStream_t s);
+                              uint32_t* sorted_ids, void* scratch, uint32_t* err, cudaStream_t s,
+                              const PaddedOut* padded_out = nullptr);
 
 // ---- ray-space hierarchy build (build.cu)
 uint32_t hierarchy_capacity(uint32_t max_rays, uint32_t packet, uint32_t offsets[4]);
