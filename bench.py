@@ -186,7 +186,9 @@ def cpu_baseline(s, crop=(240, 136), threads=None, steps=1):
     cam = rsh.camera_look_at(s.eye, s.target, s.up, s.fov, W, H).as_array()
     lo = s.positions[..., :3].reshape(-1, 3).min(0)
     hi = s.positions[..., :3].reshape(-1, 3).max(0)
-    g, b, P, K = 5, 4, 8, 8
+    # the GPU path's default configuration (grid bits, direction bits, packet, cluster, ray level)
+    dc = rsh.default_config()
+    g, b, P, K, rl = dc.grid_bits, dc.dir_log2, dc.packet_size, dc.cluster_size, dc.ray_level
     t0 = time.perf_counter()
     oh = oracle.ObjH(s.positions, K, lo, hi)
     build_s = time.perf_counter() - t0
@@ -197,7 +199,7 @@ def cpu_baseline(s, crop=(240, 136), threads=None, steps=1):
     cpix = ((py[sel] - y0) * cw + (px[sel] - x0)).astype(np.uint32)
     scale = oracle.hash_scale(lo, hi, g)
     keys = oracle.hash_rays(crays, lo, scale, g, b)
-    hits, _, _, _ = oh.trace_keyed(crays, keys, 3 * g + 2 * b, P, False)
+    hits, _, _, _ = oh.trace_keyed(crays, keys, 3 * g + 2 * b, P, False, rl)
     spos0, snrm0 = oracle.resolve(s.positions, s.normals, s.material_ids, crays, hits, cpix, cw * chh)
     lp = np.array([l["position"] for l in s.lights], np.float32)
     L = len(lp)
@@ -210,10 +212,10 @@ def cpu_baseline(s, crop=(240, 136), threads=None, steps=1):
         for bnc in range(s.depth):
             t1 = time.perf_counter()
             srays, skeys = oracle.raygen_shadow(spos, snrm, cw, chh, lp, 0.01, lo, scale, g, b)
-            flags, R1, _, _ = oh.trace_keyed(srays, skeys, lbits + 3 * g + 2 * b, P, True)
+            flags, R1, _, _ = oh.trace_keyed(srays, skeys, lbits + 3 * g + 2 * b, P, True, rl)
             rrays, rkeys = oracle.raygen_reflect(spos, snrm, prev, cam[:3] if prev is None else None, cw, chh, 0.01,
                                                  s.jitter, s.seed, bnc, lo, scale, g, b)
-            rh, R2, _, _ = oh.trace_keyed(rrays, rkeys, 3 * g + 2 * b, P, False)
+            rh, R2, _, _ = oh.trace_keyed(rrays, rkeys, 3 * g + 2 * b, P, False, rl)
             spos, snrm = oracle.resolve(s.positions, s.normals, s.material_ids, rrays, rh, None, cw * chh)
             t_sec += time.perf_counter() - t1
             rays_total += R1 + R2

@@ -135,7 +135,7 @@ typedef struct rsh_config {
     uint32_t grid_bits;        /* hash origin grid bits per axis (default 4) */
     uint32_t dir_log2;         /* hash direction bins per axis, log2 (default 6) */
     uint32_t packet_size;      /* rays per hierarchy leaf: 8, 16 or 32 (default 8; Constants.h:29) */
-    uint32_t cluster_size;     /* triangles per object-hierarchy leaf: 1..64 (default 4) */
+    uint32_t cluster_size;     /* most triangles per object-hierarchy leaf: 1..64 (default 4; batched form <= 32) */
     float epsilon;             /* ray offset (default 0.01; RayTracer.cu:34) */
     uint64_t hbm_budget;       /* bytes the context may allocate (0: 90% of free memory) */
     uint64_t candidate_capacity; /* plain-path traversal candidates per pass (0: automatic) */
@@ -143,7 +143,7 @@ typedef struct rsh_config {
     float reflect_jitter;      /* 0: mirror reflections; >0: cosine-lobe perturbation weight */
     uint32_t seed;             /* seed of the reflection perturbation */
     uint32_t ray_level;        /* batched form: object-tree level at and below which rays leave their packet
-                                  and descend one by one (0: packets down to the clusters; default 3) */
+                                  and descend one by one (0: packets down to the clusters; default 4) */
 } rsh_config;
 
 #define RSH_FLAG_STAGE_TIMERS 1u   /* record per-stage CUDA events (TestManager timers) */

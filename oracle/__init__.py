@@ -66,6 +66,8 @@ def lib():
             "orc_objh_levels": (U32, [P]),
             "orc_objh_level_size": (U32, [P, U32]),
             "orc_objh_get": (None, [P, P, P, P]),
+            "orc_objh_kid_count": (U32, [P]),
+            "orc_objh_kids": (None, [P, P]),
             "orc_traverse": (U64, [P, P, U32, U32, U32, P, U64, P]),
             "orc_intersect": (None, [P, P, P, U32, U32, P, U64, I, P, P]),
             "orc_brute": (None, [P, U32, P, U32, I, P, P]),
@@ -195,6 +197,16 @@ class ObjH:
         lib().orc_objh_get(self.h, _p(order), _p(tris), _p(sph))
         return order, tris, sph[:total]
 
+    def kids(self) -> list[np.ndarray]:
+        """Per level: child-range starts (size + 1 entries; level 0: the clusters' triangle ranges)."""
+        flat = np.empty(max(lib().orc_objh_kid_count(self.h), 1), np.uint32)
+        lib().orc_objh_kids(self.h, _p(flat))
+        out, o = [], 0
+        for n in self.levels():
+            out.append(flat[o:o + n + 1].copy())
+            o += n + 1
+        return out
+
     def traverse(self, nodes, n, P, max_rays=None, cap=1 << 28):
         max_rays = n if max_rays is None else max_rays
         tests = np.zeros(1, np.uint64)
@@ -212,7 +224,7 @@ class ObjH:
                             int(any_hit), _p(flags), _p(hits))
         return flags if any_hit else hits
 
-    def trace_keyed(self, rays, keys, key_bits, P, any_hit, ray_level=3):
+    def trace_keyed(self, rays, keys, key_bits, P, any_hit, ray_level=4):
         rays = np.ascontiguousarray(rays, RAY_DTYPE)
         keys = _u32(keys)
         n = len(keys)

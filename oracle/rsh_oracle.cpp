@@ -357,17 +357,37 @@ Node merge_nodes(const Node* ch, uint32_t m) {
 struct ObjH {
     uint32_t T = 0, cluster = 8, levels = 0;
     uint32_t off[16] = {}, size[16] = {};
-    std::vector<float> sph;   // 4 per node
-    std::vector<float> tris;  // 12 per triangle, cluster order, w of vertex 0 = original id bits
+    uint32_t koff[16] = {};      // level l's child-range array starts at kid[koff[l]] (size[l] + 1 entries)
+    std::vector<float> sph;      // 4 per node
+    std::vector<uint32_t> kid;   // node j of level l: children [kid[koff[l]+j], kid[koff[l]+j+1]) of level l-1
+                                 // (level 0: the cluster's triangles)
+    std::vector<float> tris;     // 12 per triangle, cluster order, w of vertex 0 = original id bits
     std::vector<uint32_t> order;
 };
+
+// children of node (L, idx) at level L-1 (L == levels: the virtual root over the top level)
+inline void children(const ObjH& h, uint32_t L, uint32_t idx, uint32_t& first, uint32_t& cnt) {
+    if (L == h.levels) {
+        first = 0;
+        cnt = h.size[L - 1];
+        return;
+    }
+    const uint32_t* k = &h.kid[h.koff[L] + idx];
+    first = k[0];
+    cnt = k[1] - k[0];
+}
+// triangles of cluster c
+inline void cluster_tris(const ObjH& h, uint32_t c, uint32_t& t0, uint32_t& t1) {
+    t0 = h.kid[h.koff[0] + c];
+    t1 = h.kid[h.koff[0] + c + 1];
+}
 
 void traverse_packet(const Node& p, const ObjH& h, uint32_t L, uint32_t idx, std::vector<uint32_t>& clusters,
                      uint64_t& tests) {
     // children of (L, idx): level L-1 nodes [8 idx, ...) or the top level for the virtual root
     const uint32_t cl = L - 1;
-    const uint32_t first = (L == h.levels) ? 0 : 8 * idx;
-    const uint32_t cnt = std::min<uint32_t>(8, h.size[cl] - first);
+    uint32_t first, cnt;
+    children(h, L, idx, first, cnt);
     for (uint32_t c = 0; c < cnt; ++c) {
         const float* s = &h.sph[4ull * (h.off[cl] + first + c)];
         ++tests;
@@ -392,15 +412,16 @@ bool ray_descend(const ObjH& h, const Ray& r, const RayWT& w, uint32_t L0, uint3
         const uint32_t e = stk[--sp];
         const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
         const uint32_t cl = L - 1;
-        const uint32_t first = (L == h.levels) ? 0 : 8 * idx;
-        const uint32_t cnt = std::min<uint32_t>(8, h.size[cl] - first);
+        uint32_t first, cnt;
+        children(h, L, idx, first, cnt);
         rc.tmax = tcur;
         if (cl == 0) {
             for (uint32_t c = 0; c < cnt; ++c) {
                 ++ntests;
                 rc.tmax = tcur;
                 if (!ray_hits_sphere(rc, &h.sph[4ull * (h.off[0] + first + c)])) continue;
-                const uint32_t t0 = (first + c) * h.cluster, t1 = std::min(t0 + h.cluster, h.T);
+                uint32_t t0, t1;
+                cluster_tris(h, first + c, t0, t1);
                 for (uint32_t t = t0; t < t1; ++t) {
                     const float* v = &h.tris[12ull * t];
                     float th;
@@ -704,6 +725,12 @@ void orc_build_rsh(const float* rays_in, const uint32_t* ids, uint32_t n, uint32
 }
 
 // ---------------------------------------------------------------- object hierarchy
+// Restates the GPU build (objh.cu): Morton order of the triangle centroids; boundary strength before
+// sorted triangle k = highest differing bit of the 64-bit keys (code << 32 | k); level 0 groups triangles
+// into clusters of at most `cluster`, higher levels group the level below into nodes of at most 8, cutting
+// boundary j iff the range it splits (between the nearest stronger boundaries) holds more than G items
+// (fixed groups of G when a level would shrink less than 2x for clusters or 4x above); spheres from every
+// vertex of a node's triangle range; up to the first level of at most 8 nodes.
 static ObjH* g_last_objh = nullptr;
 
 static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const float lo[3], const float hi[3],
@@ -730,54 +757,88 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
     std::iota(h.order.begin(), h.order.end(), 0u);
     std::stable_sort(h.order.begin(), h.order.end(), [&](uint32_t a, uint32_t b) { return codes[a] < codes[b]; });
     h.tris.resize(12ull * T);
+    std::vector<uint32_t> scode(T);
     for (uint32_t k = 0; k < T; ++k) {
         const uint32_t t = h.order[k];
         std::memcpy(&h.tris[12ull * k], pos + 12ull * t, 48);
         h.tris[12ull * k + 3] = u2f(t);
+        scode[k] = codes[t];
     }
-    uint32_t sizes[16], levels = 0, cur = (T + cluster - 1) / cluster;
-    sizes[levels++] = cur;
-    while (cur > 8 && levels < 16) {
-        cur = (cur + 7) / 8;
-        sizes[levels++] = cur;
-    }
-    uint32_t total = 0;
-    for (uint32_t l = 0; l < levels; ++l) {
-        h.off[l] = total;
-        h.size[l] = sizes[l];
-        total += sizes[l];
-    }
-    h.levels = T ? levels : 0;
-    h.sph.assign(4ull * total, 0.0f);
-    for (uint32_t j = 0; j < sizes[0] && T; ++j) {
-        const uint32_t t0 = j * cluster, t1 = std::min(t0 + cluster, T);
-        float mn[3] = {INF, INF, INF}, mx[3] = {-INF, -INF, -INF};
-        for (uint32_t t = t0; t < t1; ++t)
-            for (int v = 0; v < 3; ++v)
-                for (int i = 0; i < 3; ++i) {
-                    mn[i] = std::fmin(mn[i], h.tris[12ull * t + 4 * v + i]);
-                    mx[i] = std::fmax(mx[i], h.tris[12ull * t + 4 * v + i]);
-                }
-        const V3 c = V3{(mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f};
-        float r2 = 0.f;
-        for (uint32_t t = t0; t < t1; ++t)
-            for (int v = 0; v < 3; ++v) {
-                const float* p = &h.tris[12ull * t + 4 * v];
-                const V3 d = V3{p[0] - c.x, p[1] - c.y, p[2] - c.z};
-                r2 = std::fmax(r2, dot(d, d));
+    h.levels = 0;
+    h.sph.clear();
+    h.kid.clear();
+    if (T == 0) return;
+    // boundary strength before sorted triangle k: highest differing bit of the 64-bit keys
+    // (code << 32 | k) of triangles k-1 and k; 64 at both ends
+    auto dtri = [&](uint32_t k) -> uint32_t {
+        if (k == 0 || k >= T) return 64u;
+        const uint32_t a = scode[k - 1], b = scode[k];
+        if (a != b) return 32u + (31u - (uint32_t)__builtin_clz(a ^ b));
+        return 31u - (uint32_t)__builtin_clz((k - 1) ^ k);
+    };
+    // items of the level being grouped: start[j] = first triangle of item j (start[n] = T)
+    std::vector<uint32_t> start(T + 1);
+    std::iota(start.begin(), start.end(), 0u);
+    uint32_t n = T;
+    uint32_t total_nodes = 0, total_kids = 0;
+    std::vector<std::vector<uint32_t>> lvl_first;  // per level: child-range starts (+ sentinel)
+    std::vector<std::vector<uint32_t>> lvl_tri;    // per level: triangle-range starts (+ sentinel)
+    while (true) {
+        const uint32_t l = h.levels;
+        const uint32_t G = (l == 0) ? cluster : 8u;
+        auto delta = [&](uint32_t j) -> uint32_t { return (j == 0 || j >= n) ? 64u : dtri(start[j]); };
+        std::vector<uint32_t> firsts;
+        for (uint32_t j = 0; j < n; ++j) {
+            bool cut = (j == 0);
+            if (!cut) {
+                const uint32_t d = delta(j);
+                int64_t lo = -1, hi = -1;
+                for (int64_t q = (int64_t)j - 1; q >= 0 && q >= (int64_t)j - (int64_t)G; --q)
+                    if (delta((uint32_t)q) > d) {
+                        lo = q;
+                        break;
+                    }
+                for (uint64_t q = (uint64_t)j + 1; q <= n && q <= (uint64_t)j + G; ++q)
+                    if (delta((uint32_t)q) > d) {
+                        hi = (int64_t)q;
+                        break;
+                    }
+                cut = lo < 0 || hi < 0 || (hi - lo) > (int64_t)G;
             }
-        float* s = &h.sph[4ull * j];
-        s[0] = c.x;
-        s[1] = c.y;
-        s[2] = c.z;
-        s[3] = std::sqrt(r2) * kRadSlack;
+            if (cut) firsts.push_back(j);
+        }
+        uint64_t nn = firsts.size();
+        // fixed groups of G when the Morton groups reduce too little (>= 2x for clusters, >= 4x above)
+        if ((l == 0 && nn * 2 > (uint64_t)n + 1) || (l > 0 && nn * 4 > (uint64_t)n + 3)) {
+            firsts.clear();
+            for (uint32_t j = 0; j < n; j += G) firsts.push_back(j);
+            nn = firsts.size();
+        }
+        firsts.push_back(n);
+        std::vector<uint32_t> tstart(nn + 1);
+        for (uint64_t g = 0; g <= nn; ++g) tstart[g] = start[firsts[g]];
+        h.off[l] = total_nodes;
+        h.size[l] = (uint32_t)nn;
+        h.koff[l] = total_kids;
+        total_nodes += (uint32_t)nn;
+        total_kids += (uint32_t)nn + 1;
+        lvl_first.push_back(firsts);
+        lvl_tri.push_back(tstart);
+        h.levels = l + 1;
+        start.assign(tstart.begin(), tstart.end());
+        n = (uint32_t)nn;
+        if (n <= 8 || h.levels >= 16) break;
     }
-    // upper levels: the same formula over every vertex of the subtree (triangles [j span, (j+1) span))
-    uint64_t span = cluster;
-    for (uint32_t l = 1; l < levels && T; ++l) {
-        span *= 8;
-        for (uint32_t j = 0; j < sizes[l]; ++j) {
-            const uint64_t t0 = (uint64_t)j * span, t1 = std::min<uint64_t>(t0 + span, T);
+    h.sph.assign(4ull * total_nodes, 0.0f);
+    h.kid.assign(total_kids, 0u);
+    for (uint32_t l = 0; l < h.levels; ++l) {
+        // level 0 stores the clusters' triangle ranges, higher levels their child ranges
+        const std::vector<uint32_t>& k = (l == 0) ? lvl_tri[0] : lvl_first[l];
+        std::memcpy(&h.kid[h.koff[l]], k.data(), 4ull * (h.size[l] + 1));
+        // spheres: midpoint of the vertex box, radius = max vertex distance (x (1 + 2^-20)), over every
+        // vertex of the node's triangle range
+        for (uint32_t j = 0; j < h.size[l]; ++j) {
+            const uint64_t t0 = lvl_tri[l][j], t1 = lvl_tri[l][j + 1];
             float mn[3] = {INF, INF, INF}, mx[3] = {-INF, -INF, -INF};
             for (uint64_t v = 3 * t0; v < 3 * t1; ++v)
                 for (int i = 0; i < 3; ++i) {
@@ -810,6 +871,12 @@ void* orc_objh_build(const float* pos, uint32_t T, uint32_t cluster, const float
 void orc_objh_free(void* hp) { delete static_cast<ObjH*>(hp); }
 uint32_t orc_objh_levels(void* hp) { return static_cast<ObjH*>(hp)->levels; }
 uint32_t orc_objh_level_size(void* hp, uint32_t l) { return static_cast<ObjH*>(hp)->size[l]; }
+// child ranges of every level, level after level (size[l] + 1 entries each; level 0: triangle ranges)
+uint32_t orc_objh_kid_count(void* hp) { return (uint32_t)static_cast<ObjH*>(hp)->kid.size(); }
+void orc_objh_kids(void* hp, uint32_t* out) {
+    const ObjH* h = static_cast<ObjH*>(hp);
+    std::memcpy(out, h->kid.data(), 4ull * h->kid.size());
+}
 void orc_objh_get(void* hp, uint32_t* order, float* tris, float* spheres) {
     const ObjH* h = static_cast<ObjH*>(hp);
     if (order) std::memcpy(order, h->order.data(), 4ull * h->T);
@@ -866,7 +933,8 @@ void orc_intersect(void* hp, const float* rays_in, const uint32_t* ids, uint32_t
             if (!(r.tmax > r.tmin)) continue;
             if (!ray_hits_sphere(r, &h.sph[4ull * cluster])) continue;
             const RayWT w = wt_setup(r);
-            const uint32_t t0 = cluster * h.cluster, t1 = std::min(t0 + h.cluster, h.T);
+            uint32_t t0, t1;
+            cluster_tris(h, cluster, t0, t1);
             for (uint32_t t = t0; t < t1; ++t) {
                 const float* v = &h.tris[12ull * t];
                 float th;
@@ -1053,8 +1121,8 @@ uint32_t orc_trace_keyed(void* hp, const float* rays_in, const uint32_t* keys, u
                         continue;
                     }
                     const uint32_t cl = L - 1;
-                    const uint32_t first = (L == h.levels) ? 0 : 8 * idx;
-                    const uint32_t cnt = std::min<uint32_t>(8, h.size[cl] - first);
+                    uint32_t first, cnt;
+                    children(h, L, idx, first, cnt);
                     float te[8];
                     uint32_t ci[8];
                     uint32_t nh = 0;
@@ -1080,7 +1148,8 @@ uint32_t orc_trace_keyed(void* hp, const float* rays_in, const uint32_t* keys, u
                                 if (occl[j]) continue;
                                 const Ray& ry = rays[ids[j]];
                                 if (!ray_hits_sphere(ry, &h.sph[4ull * (h.off[0] + c)])) continue;
-                                const uint32_t a0 = c * h.cluster, a1 = std::min(a0 + h.cluster, h.T);
+                                uint32_t a0, a1;
+                                cluster_tris(h, c, a0, a1);
                                 for (uint32_t t2i = a0; t2i < a1; ++t2i) {
                                     const float* v = &h.tris[12ull * t2i];
                                     float th;

@@ -186,13 +186,16 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         p.flags = g.flags;
         p.hits = reinterpret_cast<unsigned long long*>(g.hits);
         RSH_TRY(make_hash_params(sc, ctx->cfg, 0, p.hp));
-        if (sc->h.level_size[0] > (1u << 23)) {  // per-ray job words hold a level-1 node index in 20 bits
-            set_error("batched traversal supports at most 8,388,608 triangle clusters per scene");
+        // per-ray job words and packet stack entries hold an object-node index of level >= 1 in 20 bits;
+        // cluster triangles are staged in shared memory (at most 32)
+        if ((sc->h.levels > 1 && sc->h.level_size[1] > (1u << 20)) || sc->h.cluster > 32) {
+            set_error("batched traversal needs at most 1,048,576 level-1 object nodes and clusters of <= 32");
             return RSH_ERR_INVALID;
         }
         FusedSeg& f = pl.h_fsegs[s];
         std::memset(&f, 0, sizeof(f));
         f.spheres = sc->h.spheres;
+        f.kids = sc->h.kids;
         f.tris = sc->h.tris;
         f.tri_count = sc->tri_count;
         f.cluster = sc->h.cluster;

@@ -122,6 +122,7 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ta.d_count = d_count;
     ta.packet = P;
     ta.spheres = sc->h.spheres;
+    ta.kids = sc->h.kids;
     for (uint32_t l = 0; l < sc->h.levels; ++l) {
         ta.lvl_off[l] = sc->h.level_off[l];
         ta.lvl_size[l] = sc->h.level_size[l];
@@ -138,6 +139,7 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ta.err = ctx->d_err;
     IsectArgs ia{};
     ia.spheres = sc->h.spheres;
+    ia.kids = sc->h.kids;
     ia.tris = sc->h.tris;
     ia.tri_count = sc->tri_count;
     ia.cluster = sc->h.cluster;
@@ -282,7 +284,7 @@ void rsh_config_default(rsh_config* c) {
     c->flags = 0;
     c->reflect_jitter = 0.0f;
     c->seed = 0x5EED0000u;
-    c->ray_level = 3;
+    c->ray_level = 4;
 }
 
 static rsh_status validate_config(const rsh_config* c) {
@@ -602,6 +604,7 @@ rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* sc) {
     if (sc->mat) cudaFree(sc->mat);
     if (sc->materials) cudaFree(sc->materials);
     if (sc->h.spheres) cudaFree(sc->h.spheres);
+    if (sc->h.kids) cudaFree(sc->h.kids);
     if (sc->h.tris) cudaFree(sc->h.tris);
     if (sc->h.order) cudaFree(sc->h.order);
     if (ctx && ctx->allocated >= sc->bytes) ctx->allocated -= sc->bytes;
@@ -627,27 +630,28 @@ rsh_status rsh_scene_get_level(const rsh_scene* sc, uint32_t level, rsh_object_n
     const uint32_t n = sc->h.level_size[level];
     std::vector<float4> sp(n);
     RSH_CUDA(cudaMemcpy(sp.data(), sc->h.spheres + sc->h.level_off[level], 16ull * n, cudaMemcpyDeviceToHost));
-    // triangles per node at this level = cluster * 8^level
-    uint64_t span = sc->h.cluster;
-    for (uint32_t l = 0; l < level; ++l) span *= 8;
+    // child ranges of every level up to this one; a node's triangles = those of its children's range
+    const uint32_t nk = sc->h.level_off[level] + sc->h.level_size[level] + level + 1;
+    std::vector<uint32_t> kids(nk);
+    RSH_CUDA(cudaMemcpy(kids.data(), sc->h.kids, 4ull * nk, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> tstart(kids.begin(), kids.begin() + sc->h.level_size[0] + 1);
+    for (uint32_t l = 1; l <= level; ++l) {
+        const uint32_t* k = kids.data() + sc->h.level_off[l] + l;
+        std::vector<uint32_t> ts(sc->h.level_size[l] + 1);
+        for (uint32_t j = 0; j <= sc->h.level_size[l]; ++j) ts[j] = tstart[k[j]];
+        tstart.swap(ts);
+    }
+    const uint32_t* kl = kids.data() + sc->h.level_off[level] + level;
     for (uint32_t j = 0; j < n; ++j) {
         rsh_object_node& o = out[j];
         o.c[0] = sp[j].x;
         o.c[1] = sp[j].y;
         o.c[2] = sp[j].z;
         o.radius = sp[j].w;
-        const uint64_t f = span * j;
-        const uint64_t l = std::min<uint64_t>(f + span, sc->tri_count);
-        o.first_tri = (uint32_t)f;
-        o.tri_count = (uint32_t)(l - f);
-        if (level == 0) {
-            o.first_child = 0;
-            o.child_count = 0;
-        } else {
-            const uint32_t cs = sc->h.level_size[level - 1];
-            o.first_child = 8 * j;
-            o.child_count = std::min<uint32_t>(8, cs - 8 * j);
-        }
+        o.first_tri = tstart[j];
+        o.tri_count = tstart[j + 1] - tstart[j];
+        o.first_child = level == 0 ? 0u : kl[j];
+        o.child_count = level == 0 ? 0u : kl[j + 1] - kl[j];
     }
     return RSH_OK;
 }
@@ -830,6 +834,7 @@ rsh_status rsh_traverse(rsh_ctx* ctx, const rsh_scene* sc, const rsh_node* nodes
     ta.d_count = d_count;
     ta.packet = packet_size;
     ta.spheres = sc->h.spheres;
+    ta.kids = sc->h.kids;
     for (uint32_t l = 0; l < sc->h.levels; ++l) {
         ta.lvl_off[l] = sc->h.level_off[l];
         ta.lvl_size[l] = sc->h.level_size[l];
@@ -862,6 +867,7 @@ static rsh_status isect_stage(const rsh_scene* sc, const rsh_ray* rays, const ui
     if (sc->tri_count == 0 || max_rays == 0) return RSH_OK;
     IsectArgs ia{};
     ia.spheres = sc->h.spheres;
+    ia.kids = sc->h.kids;
     ia.tris = sc->h.tris;
     ia.tri_count = sc->tri_count;
     ia.cluster = sc->h.cluster;

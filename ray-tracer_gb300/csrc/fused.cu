@@ -138,8 +138,8 @@ RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t la
             const uint32_t e = stk[--sp];
             const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
             if (L == 0u) {
-                const uint32_t t0 = idx * sg.cluster;
-                const uint32_t t1 = (t0 + sg.cluster < sg.tri_count) ? t0 + sg.cluster : sg.tri_count;
+                uint32_t t0, t1;
+                cluster_tris(sg.kids, idx, t0, t1);
                 for (uint32_t tt = t0; tt < t1; ++tt) {
                     const float4 v0 = __ldg(sg.tris + 3ull * tt), v1 = __ldg(sg.tris + 3ull * tt + 1),
                                  v2 = __ldg(sg.tris + 3ull * tt + 2);
@@ -161,9 +161,8 @@ RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t la
                 }
             } else {
                 const uint32_t cl = L - 1u;
-                const uint32_t first = (L == sg.levels) ? 0u : 8u * idx;
-                const uint32_t size = sg.lvl_size[cl];
-                const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+                uint32_t first, cnt;
+                node_children(sg.kids, sg.lvl_off, sg.lvl_size, sg.levels, L, idx, first, cnt);
                 const float4* sb = sg.spheres + sg.lvl_off[cl] + first;
                 float te[8];
                 uint32_t ci[8];
@@ -359,9 +358,8 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
                     if (m == 0) continue;
                 }
                 const uint32_t cl = L - 1u;
-                const uint32_t first = (L == sg.levels) ? 0u : 8u * idx;
-                const uint32_t size = sg.lvl_size[cl];
-                const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+                uint32_t first, cnt;
+                node_children(sg.kids, sg.lvl_off, sg.lvl_size, sg.levels, L, idx, first, cnt);
                 const bool has = ch < cnt;
                 float4 Sph = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (has) Sph = __ldg(sg.spheres + sg.lvl_off[cl] + first + ch);
@@ -396,8 +394,8 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
                         const uint32_t pm = __shfl_sync(0xffffffffu, cm, c) & alive;
                         if (pm == 0) continue;
                         const uint32_t cluster = first + c;
-                        const uint32_t t0i = cluster * sg.cluster;
-                        const uint32_t t1i = (t0i + sg.cluster < sg.tri_count) ? t0i + sg.cluster : sg.tri_count;
+                        uint32_t t0i, t1i;
+                        cluster_tris(sg.kids, cluster, t0i, t1i);
                         const uint32_t K = t1i - t0i;
                         for (uint32_t j = lane; j < 3u * K; j += 32) S.tri[j] = __ldg(sg.tris + 3ull * t0i + j);
                         __syncwarp();

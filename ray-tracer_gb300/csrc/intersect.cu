@@ -39,8 +39,8 @@ __global__ void __launch_bounds__(256) k_intersect(IsectArgs a) {
         if (ANY && *(volatile uint32_t*)(a.flags + id) == RSH_OCCLUDED) continue;
         if (!ray_hits_sphere(o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, __ldg(a.spheres + cluster))) continue;
         const RayWT r = wt_setup(o, d);
-        const uint32_t t0 = cluster * a.cluster;
-        const uint32_t t1 = (t0 + a.cluster < a.tri_count) ? t0 + a.cluster : a.tri_count;
+        uint32_t t0, t1;
+        cluster_tris(a.kids, cluster, t0, t1);
         unsigned long long best = RSH_HIT_NONE;
         for (uint32_t t = t0; t < t1; ++t) {
             const float4 v0 = __ldg(a.tris + 3ull * t);
@@ -94,8 +94,8 @@ __global__ void __launch_bounds__(256) k_intersect_rays(IsectArgs a) {
             }
         }
         const RayWT r = wt_setup(o, d);
-        const uint32_t t0 = cluster * a.cluster;
-        const uint32_t t1 = (t0 + a.cluster < a.tri_count) ? t0 + a.cluster : a.tri_count;
+        uint32_t t0, t1;
+        cluster_tris(a.kids, cluster, t0, t1);
         unsigned long long best = RSH_HIT_NONE;
         for (uint32_t t = t0; t < t1; ++t) {
             const float4 v0 = __ldg(a.tris + 3ull * t);

@@ -106,6 +106,7 @@ struct ObjHierarchy {
     uint32_t level_off[16] = {};   // offsets into spheres
     uint32_t level_size[16] = {};
     float4* spheres = nullptr;     // all levels
+    uint32_t* kids = nullptr;      // per level l (at level_off[l] + l): level_size[l] + 1 child-range starts
     float4* tris = nullptr;        // cluster order, 3 per triangle, v0.w = original id bits
     uint32_t* order = nullptr;     // cluster slot -> original triangle id
 };
@@ -122,6 +123,7 @@ struct TravArgs {
     const uint32_t* d_count;
     uint32_t packet;
     const float4* spheres;
+    const uint32_t* kids;        // object-tree child ranges (level l at lvl_off[l] + l)
     uint32_t lvl_off[16];
     uint32_t lvl_size[16];
     uint32_t levels;
@@ -142,6 +144,7 @@ cudaError_t launch_traverse(const TravArgs& a, cudaStream_t s);
 // ---- intersection (intersect.cu)
 struct IsectArgs {
     const float4* spheres;       // cluster spheres (object-hierarchy level 0)
+    const uint32_t* kids;        // level 0 child ranges: cluster c holds triangles [kids[c], kids[c + 1])
     const float4* tris;
     uint32_t tri_count;
     uint32_t cluster;
@@ -163,6 +166,7 @@ cudaError_t launch_intersect(const IsectArgs& a, bool any_hit, cudaStream_t s);
 // ---- fused persistent traversal + intersection (fused.cu)
 struct FusedSeg {
     const float4* spheres;
+    const uint32_t* kids;          // object-tree child ranges (level l at lvl_off[l] + l)
     const float4* tris;
     uint32_t tri_count;
     uint32_t cluster;

@@ -4,15 +4,27 @@
 // packed as {centre, radius, firstTri, lastTri} (main.cpp:2445-2470) and culled against the top ray
 // nodes (CalculateBoundingSpheresIntersections, RayTracer.cu:1152-1280); triangles then get a bounding
 // sphere each (CreateTriangleBoundingSphere, :301-376) inside the descent. Here the object spheres
-// become a full sphere tree built on the GPU:
+// become a full sphere tree built on the GPU, level by level, every level a list of nodes whose children
+// are consecutive nodes of the level below:
 //   1. Morton code (10 bits per axis) of every triangle centroid over the cube around the scene box;
-//   2. stable onesweep sort of (code, triangle id) -> cluster order;
-//   3. gather triangles into cluster order (original id kept in the first vertex's w);
-//   4. level 0: one sphere per cluster of `cluster` consecutive triangles: centre = midpoint of the
-//      vertex box, radius = max vertex distance (x (1 + 2^-20));
-//   5. levels 1..: fan-out 8 over consecutive nodes (until a level has at most 8 nodes); each node's
-//      sphere from all vertices of its subtree by the same formula as the clusters.
-// Every sphere encloses every vertex below it, so the hierarchy never culls a real hit.
+//   2. stable onesweep sort of (code, triangle id) -> cluster order; gather the triangles (original id
+//      kept in the first vertex's w);
+//   3. boundary strength before sorted triangle k: the highest differing bit of the 64-bit keys
+//      (code << 32 | k) of triangles k-1 and k (the splits of a binary radix tree over the keys);
+//   4. level 0 groups triangles into clusters of at most `cluster`, every level above groups the level
+//      below into nodes of at most 8: the items are cut exactly where the recursive split at the
+//      strongest boundary would stop, i.e. boundary j is a cut iff the range it splits (bounded by the
+//      nearest stronger boundaries on either side) holds more than G items -- decided from a window of
+//      G items on each side; the cut positions are compacted with the compress kernel. A level whose
+//      groups would reduce too little (< 2x for clusters, < 4x above) is cut into fixed groups of G;
+//   5. every node's sphere from all vertices of its triangle range: centre = midpoint of the vertex
+//      box, radius = max vertex distance (x (1 + 2^-20));
+//   6. up to the first level with at most 8 nodes (the children of the virtual root).
+// Every sphere encloses every vertex below it, so the hierarchy never culls a real hit. Child ranges are
+// stored per level as size + 1 starts: node j of level l covers [kids[l][j], kids[l][j + 1]) of level l-1
+// (of the triangles, for level 0).
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -48,44 +60,73 @@ __global__ void k_gather_tris(const float4* __restrict__ pos, const uint32_t* __
     order[k] = t;
 }
 
-__global__ void k_leaf_spheres(const float4* __restrict__ tris, uint32_t n, uint32_t cluster,
-                               uint32_t nleaves, float4* __restrict__ sph) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nleaves) return;
-    const uint32_t t0 = j * cluster, t1 = (t0 + cluster < n) ? t0 + cluster : n;
-    const float inf = __int_as_float(0x7f800000);
-    float mnx = inf, mny = inf, mnz = inf, mxx = -inf, mxy = -inf, mxz = -inf;
-    for (uint32_t t = t0; t < t1; ++t)
-        for (int v = 0; v < 3; ++v) {
-            const float4 p = __ldg(tris + 3ull * t + v);
-            mnx = fminf(mnx, p.x);
-            mny = fminf(mny, p.y);
-            mnz = fminf(mnz, p.z);
-            mxx = fmaxf(mxx, p.x);
-            mxy = fmaxf(mxy, p.y);
-            mxz = fmaxf(mxz, p.z);
-        }
-    const v3 c = v3{(mnx + mxx) * 0.5f, (mny + mxy) * 0.5f, (mnz + mxz) * 0.5f};
-    float r2 = 0.f;
-    for (uint32_t t = t0; t < t1; ++t)
-        for (int v = 0; v < 3; ++v) {
-            const float4 p = __ldg(tris + 3ull * t + v);
-            const v3 d = v3{p.x - c.x, p.y - c.y, p.z - c.z};
-            r2 = fmaxf(r2, dot3(d, d));
-        }
-    sph[j] = make_float4(c.x, c.y, c.z, sqrtf(r2) * kRadSlack);
+// boundary strength before sorted triangle k (k = 0 and k = T: 64, stronger than any)
+__global__ void k_delta_tri(const uint32_t* __restrict__ scode, uint32_t T, uint32_t* __restrict__ dtri) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > T) return;
+    uint32_t d = 64u;
+    if (k > 0 && k < T) {
+        const uint32_t a = __ldg(scode + k - 1), b = __ldg(scode + k);
+        d = (a != b) ? 32u + (31u - (uint32_t)__clz(a ^ b)) : 31u - (uint32_t)__clz((k - 1) ^ k);
+    }
+    dtri[k] = d;
 }
 
-// Level >= 1: the same formula over every vertex of the node's subtree (one warp per node); tighter than
-// enclosing the children's spheres. Min/max and max reductions are exact in any order.
-__global__ void k_level_spheres(const float4* __restrict__ tris, uint32_t n, uint64_t span, uint32_t nnodes,
+// Cut flags of one level: key 0 (kept by the compaction) where a group starts, RSH_KEY_NONE elsewhere.
+// start == nullptr: the items are the triangles themselves.
+__global__ void k_level_cuts(const uint32_t* __restrict__ dtri, const uint32_t* __restrict__ start, uint32_t n,
+                             uint32_t G, uint32_t* __restrict__ cutkey) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    auto delta = [&](uint32_t q) -> uint32_t {
+        return (q == 0 || q >= n) ? 64u : __ldg(dtri + (start ? __ldg(start + q) : q));
+    };
+    bool cut = (j == 0);
+    if (!cut) {
+        const uint32_t d = delta(j);
+        int64_t lo = -1, hi = -1;
+        for (int64_t q = (int64_t)j - 1; q >= 0 && q >= (int64_t)j - (int64_t)G; --q)
+            if (delta((uint32_t)q) > d) {
+                lo = q;
+                break;
+            }
+        for (uint64_t q = (uint64_t)j + 1; q <= n && q <= (uint64_t)j + G; ++q)
+            if (delta((uint32_t)q) > d) {
+                hi = (int64_t)q;
+                break;
+            }
+        cut = lo < 0 || hi < 0 || (hi - lo) > (int64_t)G;
+    }
+    cutkey[j] = cut ? 0u : RSH_KEY_NONE;
+}
+
+__global__ void k_fixed_firsts(uint32_t* __restrict__ firsts, uint32_t nn, uint32_t G) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < nn) firsts[g] = g * G;
+}
+
+// Node g of the new level: children [firsts[g], firsts[g+1]) of the items, triangles
+// [start(firsts[g]), start(firsts[g+1])); writes the level's child-range starts (triangle starts at level 0)
+// and the new items' triangle starts (both nn + 1 entries).
+__global__ void k_level_nodes(const uint32_t* __restrict__ firsts, uint32_t nn, uint32_t n,
+                              const uint32_t* __restrict__ start, uint32_t T, bool level0,
+                              uint32_t* __restrict__ kids, uint32_t* __restrict__ new_start) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g > nn) return;
+    const uint32_t f = (g < nn) ? __ldg(firsts + g) : n;
+    const uint32_t ts = (f >= n) ? T : (start ? __ldg(start + f) : f);
+    kids[g] = level0 ? ts : f;
+    new_start[g] = ts;
+}
+
+// One warp per node: the sphere over every vertex of the node's triangle range. Min/max and max
+// reductions are exact in any order.
+__global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t* __restrict__ tstart, uint32_t nnodes,
                                 float4* __restrict__ sph) {
     const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (j >= nnodes) return;
-    const uint64_t t0 = (uint64_t)j * span;
-    const uint64_t t1 = (t0 + span < n) ? t0 + span : n;
-    const uint64_t v0 = 3 * t0, v1 = 3 * t1;
+    const uint64_t v0 = 3ull * __ldg(tstart + j), v1 = 3ull * __ldg(tstart + j + 1);
     const float inf = __int_as_float(0x7f800000);
     float mnx = inf, mny = inf, mnz = inf, mxx = -inf, mxy = -inf, mxz = -inf;
     for (uint64_t v = v0 + lane; v < v1; v += 32) {
@@ -119,7 +160,11 @@ __global__ void k_level_spheres(const float4* __restrict__ tris, uint32_t n, uin
 }
 
 size_t objh_scratch_bytes(uint32_t tri_count) {
-    return 4ull * tri_count * 2 + sort_scratch_bytes(tri_count, 30) + 4096;
+    const size_t T = tri_count;
+    // codes + sorted codes, sort scratch, then dtri, two start arrays, cut keys, firsts, compress outputs
+    const size_t a = 8 * T + 256;
+    const size_t b = std::max(sort_scratch_bytes(tri_count, 30), compress_scratch_bytes(tri_count)) + 256;
+    return a + b + 4 * (T + 1) * 7 + 4096;
 }
 
 cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint32_t cluster,
@@ -128,28 +173,13 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     (void)scratch_bytes;
     h.tri_count = n;
     h.cluster = cluster;
-    if (n == 0) {
-        h.levels = 0;
-        return cudaSuccess;
-    }
-    // level sizes
-    uint32_t sizes[16];
-    uint32_t levels = 0;
-    uint32_t cur = (n + cluster - 1) / cluster;
-    sizes[levels++] = cur;
-    while (cur > 8 && levels < 16) {
-        cur = (cur + 7) / 8;
-        sizes[levels++] = cur;
-    }
-    uint32_t total = 0;
-    for (uint32_t l = 0; l < levels; ++l) {
-        h.level_off[l] = total;
-        h.level_size[l] = sizes[l];
-        total += sizes[l];
-    }
-    h.levels = levels;
+    h.levels = 0;
+    if (n == 0) return cudaSuccess;
     cudaError_t e;
-    if ((e = cudaMalloc(&h.spheres, sizeof(float4) * total)) != cudaSuccess) return e;
+    // node capacity: level 0 holds at most n nodes, every level above at most (size + 3) / 4
+    const size_t node_cap = (size_t)n + (n + 2) / 3 + 64;
+    if ((e = cudaMalloc(&h.spheres, sizeof(float4) * node_cap)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h.kids, sizeof(uint32_t) * (node_cap + 16))) != cudaSuccess) return e;
     if ((e = cudaMalloc(&h.tris, sizeof(float4) * 3ull * n)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&h.order, sizeof(uint32_t) * n)) != cudaSuccess) return e;
 
@@ -157,7 +187,17 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     uint32_t* codes = reinterpret_cast<uint32_t*>(b);
     uint32_t* sorted_codes = codes + n;
     uint32_t* perm = reinterpret_cast<uint32_t*>(h.order);  // sorted values land in order[] first
-    void* sort_scratch = b + ((8ull * n + 255) & ~255ull);
+    char* work = b + ((8ull * n + 255) & ~255ull);
+    void* sort_scratch = work;
+    char* rest = work + ((std::max(sort_scratch_bytes(n, 30), compress_scratch_bytes(n)) + 255) & ~255ull);
+    uint32_t* dtri = reinterpret_cast<uint32_t*>(rest);
+    uint32_t* startA = dtri + (n + 1);
+    uint32_t* startB = startA + (n + 1);
+    uint32_t* cutkey = startB + (n + 1);
+    uint32_t* firsts = cutkey + (n + 1);
+    uint32_t* cko = firsts + (n + 1);
+    uint32_t* cbo = cko + (n + 1);
+    uint32_t* counts = cbo + (n + 1);
     v3 vlo = v3{lo[0], lo[1], lo[2]};
     v3 vsc;
     // one scale for all axes (the cube over the largest extent): Morton bits follow physical size, so a
@@ -181,23 +221,54 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     }
     k_gather_tris<<<(n + 255) / 256, 256, 0, s>>>(positions_dev, perm_tmp, n, h.tris, perm);
     note_launch();
+    k_delta_tri<<<(n + 256) / 256, 256, 0, s>>>(sorted_codes, n, dtri);
+    note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) {
         cudaFree(perm_tmp);
         return e;
     }
-    k_leaf_spheres<<<(sizes[0] + 127) / 128, 128, 0, s>>>(h.tris, n, cluster, sizes[0], h.spheres);
-    note_launch();
-    uint64_t span = cluster;
-    for (uint32_t l = 1; l < levels; ++l) {
-        span *= 8;
-        k_level_spheres<<<(sizes[l] * 32 + 127) / 128, 128, 0, s>>>(h.tris, n, span, sizes[l],
-                                                                   h.spheres + h.level_off[l]);
+    // levels, bottom up; each level's size is read back (a scene build, not a per-frame step)
+    uint32_t items = n, total = 0;
+    const uint32_t* start = nullptr;  // items of level 0 are the triangles
+    uint32_t* nstart = startA;
+    while (true) {
+        const uint32_t l = h.levels;
+        const uint32_t G = (l == 0) ? cluster : 8u;
+        k_level_cuts<<<(items + 255) / 256, 256, 0, s>>>(dtri, start, items, G, cutkey);
         note_launch();
+        if ((e = launch_compress(cutkey, items, firsts, cko, cbo, counts, work, err, s)) != cudaSuccess) break;
+        uint32_t nn = 0;
+        if ((e = cudaMemcpyAsync(&nn, counts, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+        // fixed groups of G when the Morton groups reduce too little
+        if ((l == 0 && 2ull * nn > (uint64_t)items + 1) || (l > 0 && 4ull * nn > (uint64_t)items + 3) || nn == 0) {
+            nn = (items + G - 1) / G;
+            k_fixed_firsts<<<(nn + 255) / 256, 256, 0, s>>>(firsts, nn, G);
+            note_launch();
+        }
+        if ((size_t)total + nn > node_cap) {
+            e = cudaErrorInvalidValue;
+            break;
+        }
+        h.level_off[l] = total;
+        h.level_size[l] = nn;
+        k_level_nodes<<<(nn + 256) / 256, 256, 0, s>>>(firsts, nn, items, start, n, l == 0,
+                                                       h.kids + total + l, nstart);
+        note_launch();
+        k_level_spheres<<<(nn * 32 + 127) / 128, 128, 0, s>>>(h.tris, nstart, nn, h.spheres + total);
+        note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        total += nn;
+        h.levels = l + 1;
+        start = nstart;
+        nstart = (nstart == startA) ? startB : startA;
+        items = nn;
+        if (items <= 8 || h.levels >= 16) break;
     }
-    e = cudaGetLastError();
-    cudaStreamSynchronize(s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
     cudaFree(perm_tmp);
-    return e != cudaSuccess ? e : cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return e2 != cudaSuccess ? e2 : cudaGetLastError();
 }
 
 }  // namespace rsh

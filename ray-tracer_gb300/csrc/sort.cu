@@ -173,7 +173,10 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
     // the first one holding an inclusive prefix; a not-yet-published word restarts the step there
     uint32_t excl = 0u;
     if (tile > 0) {
-        constexpr int LB = 8;
+#ifndef RSH_SORT_LB
+#define RSH_SORT_LB 8
+#endif
+        constexpr int LB = RSH_SORT_LB;
         int64_t j = (int64_t)tile - 1;
         uint32_t spins = 0;
         while (j >= 0) {

@@ -147,4 +147,24 @@ RSH_DEV unsigned long long hit_key(float t, uint32_t tri) {
     return ((unsigned long long)__float_as_uint(t) << 32) | (unsigned long long)tri;
 }
 
+// ---------------------------------------------------------------- object-tree child ranges
+// Children of object node (L, idx) at level L-1: [first, first + cnt). L == levels is the virtual root
+// over the top level. Level l's child-range starts sit at kids[lvl_off[l] + l].
+RSH_DEV void node_children(const uint32_t* __restrict__ kids, const uint32_t* lvl_off, const uint32_t* lvl_size,
+                           uint32_t levels, uint32_t L, uint32_t idx, uint32_t& first, uint32_t& cnt) {
+    if (L == levels) {
+        first = 0u;
+        cnt = lvl_size[L - 1];
+        return;
+    }
+    const uint32_t* k = kids + lvl_off[L] + L + idx;
+    first = __ldg(k);
+    cnt = __ldg(k + 1) - first;
+}
+// Triangles of cluster c: [t0, t1).
+RSH_DEV void cluster_tris(const uint32_t* __restrict__ kids, uint32_t c, uint32_t& t0, uint32_t& t1) {
+    t0 = __ldg(kids + c);
+    t1 = __ldg(kids + c + 1);
+}
+
 }  // namespace rsh

@@ -54,9 +54,8 @@ RSH_DEV bool ray_emit(const TravArgs& a, uint32_t k, float4 o, float4 d, uint32_
         const uint32_t e = stk[--sp];
         const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
         const uint32_t cl = L - 1u;
-        const uint32_t first = (L == a.levels) ? 0u : 8u * idx;
-        const uint32_t size = a.lvl_size[cl];
-        const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+        uint32_t first, cnt;
+        node_children(a.kids, a.lvl_off, a.lvl_size, a.levels, L, idx, first, cnt);
         const float4* sb = a.spheres + a.lvl_off[cl] + first;
         for (uint32_t c = 0; c < cnt; ++c) {
             ++tests;
@@ -154,9 +153,8 @@ __global__ void __launch_bounds__(TV_WARPS * 32) k_traverse(TravArgs a) {
                 }
             }
             const uint32_t cl = L - 1u;
-            const uint32_t first = (L == levels) ? 0u : 8u * idx;
-            const uint32_t size = a.lvl_size[cl];
-            const uint32_t cnt = (size - first < 8u) ? size - first : 8u;
+            uint32_t first, cnt;
+            node_children(a.kids, a.lvl_off, a.lvl_size, levels, L, idx, first, cnt);
             const bool has = ch < cnt;
             float4 S = make_float4(0.f, 0.f, 0.f, 0.f);
             if (has) S = __ldg(a.spheres + a.lvl_off[cl] + first + ch);

@@ -56,6 +56,7 @@ def compute():
     nodes, off = oracle.build_rsh(rrays, di, len(di), P, max_rays=W * H)
     oh = oracle.ObjH(s.positions, K, lo, hi)
     order, tris, sph = oh.arrays()
+    kids = np.concatenate(oh.kids())
     cand, _ = oh.traverse(nodes, len(di), P, max_rays=W * H)
     rhits = oh.intersect(rrays, di, len(di), P, cand, False, W * H)
     valid_s = skeys != oracle.KEY_NONE
@@ -63,7 +64,7 @@ def compute():
     return dict(cam=cam, prays=prays.view(np.uint8), pix=pix, phits=phits, spos=spos, snrm=snrm, skeys=skeys,
                 srays=srays.view(np.uint8), sflags=sflags.astype(np.uint32), rkeys=rkeys, rrays=rrays.view(np.uint8),
                 trimmed=tr, ckeys=ck, cbases=cb, csizes=cs, skeys_sorted=sk, svals_sorted=sv, dec_keys=dk,
-                dec_ids=di, nodes=nodes.view(np.uint8), node_off=off, order=order, sph=sph, cand=cand,
+                dec_ids=di, nodes=nodes.view(np.uint8), node_off=off, order=order, sph=sph, kids=kids, cand=cand,
                 rhits=rhits)
 
 

@@ -280,9 +280,23 @@ def test_object_hierarchy_bitexact(ctx, which, cornell, soup_scene):
     assert len(levels[-1]) <= 8
     flat = np.concatenate([np.stack([l["c"][:, 0], l["c"][:, 1], l["c"][:, 2], l["radius"]], 1) for l in levels])
     assert flat.astype(np.float32).tobytes() == sph.tobytes()
-    # every vertex lies inside its cluster sphere
+    # explicit child ranges equal the oracle's; clusters hold <= 8 triangles, nodes <= 8 children
+    kids = oh.kids()
     T = s.tri_count
-    cl = np.arange(T) // 8
+    assert np.array_equal(np.append(levels[0]["first_tri"], T), kids[0])
+    assert levels[0]["tri_count"].max() <= 8 and levels[0]["tri_count"].min() >= 1
+    for l in range(1, len(levels)):
+        assert np.array_equal(np.append(levels[l]["first_child"], len(levels[l - 1])), kids[l])
+        assert levels[l]["child_count"].max() <= 8 and levels[l]["child_count"].min() >= 1
+        # a node's triangles are exactly its children's
+        fc, cc = levels[l]["first_child"], levels[l]["child_count"]
+        below = levels[l - 1]
+        assert np.array_equal(levels[l]["first_tri"], below["first_tri"][fc])
+        last = fc + cc - 1
+        assert np.array_equal(levels[l]["first_tri"] + levels[l]["tri_count"],
+                              below["first_tri"][last] + below["tri_count"][last])
+    # every vertex lies inside its cluster sphere
+    cl = np.repeat(np.arange(len(levels[0])), levels[0]["tri_count"])
     v = tris.reshape(T, 3, 4)[:, :, :3]
     c = flat[cl, :3]
     d = np.linalg.norm(v - c[:, None, :], axis=2).max(1)
