@@ -135,7 +135,7 @@ typedef struct rsh_config {
     uint32_t grid_bits;        /* hash origin grid bits per axis (default 4) */
     uint32_t dir_log2;         /* hash direction bins per axis, log2 (default 6) */
     uint32_t packet_size;      /* rays per hierarchy leaf: 8, 16 or 32 (default 8; Constants.h:29) */
-    uint32_t cluster_size;     /* most triangles per object-hierarchy leaf: 1..64 (default 4; batched form <= 32) */
+    uint32_t cluster_size;     /* most triangles per object-hierarchy leaf: 1..64 (default 6; batched form <= 32) */
     float epsilon;             /* ray offset (default 0.01; RayTracer.cu:34) */
     uint64_t hbm_budget;       /* bytes the context may allocate (0: 90% of free memory) */
     uint64_t candidate_capacity; /* plain-path traversal candidates per pass (0: automatic) */

@@ -277,7 +277,7 @@ void rsh_config_default(rsh_config* c) {
     c->grid_bits = 4;
     c->dir_log2 = 6;
     c->packet_size = 8;
-    c->cluster_size = 4;
+    c->cluster_size = 6;
     c->epsilon = 0.01f;
     c->hbm_budget = 0;
     c->candidate_capacity = 0;
