@@ -72,6 +72,24 @@ RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
 
 RSH_DEV uint32_t job_word(uint32_t i, uint32_t L, uint32_t idx) { return i | (L << 8) | (idx << 12); }
 
+// Ray vs sphere cull of a per-ray job, with the relative slack of ray_hits_sphere (about 100x the
+// rounding error of the cross and dot products, so the cull stays conservative); tc = distance along the
+// ray to the sphere's near side, the nearest-first order key. It only culls and decides no result, so it
+// uses fused multiply-adds (the library is otherwise built without contraction).
+RSH_DEV bool job_hits_sphere(float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
+                             float4 s, float& tc) {
+    const float vx = s.x - ox, vy = s.y - oy, vz = s.z - oz;
+    const float t = fmaf(vz, dz, fmaf(vy, dy, vx * dx));
+    const float wx = fmaf(vy, dz, -(vz * dy));
+    const float wy = fmaf(vz, dx, -(vx * dz));
+    const float wz = fmaf(vx, dy, -(vy * dx));
+    const float perp2 = fmaf(wz, wz, fmaf(wy, wy, wx * wx));
+    const float slack = (((fabsf(vx) + fabsf(vy)) + fabsf(vz)) + s.w) * 1e-5f;
+    const float r = s.w + slack;
+    tc = t - s.w;
+    return !(perp2 > r * r) && !(t + r < tmin) && !(t - r > tmax);
+}
+
 template <int P>
 RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t lane, unsigned long long& ntests,
                       unsigned long long& ttests, uint32_t* err) {
@@ -170,8 +188,12 @@ RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t la
                 for (uint32_t c = 0; c < cnt; ++c) {
                     const float4 q = __ldg(sb + c);
                     ++ntests;
-                    if (!ray_hits_sphere(ox, oy, oz, dx, dy, dz, tmin, tcur, q)) continue;
-                    const float tc = ((q.x - ox) * dx + (q.y - oy) * dy) + (q.z - oz) * dz - q.w;
+                    float tc;
+                    if (!job_hits_sphere(ox, oy, oz, dx, dy, dz, tmin, tcur, q, tc)) continue;
+                    if (any) {  // any hit: the order of the subtrees does not change the result, skip sorting
+                        ci[nh++] = first + c;
+                        continue;
+                    }
                     uint32_t k = nh++;  // keep te[] sorted descending (farthest first)
                     while (k > 0 && te[k - 1] < tc) {
                         te[k] = te[k - 1];
