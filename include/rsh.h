@@ -148,6 +148,11 @@ typedef struct rsh_config {
 
 #define RSH_FLAG_STAGE_TIMERS 1u   /* record per-stage CUDA events (TestManager timers) */
 #define RSH_FLAG_FUSED 2u          /* rsh_render_frame traces each bounce through the batched form */
+/* rsh_render_frame casts 16 shadow rays per light from the reference's soft-shadow grid around the light
+ * and shades with its sample weights and log2(1 + 2 s) factor (SOFT_SHADOWS, RayTracer.cu:1550-1603,
+ * 1680-1696); shadow slots per pixel = lights x 16. Each sample is traced exactly (the reference tests the
+ * samples only against the centre ray's candidate triangles). */
+#define RSH_FLAG_SOFT_SHADOWS 8u
 #define RSH_FLAG_RAH 4u            /* plain path: ray-hierarchy ablation without hashing/sorting: packets
                                       of consecutive trimmed rays (the reference's algorithm 1 "RAH",
                                       main.cpp:1016-1037) */
@@ -278,6 +283,15 @@ rsh_status rsh_raygen_shadow(const float* surface_pos, const float* surface_nrm,
                              uint32_t height, const rsh_light* lights_host, uint32_t light_count,
                              float epsilon, const rsh_hash_params* hp, rsh_ray* rays, uint32_t* keys,
                              rsh_stream_t stream);
+
+/* Soft-shadow rays: 16 per (pixel, light) from the 4x4 grid around the light without its centre
+ * (RayTracer.cu:1550-1599). Slot of (x, y, light l, sample k) = x + W*((16 l + k) + 16 L y); sample k =
+ * i + 4 j sits at light + axis0 (a - 2) / 8 + axis1 (b - 2) / 8 with a = i, b = j skipping 2; the hash tag
+ * is 16 l + k, so hp->tag_bits must cover 16 L. Rays exist where the centre ray of rsh_raygen_shadow does. */
+rsh_status rsh_raygen_soft_shadow(const float* surface_pos, const float* surface_nrm, uint32_t width,
+                                  uint32_t height, const rsh_light* lights_host, uint32_t light_count,
+                                  float epsilon, const rsh_hash_params* hp, rsh_ray* rays, uint32_t* keys,
+                                  rsh_stream_t stream);
 
 /* Reflection rays from a surface buffer. prev_rays == NULL: the surface is the primary G-buffer and
  * the incident direction is (p - eye); otherwise it is prev_rays[slot].d (the ray that hit it).

@@ -55,6 +55,9 @@ def lib():
             "orc_hash": (None, [P, U32, P, P, U32, U32, U32, P]),
             "orc_raygen_primary": (None, [P, U32, U32, P, P]),
             "orc_raygen_shadow": (None, [P, P, U32, U32, P, U32, F, P, P, U32, U32, P, P]),
+            "orc_raygen_shadow_samples": (None, [P, P, U32, U32, P, U32, U32, F, P, P, U32, U32, P, P]),
+            "orc_shade": (None, [P, P, P, U32, P, P, U32, U32, P, U32, U32, P, U32, P]),
+            "orc_pack": (None, [P, U32, P]),
             "orc_raygen_reflect": (None, [P, P, P, P, U32, U32, F, F, U32, U32, P, P, U32, U32, P, P]),
             "orc_compress": (None, [P, U32, P, P, P, P, P]),
             "orc_sort_pairs": (None, [P, P, U32, U32, P, P]),
@@ -119,14 +122,38 @@ def raygen_primary(cam: np.ndarray, W: int, H: int):
     return rays, pix
 
 
-def raygen_shadow(spos, snrm, W, H, light_pos, eps, lo, scale, g, b):
+def raygen_shadow(spos, snrm, W, H, light_pos, eps, lo, scale, g, b, samples=1):
+    """Shadow rays; samples = 16: the soft-shadow grid around each light (slot x + W (l*16 + s + L*16 y))."""
     light_pos = _f32(np.asarray(light_pos).reshape(-1, 3))
     L = light_pos.shape[0]
-    rays = np.zeros(W * H * L, RAY_DTYPE)
-    keys = np.empty(W * H * L, np.uint32)
-    lib().orc_raygen_shadow(_p(_f32(spos)), _p(_f32(snrm)), W, H, _p(light_pos), L, float(eps), _p(_f32(lo)),
-                            _p(_f32(scale)), g, b, _p(rays), _p(keys))
+    n = W * H * L * samples
+    rays = np.zeros(n, RAY_DTYPE)
+    keys = np.empty(n, np.uint32)
+    sp, sn, lo_, sc_ = _f32(spos), _f32(snrm), _f32(lo), _f32(scale)
+    lib().orc_raygen_shadow_samples(_p(sp), _p(sn), W, H, _p(light_pos), L, samples, float(eps), _p(lo_), _p(sc_),
+                                    g, b, _p(rays), _p(keys))
     return rays, keys
+
+
+def shade(spos, snrm, materials, shadow, accum, W, H, lights, eye, bounce, incident=None, samples=1):
+    """One surface buffer of Blinn-Phong shading into accum (W*H x 4 float32, updated in place).
+    lights: list of dicts {position, color, diffuse, specular}; materials: (M, 8) float32."""
+    lt = _f32(np.array([[*l["position"], *l.get("color", (1.0, 1.0, 1.0)), l.get("diffuse", 1.0),
+                         l.get("specular", 1.0)] for l in lights], np.float32))
+    mats = _f32(np.asarray(materials, np.float32).reshape(-1, 8))
+    inc = None if incident is None else np.ascontiguousarray(incident, RAY_DTYPE)
+    sp, sn, e3 = _f32(spos), _f32(snrm), _f32(np.asarray(eye, np.float32).reshape(3))
+    sh = None if shadow is None else _u32(shadow)
+    assert accum.dtype == np.float32 and accum.flags.c_contiguous
+    lib().orc_shade(_p(sp), _p(sn), _p(mats), mats.shape[0], _p(sh), _p(accum), W, H, _p(lt), len(lights), samples,
+                    _p(e3), bounce, _p(inc))
+
+
+def pack(accum):
+    n = accum.shape[0]
+    out = np.empty(n, np.uint32)
+    lib().orc_pack(_p(accum), n, _p(out))
+    return out
 
 
 def raygen_reflect(spos, snrm, prev, eye, W, H, eps, jitter, seed, bounce, lo, scale, g, b):

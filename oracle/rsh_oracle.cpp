@@ -525,44 +525,170 @@ void orc_raygen_primary(const float* cam /*eye,dir,right,up*/, uint32_t W, uint3
 
 // CreateShadowRays (RayTracer.cu:682-740): origin at the light, direction to the surface point, kept iff
 // N.(-d) > 0; the test interval is (eps, |light - p| - 2 eps) from the eps-offset origin (:1607-1611).
-void orc_raygen_shadow(const float* spos, const float* snrm, uint32_t W, uint32_t H, const float* light_pos,
-                       uint32_t L, float eps, const float lo[3], const float scale[3], uint32_t g, uint32_t b,
-                       float* rays_out, uint32_t* keys) {
+// Soft-shadow sample k (0..15) of a shadow ray with direction d from light position lp: the reference's
+// 4x4 grid around the light without its centre row/column (RayTracer.cu:1550-1599): k = i + 4 j,
+// a = i (+1 from i = 2), b = j (+1 from j = 2), position lp + axis0 (a - 2) / 8 + axis1 (b - 2) / 8 with
+// axis0 = cross(e, d) for the axis e picked by min(|dx|, max(|dy|, |dz|)), axis1 = cross(d, axis0).
+static V3 soft_sample_pos(V3 lp, V3 d, uint32_t k) {
+    const uint32_t i = k & 3u, j = k >> 2;
+    const float ca = (float)((int)(i + (i >= 2u ? 1u : 0u)) - 2), cb = (float)((int)(j + (j >= 2u ? 1u : 0u)) - 2);
+    const float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    const float mn = std::fmin(ax, std::fmax(ay, az));
+    const V3 e = (ax == mn) ? V3{1.f, 0.f, 0.f} : (ay == mn) ? V3{0.f, 1.f, 0.f} : V3{0.f, 0.f, 1.f};
+    const V3 a0 = cross(e, d);
+    const V3 a1 = cross(d, a0);
+    return V3{(lp.x + (a0.x * ca) * 0.125f) + (a1.x * cb) * 0.125f, (lp.y + (a0.y * ca) * 0.125f) + (a1.y * cb) * 0.125f,
+              (lp.z + (a0.z * ca) * 0.125f) + (a1.z * cb) * 0.125f};
+}
+
+// CreateShadowRays (RayTracer.cu:682-740): S = 1, or S = 16 soft-shadow samples per light. Slot of
+// (pixel x, y, light l, sample s) = x + W (v + L S y), v = l S + s; the hash tag is v.
+void orc_raygen_shadow_samples(const float* spos, const float* snrm, uint32_t W, uint32_t H, const float* light_pos,
+                               uint32_t L, uint32_t S, float eps, const float lo[3], const float scale[3], uint32_t g,
+                               uint32_t b, float* rays_out, uint32_t* keys) {
     const HashP hp = mkhp(lo, scale, g, b);
     Ray* rays = reinterpret_cast<Ray*>(rays_out);
-    const uint64_t n = (uint64_t)W * H * L;
+    const uint32_t V = L * S;
+    const uint64_t n = (uint64_t)W * H * V;
 #pragma omp parallel for schedule(static)
     for (int64_t si = 0; si < (int64_t)n; ++si) {
         const uint32_t slot = (uint32_t)si;
-        const uint32_t x = slot % W, l = (slot / W) % L, y = slot / (W * L);
+        const uint32_t x = slot % W, v = (slot / W) % V, y = slot / (W * V);
+        const uint32_t l = v / S, s = v % S;
         const uint32_t pix = y * W + x;
         uint32_t key = KEY_NONE;
         if (spos[4ull * pix + 3] != 0.0f) {
             const V3 p = V3{spos[4ull * pix], spos[4ull * pix + 1], spos[4ull * pix + 2]};
             const V3 nn = normalize(V3{snrm[4ull * pix], snrm[4ull * pix + 1], snrm[4ull * pix + 2]});
             const V3 lp = V3{light_pos[3 * l], light_pos[3 * l + 1], light_pos[3 * l + 2]};
-            const V3 v = sub(p, lp);
-            const float len = length(v);
-            const V3 d = V3{v.x / len, v.y / len, v.z / len};
+            const V3 vv = sub(p, lp);
+            const float len = length(vv);
+            const V3 d = V3{vv.x / len, vv.y / len, vv.z / len};
             const float diffuse = dot(d, V3{-nn.x, -nn.y, -nn.z});
             const float tmax = len - 2.0f * eps;
             if (diffuse > 0.0f && tmax > eps) {
-                const V3 o = add(lp, mul(d, eps));
-                Ray r;
-                r.o[0] = o.x;
-                r.o[1] = o.y;
-                r.o[2] = o.z;
-                r.tmin = eps;
-                r.d[0] = d.x;
-                r.d[1] = d.y;
-                r.d[2] = d.z;
-                r.tmax = tmax;
-                rays[slot] = r;
-                key = ray_hash(r.o, r.d, hp, l);
+                V3 src = lp, dir = d;
+                float tm = tmax;
+                bool ok = true;
+                if (S > 1) {
+                    src = soft_sample_pos(lp, d, s);
+                    const V3 vs = sub(p, src);
+                    const float ls = length(vs);
+                    dir = V3{vs.x / ls, vs.y / ls, vs.z / ls};
+                    tm = ls - 2.0f * eps;
+                    ok = tm > eps;
+                }
+                if (ok) {
+                    const V3 o = add(src, mul(dir, eps));
+                    Ray r;
+                    r.o[0] = o.x;
+                    r.o[1] = o.y;
+                    r.o[2] = o.z;
+                    r.tmin = eps;
+                    r.d[0] = dir.x;
+                    r.d[1] = dir.y;
+                    r.d[2] = dir.z;
+                    r.tmax = tm;
+                    rays[slot] = r;
+                    key = ray_hash(r.o, r.d, hp, v);
+                }
             }
         }
         if (key == KEY_NONE) rays[slot] = Ray{{0.f, 0.f, 0.f}, 0.f, {0.f, 0.f, 0.f}, -1.f};
         keys[slot] = key;
+    }
+}
+void orc_raygen_shadow(const float* spos, const float* snrm, uint32_t W, uint32_t H, const float* light_pos,
+                       uint32_t L, float eps, const float lo[3], const float scale[3], uint32_t g, uint32_t b,
+                       float* rays_out, uint32_t* keys) {
+    orc_raygen_shadow_samples(spos, snrm, W, H, light_pos, L, 1, eps, lo, scale, g, b, rays_out, keys);
+}
+
+// Soft-shadow weight of sample k (RayTracer.cu:1680-1690): inner four 0.55/16, corners 0.5375/16, edges
+// 0.525/16, summed over the unoccluded samples; the light's term is scaled by log2(1 + 2 sum).
+static float soft_weight(uint32_t k) {
+    if (k == 5 || k == 6 || k == 9 || k == 10) return 0.55f / 16.0f;
+    if (k == 0 || k == 3 || k == 12 || k == 15) return 0.5375f / 16.0f;
+    return 0.525f / 16.0f;
+}
+
+// Blinn-Phong shading of one surface buffer into the accumulators (ColorPrimaryShadowRay
+// RayTracer.cu:1616-1709, ColorReflectionRay :1776-1882): lights = L x {position[3], color[3], diffuse,
+// specular}, materials = M x {diffuse[4] (w = reflectance), specular[4] (w = shininess)}, shadow flags per
+// (pixel, light, sample) slot or NULL (unshadowed), accum = W*H x {rgb, carried reflectance}.
+// incident == NULL: the incident direction is p - eye.
+void orc_shade(const float* spos, const float* snrm, const float* materials, uint32_t nmat, const uint32_t* shadow,
+               float* accum, uint32_t W, uint32_t H, const float* lights, uint32_t L, uint32_t S, const float eye[3],
+               uint32_t bounce, const float* incident) {
+    const uint64_t npix = (uint64_t)W * H;
+#pragma omp parallel for schedule(static)
+    for (int64_t pi = 0; pi < (int64_t)npix; ++pi) {
+        const uint32_t pix = (uint32_t)pi;
+        float acc[4] = {0.f, 0.f, 0.f, 1.f};
+        if (bounce != 0)
+            for (int i = 0; i < 4; ++i) acc[i] = accum[4ull * pix + i];
+        const float* p4 = spos + 4ull * pix;
+        if (p4[3] != 0.0f && acc[3] > 0.0f) {
+            const V3 p = V3{p4[0], p4[1], p4[2]};
+            const float* n4 = snrm + 4ull * pix;
+            const V3 n = normalize(V3{n4[0], n4[1], n4[2]});
+            uint32_t mid = f2u(n4[3]);
+            if (mid >= nmat) mid = 0;
+            const float* md = materials + 8ull * mid;
+            const float* ms = md + 4;
+            V3 inc;
+            if (incident) {
+                const float* r = incident + 8ull * pix;
+                inc = V3{r[4], r[5], r[6]};
+            } else {
+                inc = normalize(sub(p, V3{eye[0], eye[1], eye[2]}));
+            }
+            const uint32_t x = pix % W, y = pix / W;
+            float cr = 0.f, cg = 0.f, cb = 0.f;
+            for (uint32_t l = 0; l < L; ++l) {
+                float factor = 1.0f;
+                if (S == 1) {
+                    if (shadow && shadow[x + W * (l + L * y)] == OCCLUDED) continue;
+                } else if (shadow) {
+                    float sf = 0.0f;
+                    for (uint32_t k = 0; k < S; ++k)
+                        if (shadow[x + W * ((l * S + k) + L * S * y)] != OCCLUDED) sf += soft_weight(k);
+                    factor = std::log2(1.0f + sf * 2.0f);
+                }
+                const float* Lt = lights + 8ull * l;
+                V3 ld = sub(V3{Lt[0], Lt[1], Lt[2]}, p);
+                const float dist = length(ld);
+                ld = V3{ld.x / dist, ld.y / dist, ld.z / dist};
+                const float att = 1.0f / (0.75f + dist * 0.0005f + dist * dist * 0.00005f);
+                const float diff = std::fmin(std::fmax(dot(ld, n), 0.0f), 1.0f);
+                if (diff > 0.0f) {
+                    const V3 hv = normalize(sub(ld, inc));
+                    const float sp = std::fmin(std::fmax(std::pow(std::fmax(dot(hv, n), 0.0f), ms[3]), 0.0f), 1.0f);
+                    const float kd = diff * Lt[6] * att * factor, ks = sp * Lt[7] * att * factor;
+                    cr += (md[0] * kd + ms[0] * ks) * Lt[3];
+                    cg += (md[1] * kd + ms[1] * ks) * Lt[4];
+                    cb += (md[2] * kd + ms[2] * ks) * Lt[5];
+                }
+            }
+            acc[0] += acc[3] * cr;
+            acc[1] += acc[3] * cg;
+            acc[2] += acc[3] * cb;
+            acc[3] *= md[3];
+        } else {
+            acc[3] = 0.0f;
+        }
+        for (int i = 0; i < 4; ++i) accum[4ull * pix + i] = acc[i];
+    }
+}
+
+// RgbToInt (RayTracer.cu:1702): clamp(c * 255) per channel, alpha 255.
+void orc_pack(const float* accum, uint32_t n, uint32_t* rgba) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* c = accum + 4ull * i;
+        const uint32_t r = (uint32_t)std::fmin(std::fmax(c[0] * 255.0f, 0.0f), 255.0f);
+        const uint32_t g = (uint32_t)std::fmin(std::fmax(c[1] * 255.0f, 0.0f), 255.0f);
+        const uint32_t b = (uint32_t)std::fmin(std::fmax(c[2] * 255.0f, 0.0f), 255.0f);
+        rgba[i] = r | (g << 8) | (b << 16) | (255u << 24);
     }
 }
 

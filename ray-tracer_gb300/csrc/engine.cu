@@ -735,6 +735,26 @@ rsh_status rsh_raygen_shadow(const float* surface_pos, const float* surface_nrm,
     if (light_count > (1u << hp->tag_bits)) return RSH_ERR_INVALID;
     LightsP lp{};
     lp.count = light_count;
+    lp.samples = 1;
+    for (uint32_t l = 0; l < light_count; ++l)
+        for (int i = 0; i < 3; ++i) lp.pos[l][i] = lights_host[l].position[i];
+    RSH_CUDA(launch_raygen_shadow(reinterpret_cast<const float4*>(surface_pos),
+                                  reinterpret_cast<const float4*>(surface_nrm), width, height, lp, epsilon,
+                                  to_hashp(*hp), rays, keys, stream));
+    return RSH_OK;
+}
+
+rsh_status rsh_raygen_soft_shadow(const float* surface_pos, const float* surface_nrm, uint32_t width,
+                                  uint32_t height, const rsh_light* lights_host, uint32_t light_count,
+                                  float epsilon, const rsh_hash_params* hp, rsh_ray* rays, uint32_t* keys,
+                                  rsh_stream_t stream) {
+    if (!surface_pos || !surface_nrm || !lights_host || !hp || !rays || !keys) return RSH_ERR_INVALID;
+    if (light_count == 0 || light_count > 8) return RSH_ERR_INVALID;
+    if (16ull * light_count > (1ull << hp->tag_bits)) return RSH_ERR_INVALID;
+    if ((uint64_t)width * height * light_count * 16 >= (1ull << 31)) return RSH_ERR_INVALID;
+    LightsP lp{};
+    lp.count = light_count;
+    lp.samples = 16;
     for (uint32_t l = 0; l < light_count; ++l)
         for (int i = 0; i < 3; ++i) lp.pos[l][i] = lights_host[l].position[i];
     RSH_CUDA(launch_raygen_shadow(reinterpret_cast<const float4*>(surface_pos),
@@ -935,7 +955,9 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
                             uint32_t* rgba_out, rsh_stream_t stream) {
     if (!ctx || !sc || W == 0 || H == 0 || !ctx->cam_set) return RSH_ERR_INVALID;
     if (ctx->light_count == 0 && depth > 0) return RSH_ERR_INVALID;
-    if ((uint64_t)W * H * (ctx->light_count ? ctx->light_count : 1) >= (1ull << 31)) return RSH_ERR_INVALID;
+    // soft shadows: 16 shadow rays per light (RayTracer.cu:1550-1603), shaded by :1680-1696
+    const uint32_t S = (ctx->cfg.flags & RSH_FLAG_SOFT_SHADOWS) ? 16u : 1u;
+    if ((uint64_t)W * H * (ctx->light_count ? ctx->light_count : 1) * S >= (1ull << 31)) return RSH_ERR_INVALID;
     cudaStream_t s = stream;
     const uint32_t L = ctx->light_count;
     const uint32_t npix = W * H;
@@ -943,15 +965,16 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     ctx->fw = W;
     ctx->fh = H;
     ctx->fdepth = depth;
-    ctx->flights = L;
+    ctx->flights = L * S;  // shadow slots per pixel
     ctx->last_stream = s;
     ctx->overflow_passes = 0;
     ctx->tev_used = 0;
     ctx->tmarks.clear();
     std::memset(&ctx->stats, 0, sizeof(ctx->stats));
     RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
+    const uint32_t LS = L * S;  // light samples per pixel
     uint32_t lbits = 0;
-    while ((1u << lbits) < L) ++lbits;
+    while ((1u << lbits) < LS) ++lbits;
     HashP hp_s, hp_r;
     RSH_TRY(make_hash_params(sc, ctx->cfg, 0, hp_r));
     // the batched form re-keys every segment itself (segment tag instead of the light tag)
@@ -968,12 +991,12 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     RSH_TRY(ensure_buf(ctx, ctx->surf0_nrm, 16ull * npix));
     void *accum, *keys, *keys2;
     RSH_TRY(ensure(ctx, "accum", 16ull * npix, &accum));
-    RSH_TRY(ensure(ctx, "keys", 4ull * npix * (L ? L : 1), &keys));
+    RSH_TRY(ensure(ctx, "keys", 4ull * npix * (LS ? LS : 1), &keys));
     RSH_TRY(ensure(ctx, "keys2", 4ull * npix, &keys2));
     for (uint32_t b = 0; b < depth; ++b) {
         BounceBufs& bb = ctx->bounce[b];
-        RSH_TRY(ensure_buf(ctx, bb.shadow_rays, sizeof(rsh_ray) * (size_t)npix * L));
-        RSH_TRY(ensure_buf(ctx, bb.shadow_flags, 4ull * npix * L));
+        RSH_TRY(ensure_buf(ctx, bb.shadow_rays, sizeof(rsh_ray) * (size_t)npix * LS));
+        RSH_TRY(ensure_buf(ctx, bb.shadow_flags, 4ull * npix * LS));
         RSH_TRY(ensure_buf(ctx, bb.refl_rays, sizeof(rsh_ray) * (size_t)npix));
         RSH_TRY(ensure_buf(ctx, bb.refl_hits, 8ull * npix));
         RSH_TRY(ensure_buf(ctx, bb.surf_pos, 16ull * npix));
@@ -1006,6 +1029,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     const rsh_ray* incident = nullptr;
     LightsP lp{};
     lp.count = L;
+    lp.samples = S;
     for (uint32_t l = 0; l < L; ++l)
         for (int i = 0; i < 3; ++i) lp.pos[l][i] = ctx->lights[l].position[i];
     ShadeArgs sa{};
@@ -1015,6 +1039,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     sa.w = W;
     sa.h = H;
     sa.lights = L;
+    sa.samples = S;
     for (uint32_t l = 0; l < L; ++l) sa.light[l] = ctx->lights[l];
     for (int i = 0; i < 3; ++i) sa.eye[i] = ctx->cam.eye[i];
     for (uint32_t b = 0; b < depth; ++b) {
@@ -1033,7 +1058,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
                                            static_cast<uint32_t*>(keys2), s));
             stage_end(ctx, th, s);
             rsh_batch_segment segs[2] = {
-                {sc, srays, npix * L, 1, nullptr, sflags},
+                {sc, srays, npix * LS, 1, nullptr, sflags},
                 {sc, rrays, npix, 0, reinterpret_cast<uint64_t*>(rhits), nullptr}};
             RSH_TRY(rsh_batch_trace(ctx, segs, 2, s));
             const uint32_t* seg_cnt = static_cast<const uint32_t*>(ctx->bufs["b_seg_cnt"].ptr);
@@ -1046,9 +1071,9 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
             th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);
             RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays,
                                           static_cast<uint32_t*>(keys), s));
-            RSH_CUDA(cudaMemsetAsync(sflags, 0, 4ull * npix * L, s));
+            RSH_CUDA(cudaMemsetAsync(sflags, 0, 4ull * npix * LS, s));
             stage_end(ctx, th, s);
-            RSH_TRY(trace_keyed(ctx, sc, srays, static_cast<uint32_t*>(keys), npix * L, hp_s.key_bits, true, sflags,
+            RSH_TRY(trace_keyed(ctx, sc, srays, static_cast<uint32_t*>(keys), npix * LS, hp_s.key_bits, true, sflags,
                                 nullptr, fc + 4 * b, s));
             // reflection batch
             th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);

@@ -66,7 +66,7 @@ struct rsh_ctx {
     rsh_camera cam{};
     bool cam_set = false;
     // frame state
-    uint32_t fw = 0, fh = 0, fdepth = 0, flights = 0;
+    uint32_t fw = 0, fh = 0, fdepth = 0, flights = 0;  // flights: shadow slots per pixel (lights x samples)
     std::vector<BounceBufs> bounce;
     rsh::DevBuf prim_rays, prim_hits, prim_pix, surf0_pos, surf0_nrm;
     rsh_frame_stats stats{};

@@ -37,6 +37,7 @@ inline HashP to_hashp(const rsh_hash_params& h) {
 
 struct LightsP {
     uint32_t count;
+    uint32_t samples;  // shadow rays per light: 1, or 16 (soft shadows)
     float pos[8][3];
 };
 
@@ -209,10 +210,11 @@ struct ShadeArgs {
     const float4* snrm;
     const rsh_material* materials;
     uint32_t material_count;
-    const uint32_t* shadow;   // W*H*L slots
+    const uint32_t* shadow;   // W*H*L*samples slots
     float4* accum;            // W*H rgb accumulators + weight in w
     uint32_t w, h;
     uint32_t lights;
+    uint32_t samples;         // shadow samples per light (1, or 16 for soft shadows)
     rsh_light light[8];
     float eye[3];
     uint32_t bounce;

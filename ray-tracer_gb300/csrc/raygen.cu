@@ -49,16 +49,33 @@ cudaError_t launch_raygen_primary(const CameraP& cam, uint32_t w, uint32_t h, rs
 }
 
 // ------------------------------------------------------------------ shadow rays
+// Soft-shadow sample k (0..15) around light position lp for the shadow direction d: the reference's 4x4
+// grid without its centre row/column (RayTracer.cu:1550-1599): k = i + 4 j, a = i (+1 from i = 2),
+// b = j (+1 from j = 2), position lp + axis0 (a - 2) / 8 + axis1 (b - 2) / 8, axis0 = cross(e, d) for the
+// axis e the reference picks by min(|dx|, max(|dy|, |dz|)), axis1 = cross(d, axis0) (neither normalised).
+RSH_DEV v3 soft_sample_pos(v3 lp, v3 d, uint32_t k) {
+    const uint32_t i = k & 3u, j = k >> 2;
+    const float ca = (float)((int)(i + (i >= 2u ? 1u : 0u)) - 2), cb = (float)((int)(j + (j >= 2u ? 1u : 0u)) - 2);
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    const float mn = fminf(ax, fmaxf(ay, az));
+    const v3 e = (ax == mn) ? v3{1.f, 0.f, 0.f} : (ay == mn) ? v3{0.f, 1.f, 0.f} : v3{0.f, 0.f, 1.f};
+    const v3 a0 = cross3(e, d);
+    const v3 a1 = cross3(d, a0);
+    return v3{(lp.x + (a0.x * ca) * 0.125f) + (a1.x * cb) * 0.125f, (lp.y + (a0.y * ca) * 0.125f) + (a1.y * cb) * 0.125f,
+              (lp.z + (a0.z * ca) * 0.125f) + (a1.z * cb) * 0.125f};
+}
+
 __global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* __restrict__ snrm,
                                 uint32_t w, uint32_t h, LightsP lights, float eps, HashP hp,
                                 rsh_ray* rays, uint32_t* keys) {
-    const uint32_t L = lights.count;
+    const uint32_t L = lights.count, S = lights.samples ? lights.samples : 1u, V = L * S;
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= w * h * L) return;
-    // slot = x + W*(l + L*y)  (RayTracer.cu:700-702)
+    if (slot >= w * h * V) return;
+    // slot = x + W*(v + L*S*y), v = l*S + s  (RayTracer.cu:700-702 with S samples per light)
     const uint32_t x = slot % w;
-    const uint32_t l = (slot / w) % L;
-    const uint32_t y = slot / (w * L);
+    const uint32_t v = (slot / w) % V;
+    const uint32_t y = slot / (w * V);
+    const uint32_t l = v / S, s = v % S;
     const uint32_t pix = y * w + x;
     const float4 p4 = __ldg(spos + pix);
     uint32_t key = RSH_KEY_NONE;
@@ -66,15 +83,28 @@ __global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* _
         const v3 p = mk3(p4);
         const v3 nn = norm3(mk3(__ldg(snrm + pix)));
         const v3 lp = mk3(lights.pos[l][0], lights.pos[l][1], lights.pos[l][2]);
-        const v3 v = p - lp;
-        const float len = len3(v);
-        const v3 d = v3{v.x / len, v.y / len, v.z / len};
+        const v3 vl = p - lp;
+        const float len = len3(vl);
+        const v3 d = v3{vl.x / len, vl.y / len, vl.z / len};
         const float diffuse = dot3(d, -nn);
         const float tmax = len - 2.0f * eps;
         if (diffuse > 0.0f && tmax > eps) {
-            const v3 o = lp + d * eps;
-            store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps), make_float4(d.x, d.y, d.z, tmax));
-            key = ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, hp, l);
+            v3 src = lp, dir = d;
+            float tm = tmax;
+            bool ok = true;
+            if (S > 1) {  // a sample of the 4x4 grid: its own origin, direction and interval
+                src = soft_sample_pos(lp, d, s);
+                const v3 vs = p - src;
+                const float ls = len3(vs);
+                dir = v3{vs.x / ls, vs.y / ls, vs.z / ls};
+                tm = ls - 2.0f * eps;
+                ok = tm > eps;
+            }
+            if (ok) {
+                const v3 o = src + dir * eps;
+                store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps), make_float4(dir.x, dir.y, dir.z, tm));
+                key = ray_hash(o.x, o.y, o.z, dir.x, dir.y, dir.z, hp, v);
+            }
         }
     }
     if (key == RSH_KEY_NONE)  // empty slot: an explicit no-ray (tmax < tmin) for consumers without keys
@@ -85,7 +115,7 @@ __global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* _
 cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_t w, uint32_t h,
                                  const LightsP& lights, float eps, const HashP& hp, rsh_ray* rays,
                                  uint32_t* keys, cudaStream_t s) {
-    const uint32_t n = w * h * lights.count;
+    const uint32_t n = w * h * lights.count * (lights.samples ? lights.samples : 1u);
     if (n == 0) return cudaSuccess;
     k_raygen_shadow<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, w, h, lights, eps, hp, rays, keys);
     note_launch();

@@ -149,6 +149,7 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
             const HashP& hp_s = hp_r;
             LightsP lp{};
             lp.count = L;
+            lp.samples = 1;
             for (uint32_t l = 0; l < L; ++l)
                 for (int i = 0; i < 3; ++i) lp.pos[l][i] = r.lights[l].position[i];
             RSH_CUDA(launch_raygen_shadow(q->spos, q->snrm, W, H, lp, s->ctx->cfg.epsilon, hp_s, q->srays, q->keys, st));

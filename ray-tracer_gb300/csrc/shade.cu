@@ -57,6 +57,14 @@ cudaError_t launch_resolve(const float4* tris_orig_pos, const float4* tris_orig_
     return cudaGetLastError();
 }
 
+// Soft-shadow weight of sample k (RayTracer.cu:1680-1690): inner four 0.55/16, corners 0.5375/16,
+// edges 0.525/16.
+RSH_DEV float soft_weight(uint32_t k) {
+    if (k == 5 || k == 6 || k == 9 || k == 10) return 0.55f / 16.0f;
+    if (k == 0 || k == 3 || k == 12 || k == 15) return 0.5375f / 16.0f;
+    return 0.525f / 16.0f;
+}
+
 __global__ void k_shade(ShadeArgs a) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= a.w * a.h) return;
@@ -79,9 +87,19 @@ __global__ void k_shade(ShadeArgs a) {
         }
         const uint32_t x = pix % a.w, y = pix / a.w;
         float cr = 0.f, cg = 0.f, cb = 0.f;
+        const uint32_t S = a.samples ? a.samples : 1u;
         for (uint32_t l = 0; l < a.lights; ++l) {
-            const uint32_t slot = x + a.w * (l + a.lights * y);
-            if (a.shadow && a.shadow[slot] == RSH_OCCLUDED) continue;
+            float factor = 1.0f;
+            if (S == 1) {
+                const uint32_t slot = x + a.w * (l + a.lights * y);
+                if (a.shadow && a.shadow[slot] == RSH_OCCLUDED) continue;
+            } else if (a.shadow) {
+                // soft shadows (RayTracer.cu:1680-1696): weighted unoccluded samples, log2(1 + 2 sum)
+                float sf = 0.0f;
+                for (uint32_t k = 0; k < S; ++k)
+                    if (a.shadow[x + a.w * ((l * S + k) + a.lights * S * y)] != RSH_OCCLUDED) sf += soft_weight(k);
+                factor = log2f(1.0f + sf * 2.0f);
+            }
             const rsh_light& L = a.light[l];
             v3 ld = v3{L.position[0], L.position[1], L.position[2]} - p;
             const float dist = len3(ld);
@@ -91,7 +109,7 @@ __global__ void k_shade(ShadeArgs a) {
             if (diff > 0.0f) {
                 const v3 hv = norm3(ld - inc);
                 const float sp = fminf(fmaxf(powf(fmaxf(dot3(hv, n), 0.0f), m.specular[3]), 0.0f), 1.0f);
-                const float kd = diff * L.diffuse_intensity * att, ks = sp * L.specular_intensity * att;
+                const float kd = diff * L.diffuse_intensity * att * factor, ks = sp * L.specular_intensity * att * factor;
                 cr += (m.diffuse[0] * kd + m.specular[0] * ks) * L.color[0];
                 cg += (m.diffuse[1] * kd + m.specular[1] * ks) * L.color[1];
                 cb += (m.diffuse[2] * kd + m.specular[2] * ks) * L.color[2];

@@ -26,6 +26,7 @@ OCCLUDED = 0xFFFFFFFF
 FLAG_STAGE_TIMERS = 1
 FLAG_FUSED = 2
 FLAG_RAH = 4
+FLAG_SOFT_SHADOWS = 8
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 NODE_DTYPE = np.dtype([("c", "<f4", 3), ("radius", "<f4"), ("axis", "<f4", 3), ("cos_spread", "<f4"),
@@ -161,6 +162,7 @@ SIGNATURES = {
     "rsh_hash_params_make": (C.c_int, [_P, _P, _U32, _U32, _U32, _P]),
     "rsh_raygen_primary": (C.c_int, [_P, _U32, _U32, _P, _P, _P]),
     "rsh_raygen_shadow": (C.c_int, [_P, _P, _U32, _U32, _P, _U32, _F, _P, _P, _P, _P]),
+    "rsh_raygen_soft_shadow": (C.c_int, [_P, _P, _U32, _U32, _P, _U32, _F, _P, _P, _P, _P]),
     "rsh_raygen_reflect": (C.c_int, [_P, _P, _P, _P, _U32, _U32, _F, _F, _U32, _U32, _P, _P, _P, _P]),
     "rsh_hash": (C.c_int, [_P, _U32, _P, _U32, _P, _P]),
     "rsh_compress": (C.c_int, [_P, _P, _U32, _P, _P, _P, _P, _P, _P]),

@@ -1,6 +1,7 @@
 """The per-frame path (rsh_render_frame) checked stage by stage against the oracle: every intermediate
 buffer of the frame is recomputed on the CPU from the GPU's previous stage and must match bit for bit;
-every hit record / shadow flag must equal the brute-force oracle."""
+every hit record / shadow flag must equal the brute-force oracle; the image must equal the oracle's
+shading of the same buffers within 2/255 per channel (host and device powf / log2f may differ by an ulp)."""
 import numpy as np
 import pytest
 
@@ -11,9 +12,10 @@ from rsh import scenes
 pytestmark = pytest.mark.gpu
 
 
-def _check_frame(ctx, s, sc, W, H, depth, jitter):
+def _check_frame(ctx, s, sc, W, H, depth, jitter, samples=1):
     lights = s.lights
     L = len(lights)
+    LS = L * samples
     cam = rsh.camera_look_at(s.eye, s.target, s.up, s.fov, W, H)
     ctx.set_camera(cam)
     ctx.set_lights(lights)
@@ -39,15 +41,18 @@ def _check_frame(ctx, s, sc, W, H, depth, jitter):
     prev = None
     lp = np.array([l["position"] for l in lights], np.float32)
     nshadow = nrefl = 0
+    accum = np.zeros((npix, 4), np.float32)
+    eye = cam.as_array()[:3]
     for bnc in range(depth):
-        srays = ctx.frame_rays(bnc, True, npix * L)
-        orays, okeys = oracle.raygen_shadow(spos, snrm, W, H, lp, ctx.config.epsilon, lo, scale, g, b)
+        srays = ctx.frame_rays(bnc, True, npix * LS)
+        orays, okeys = oracle.raygen_shadow(spos, snrm, W, H, lp, ctx.config.epsilon, lo, scale, g, b, samples)
         v = okeys != oracle.KEY_NONE
         nshadow += int(v.sum())
         assert srays[v].tobytes() == orays[v].tobytes()
-        sflags = ctx.frame_shadow(bnc, npix * L)
+        sflags = ctx.frame_shadow(bnc, npix * LS)
         assert np.array_equal(sflags[v], oracle.brute(s.positions, orays[v], True))
         assert np.all(sflags[~v] == 0)
+        oracle.shade(spos, snrm, s.materials, sflags, accum, W, H, lights, eye, bnc, prev, samples)
         rrays = ctx.frame_rays(bnc, False, npix)
         o_r, o_k = oracle.raygen_reflect(spos, snrm, prev, cam.as_array()[:3] if prev is None else None, W, H,
                                          ctx.config.epsilon, jitter, ctx.config.seed, bnc, lo, scale, g, b)
@@ -65,6 +70,11 @@ def _check_frame(ctx, s, sc, W, H, depth, jitter):
     assert st["shadow_rays"] == nshadow and st["reflection_rays"] == nrefl
     img = rgba.numpy()
     assert np.any(img & 0xFFFFFF)  # something was lit
+    # the last reflection surface is shaded once more, unshadowed, then packed
+    oracle.shade(spos, snrm, s.materials, None, accum, W, H, lights, eye, depth, prev, samples)
+    want = oracle.pack(accum)
+    diff = np.abs(img.view(np.uint8).reshape(-1, 4).astype(np.int32) - want.view(np.uint8).reshape(-1, 4))
+    assert diff.max() <= 2, diff.max()
     return st
 
 
@@ -137,3 +147,20 @@ def test_rah_ablation_same_results_more_work(cornell, ray_level):
         assert np.array_equal(a, b)
     if ray_level == 0:
         assert res[rsh.FLAG_RAH][1]["node_tests"] > res[0][1]["node_tests"]
+
+
+@pytest.mark.parametrize("flags", [0, rsh.FLAG_FUSED])
+def test_frame_soft_shadows(cornell, flags):
+    """RSH_FLAG_SOFT_SHADOWS: 16 shadow rays per light, each traced exactly, shaded with the reference's
+    sample weights; the same frame as the oracle in both forms, with a penumbra."""
+    W, H = 64, 48
+    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, reflect_jitter=1.0,
+                      flags=flags | rsh.FLAG_SOFT_SHADOWS)
+    sc = ctx.scene(cornell.positions, cornell.normals, cornell.material_ids, cornell.materials)
+    st = _check_frame(ctx, cornell, sc, W, H, 2, 1.0, samples=16)
+    flags0 = ctx.frame_shadow(0, W * H * 16).reshape(H, 16, W)
+    part = (flags0 != 0).any(axis=1) & ~(flags0 != 0).all(axis=1)
+    assert part.sum() > 0  # some pixels see part of the light
+    assert st["shadow_rays"] > 0
+    sc.destroy()
+    ctx.destroy()

@@ -83,6 +83,45 @@ def _primary_surface(s, W, H):
     return cam, spos, snrm
 
 
+def test_raygen_soft_shadow_bitexact(cornell):
+    """16 soft-shadow rays per (pixel, light) from the reference's 4x4 grid around the light
+    (RayTracer.cu:1550-1599): same rays and keys as the oracle; centre-invalid slots stay empty."""
+    s = cornell
+    W, H = 64, 48
+    cam, spos, snrm = _primary_surface(s, W, H)
+    lo, hi = _lohi(s)
+    lights = s.lights + [{"position": (0.5, 0.2, 0.9)}, {"position": (-0.7, 0.9, -0.2)}]
+    lp = np.array([l["position"] for l in lights], np.float32)
+    hp = rsh.hash_params(lo, hi, 5, 4, 6)
+    d_spos, d_snrm = rsh.DeviceArray.from_numpy(spos), rsh.DeviceArray.from_numpy(snrm)
+    n = W * H * len(lights) * 16
+    d_rays = rsh.DeviceArray(n, rsh.RAY_DTYPE, zero=True)
+    d_keys = rsh.DeviceArray(n, np.uint32)
+    larr = rsh.make_lights(lights)
+    rsh.check(rsh.lib().rsh_raygen_soft_shadow(d_spos.ptr, d_snrm.ptr, W, H, larr, len(lights), 0.01, C.byref(hp),
+                                               d_rays.ptr, d_keys.ptr, None), "soft shadow")
+    orays, okeys = oracle.raygen_shadow(spos, snrm, W, H, lp, 0.01, lo, np.array(hp.scale[:]), 5, 4, samples=16)
+    assert np.array_equal(d_keys.numpy(), okeys)
+    v = okeys != rsh.KEY_NONE
+    assert v.sum() > 1000
+    assert d_rays.numpy()[v].tobytes() == orays[v].tobytes()
+    # the 16 samples of a slot start at distinct points around the light and all end at the surface point
+    o = orays.reshape(H, len(lights), 16, W)
+    vv = v.reshape(H, len(lights), 16, W)
+    y, l, x = np.argwhere(vv.all(axis=2))[0]
+    starts = o["o"][y, l, :, x]
+    assert len({tuple(q) for q in starts.round(6)}) == 16
+    hc, _ = oracle.raygen_shadow(spos, snrm, W, H, lp, 0.01, lo, np.array(hp.scale[:]), 5, 4)
+    centre = hc.reshape(H, len(lights), W)[y, l, x]
+    end = starts + o["d"][y, l, :, x] * (o["tmax"][y, l, :, x] + 0.01)[:, None]  # o + d (tmax + eps) = p
+    end_c = centre["o"] + centre["d"] * (centre["tmax"] + 0.01)
+    assert np.allclose(end, end_c[None, :], atol=1e-4)
+    with pytest.raises(rsh.RshError):  # 4 lights x 16 samples need 6 tag bits
+        rsh.check(rsh.lib().rsh_raygen_soft_shadow(d_spos.ptr, d_snrm.ptr, W, H, larr, len(lights), 0.01,
+                                                   C.byref(rsh.hash_params(lo, hi, 5, 4, 2)), d_rays.ptr,
+                                                   d_keys.ptr, None), "soft shadow tag bits")
+
+
 @pytest.mark.parametrize("jitter", [0.0, 1.0])
 def test_raygen_secondary_bitexact(cornell, jitter):
     s = cornell
