@@ -223,6 +223,23 @@ uint64_t rsh_kernel_launches(void);
  * Replaces the flat-array packing + cudaMalloc/H2D + texture binds of main.cpp:2374-2586 and the
  * per-mesh Miniball spheres of BoundingSphere.cpp:9-63. */
 rsh_status rsh_scene_upload(rsh_ctx* ctx, const rsh_scene_desc* desc, rsh_scene** out);
+
+/* A scene read from a Wavefront OBJ file (+ its MTL files), in host memory, ready for rsh_scene_upload:
+ * desc's arrays are float4 x 3 per triangle (w = 1 for positions, 0 for normals), one material id and one
+ * object id per triangle; material 0 is the reader's default (0.75 grey, shininess 100), the MTL file's
+ * materials follow in file order with their Kd, Ks, Ns and reflectance 0.5. */
+typedef struct rsh_obj_data {
+    rsh_scene_desc desc;
+    uint32_t object_count;  /* "o" / "g" groups that hold faces */
+    void* owner;            /* internal */
+} rsh_obj_data;
+
+/* Reads an OBJ file: v, vn, f (v, v/vt, v//vn, v/vt/vn; 1-based or negative indices; polygons fanned into
+ * triangles), o/g, mtllib (relative to the OBJ file), usemtl. Faces without normals get their geometric
+ * normal. Replaces OBJ_Reader::loadMesh / loadMaterial (OBJ_Reader.cpp:60-389, 395-470), which read
+ * triangles only and stored zero normals where the file had none. Host only; free with rsh_obj_free. */
+rsh_status rsh_obj_load(const char* obj_path, rsh_obj_data** out);
+void rsh_obj_free(rsh_obj_data* data);
 rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* scene);
 /* Scene bounds (exact min/max over all vertices). */
 rsh_status rsh_scene_bounds(const rsh_scene* scene, float lo[3], float hi[3]);

@@ -77,6 +77,10 @@ class SceneDesc(C.Structure):
                 ("material_count", C.c_uint32)]
 
 
+class ObjData(C.Structure):
+    _fields_ = [("desc", SceneDesc), ("object_count", C.c_uint32), ("owner", C.c_void_p)]
+
+
 class FrameStats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("reflection_rays", C.c_uint64),
                 ("chunks", C.c_uint64), ("candidates", C.c_uint64), ("node_tests", C.c_uint64),
@@ -141,6 +145,8 @@ SIGNATURES = {
     "rsh_sm_count": (C.c_int, []),
     "rsh_kernel_launches": (_U64, []),
     "rsh_scene_upload": (C.c_int, [_P, _P, _P]),
+    "rsh_obj_load": (C.c_int, [C.c_char_p, _P]),
+    "rsh_obj_free": (None, [_P]),
     "rsh_scene_destroy": (C.c_int, [_P, _P]),
     "rsh_scene_bounds": (C.c_int, [_P, _P, _P]),
     "rsh_scene_triangle_count": (_U32, [_P]),
@@ -324,6 +330,31 @@ def make_lights(lights) -> "C.Array":
         arr[i].diffuse_intensity = float(l.get("diffuse", 1.0))
         arr[i].specular_intensity = float(l.get("specular", 1.0))
     return arr
+
+
+def load_obj(path) -> dict:
+    """Reads an OBJ (+ MTL) file through rsh_obj_load; returns numpy copies of the scene arrays:
+    positions / normals float32 [T,3,4], material_ids / object_ids uint32 [T], materials float32 [M,8]."""
+    ptr = C.POINTER(ObjData)()
+    check(lib().rsh_obj_load(str(path).encode(), C.byref(ptr)), "rsh_obj_load")
+    try:
+        d = ptr.contents.desc
+        T, M = d.triangle_count, d.material_count
+
+        def arr(addr, n, dt, shape):
+            if n == 0:
+                return np.zeros(shape, dt)
+            return np.ctypeslib.as_array(C.cast(addr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                         (n,)).reshape(shape).copy()
+        out = {"positions": arr(d.positions, 12 * T, np.float32, (T, 3, 4)),
+               "normals": arr(d.normals, 12 * T, np.float32, (T, 3, 4)),
+               "material_ids": arr(d.material_ids, T, np.uint32, (T,)),
+               "object_ids": arr(d.object_ids, T, np.uint32, (T,)),
+               "materials": arr(d.materials, 8 * M, np.float32, (M, 8)),
+               "object_count": ptr.contents.object_count}
+    finally:
+        lib().rsh_obj_free(ptr)
+    return out
 
 
 class Scene:
