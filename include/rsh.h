@@ -321,6 +321,15 @@ rsh_status rsh_raygen_reflect(const float* surface_pos, const float* surface_nrm
                               uint32_t bounce, const rsh_hash_params* hp, rsh_ray* rays,
                               uint32_t* keys, rsh_stream_t stream);
 
+/* Refraction rays from a surface buffer: direction refract(i, n, eta) by GLSL's formula (eta = 1/1.52 in
+ * the reference), i = normalize(p - eye) (prev_rays == NULL) or prev_rays[slot].d; no ray where the
+ * formula gives total internal reflection. Replaces CreateRefractionRays (RayTracer.cu:793-842), which
+ * the reference creates but never casts; the hash is the one of every other ray (the reference's
+ * CreateRefractionRayIndex, :200-227, hashes atan2(x, x), a constant). */
+rsh_status rsh_raygen_refract(const float* surface_pos, const float* surface_nrm, const rsh_ray* prev_rays,
+                              const float eye[3], uint32_t width, uint32_t height, float epsilon, float eta,
+                              const rsh_hash_params* hp, rsh_ray* rays, uint32_t* keys, rsh_stream_t stream);
+
 /* Hash of arbitrary rays; rays with tmax <= tmin get RSH_KEY_NONE. tag goes above the hash bits. */
 rsh_status rsh_hash(const rsh_ray* rays, uint32_t n, const rsh_hash_params* hp, uint32_t tag,
                     uint32_t* keys, rsh_stream_t stream);

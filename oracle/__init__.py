@@ -59,6 +59,7 @@ def lib():
             "orc_shade": (None, [P, P, P, U32, P, P, U32, U32, P, U32, U32, P, U32, P]),
             "orc_pack": (None, [P, U32, P]),
             "orc_raygen_reflect": (None, [P, P, P, P, U32, U32, F, F, U32, U32, P, P, U32, U32, P, P]),
+            "orc_raygen_refract": (None, [P, P, P, P, U32, U32, F, F, P, P, U32, U32, P, P]),
             "orc_compress": (None, [P, U32, P, P, P, P, P]),
             "orc_sort_pairs": (None, [P, P, U32, U32, P, P]),
             "orc_decompress": (None, [P, P, P, P, U32, U32, P, P]),
@@ -162,6 +163,17 @@ def raygen_reflect(spos, snrm, prev, eye, W, H, eps, jitter, seed, bounce, lo, s
     prev = None if prev is None else np.ascontiguousarray(prev, RAY_DTYPE)
     lib().orc_raygen_reflect(_p(_f32(spos)), _p(_f32(snrm)), _p(prev), _p(_f32(eye)), W, H, float(eps), float(jitter),
                              seed, bounce, _p(_f32(lo)), _p(_f32(scale)), g, b, _p(rays), _p(keys))
+    return rays, keys
+
+
+def raygen_refract(spos, snrm, prev, eye, W, H, eps, eta, lo, scale, g, b):
+    rays = np.zeros(W * H, RAY_DTYPE)
+    keys = np.empty(W * H, np.uint32)
+    prev = None if prev is None else np.ascontiguousarray(prev, RAY_DTYPE)
+    sp, sn, lo_, sc_ = _f32(spos), _f32(snrm), _f32(lo), _f32(scale)
+    e3 = None if eye is None else _f32(np.asarray(eye, np.float32).reshape(3))
+    lib().orc_raygen_refract(_p(sp), _p(sn), _p(prev), _p(e3), W, H, float(eps), float(eta), _p(lo_), _p(sc_), g, b,
+                             _p(rays), _p(keys))
     return rays, keys
 
 

@@ -715,6 +715,49 @@ static V3 sphere_sample(uint32_t seed, uint32_t slot, uint32_t bounce) {
 
 // CreateReflectionRays (RayTracer.cu:742-791) / ColorAndCreateReflectionRay (:1995-2016):
 // d = reflect(incident, n), origin offset by eps (:1765), optional cosine-lobe perturbation.
+// CreateRefractionRays (RayTracer.cu:793-842): refract(i, n, eta) by GLSL's formula, no ray on total
+// internal reflection, renormalised, origin offset by eps, interval (eps, inf); hash as every other ray.
+void orc_raygen_refract(const float* spos, const float* snrm, const float* prev_rays, const float eye[3], uint32_t W,
+                        uint32_t H, float eps, float eta, const float lo[3], const float scale[3], uint32_t g,
+                        uint32_t b, float* rays_out, uint32_t* keys) {
+    const HashP hp = mkhp(lo, scale, g, b);
+    Ray* rays = reinterpret_cast<Ray*>(rays_out);
+    const Ray* prev = reinterpret_cast<const Ray*>(prev_rays);
+    const uint64_t n = (uint64_t)W * H;
+#pragma omp parallel for schedule(static)
+    for (int64_t si = 0; si < (int64_t)n; ++si) {
+        const uint32_t slot = (uint32_t)si;
+        uint32_t key = KEY_NONE;
+        if (spos[4ull * slot + 3] != 0.0f) {
+            const V3 p = V3{spos[4ull * slot], spos[4ull * slot + 1], spos[4ull * slot + 2]};
+            const V3 nn = normalize(V3{snrm[4ull * slot], snrm[4ull * slot + 1], snrm[4ull * slot + 2]});
+            const V3 i = prev ? V3{prev[slot].d[0], prev[slot].d[1], prev[slot].d[2]}
+                              : normalize(sub(p, V3{eye[0], eye[1], eye[2]}));
+            const float d = dot(nn, i);
+            const float k = 1.0f - eta * eta * (1.0f - d * d);
+            if (k >= 0.0f) {
+                const V3 tr = normalize(sub(mul(i, eta), mul(nn, eta * d + std::sqrt(k))));
+                if (tr.x == tr.x && tr.y == tr.y && tr.z == tr.z) {
+                    const V3 o = add(p, mul(tr, eps));
+                    Ray r;
+                    r.o[0] = o.x;
+                    r.o[1] = o.y;
+                    r.o[2] = o.z;
+                    r.tmin = eps;
+                    r.d[0] = tr.x;
+                    r.d[1] = tr.y;
+                    r.d[2] = tr.z;
+                    r.tmax = std::numeric_limits<float>::infinity();
+                    rays[slot] = r;
+                    key = ray_hash(r.o, r.d, hp, 0u);
+                }
+            }
+        }
+        if (key == KEY_NONE) rays[slot] = Ray{{0.f, 0.f, 0.f}, 0.f, {0.f, 0.f, 0.f}, -1.f};
+        keys[slot] = key;
+    }
+}
+
 void orc_raygen_reflect(const float* spos, const float* snrm, const float* prev_rays, const float eye[3],
                         uint32_t W, uint32_t H, float eps, float jitter, uint32_t seed, uint32_t bounce,
                         const float lo[3], const float scale[3], uint32_t g, uint32_t b, float* rays_out,

@@ -763,6 +763,18 @@ rsh_status rsh_raygen_soft_shadow(const float* surface_pos, const float* surface
     return RSH_OK;
 }
 
+rsh_status rsh_raygen_refract(const float* surface_pos, const float* surface_nrm, const rsh_ray* prev_rays,
+                              const float eye[3], uint32_t width, uint32_t height, float epsilon, float eta,
+                              const rsh_hash_params* hp, rsh_ray* rays, uint32_t* keys, rsh_stream_t stream) {
+    if (!surface_pos || !surface_nrm || !hp || !rays || !keys || (!prev_rays && !eye)) return RSH_ERR_INVALID;
+    if (!(eta > 0.0f)) return RSH_ERR_INVALID;
+    const float zero[3] = {0, 0, 0};
+    RSH_CUDA(launch_raygen_refract(reinterpret_cast<const float4*>(surface_pos),
+                                   reinterpret_cast<const float4*>(surface_nrm), prev_rays, eye ? eye : zero, width,
+                                   height, epsilon, eta, to_hashp(*hp), rays, keys, stream));
+    return RSH_OK;
+}
+
 rsh_status rsh_raygen_reflect(const float* surface_pos, const float* surface_nrm, const rsh_ray* prev_rays,
                               const float eye[3], uint32_t width, uint32_t height, float epsilon,
                               float jitter, uint32_t seed, uint32_t bounce, const rsh_hash_params* hp,

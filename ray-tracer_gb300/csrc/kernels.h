@@ -55,6 +55,9 @@ cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const 
                                   const float eye[3], uint32_t w, uint32_t h, float eps,
                                   float jitter, uint32_t seed, uint32_t bounce, const HashP& hp,
                                   rsh_ray* rays, uint32_t* keys, cudaStream_t s);
+cudaError_t launch_raygen_refract(const float4* spos, const float4* snrm, const rsh_ray* prev, const float eye[3],
+                                  uint32_t w, uint32_t h, float eps, float eta, const HashP& hp, rsh_ray* rays,
+                                  uint32_t* keys, cudaStream_t s);
 cudaError_t launch_hash(const rsh_ray* rays, uint32_t n, const HashP& hp, uint32_t tag,
                         uint32_t* keys, cudaStream_t s);
 // Segmented hash for the batched form: segment s covers rays [seg_start[s], seg_start[s+1]) of the

@@ -197,6 +197,57 @@ cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const 
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ refraction rays
+// CreateRefractionRays (RayTracer.cu:793-842): direction refract(i, n, eta) (GLSL's formula: k = 1 -
+// eta^2 (1 - (n.i)^2), t = eta i - (eta n.i + sqrt k) n; no ray when k < 0, total internal reflection),
+// i = normalize(p - eye) or the incident ray, the surface normal as stored; renormalised, origin offset by
+// eps, interval (eps, inf). The reference creates these rays but never casts them.
+__global__ void k_raygen_refract(const float4* __restrict__ spos, const float4* __restrict__ snrm,
+                                 const rsh_ray* __restrict__ prev, v3 eye, uint32_t n, float eps, float eta,
+                                 HashP hp, rsh_ray* rays, uint32_t* keys) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n) return;
+    const float4 p4 = __ldg(spos + slot);
+    uint32_t key = RSH_KEY_NONE;
+    if (p4.w != 0.0f) {
+        const v3 p = mk3(p4);
+        const v3 nn = norm3(mk3(__ldg(snrm + slot)));
+        v3 i;
+        if (prev) {
+            float4 po, pd;
+            load_ray(prev, slot, po, pd);
+            i = mk3(pd);
+        } else {
+            i = norm3(p - eye);
+        }
+        const float d = dot3(nn, i);
+        const float k = 1.0f - eta * eta * (1.0f - d * d);
+        if (k >= 0.0f) {
+            const v3 t = norm3(i * eta - nn * (eta * d + sqrtf(k)));
+            if (t.x == t.x && t.y == t.y && t.z == t.z) {
+                const v3 o = p + t * eps;
+                store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps),
+                          make_float4(t.x, t.y, t.z, __int_as_float(0x7f800000)));
+                key = ray_hash(o.x, o.y, o.z, t.x, t.y, t.z, hp, 0u);
+            }
+        }
+    }
+    if (key == RSH_KEY_NONE)
+        store_ray(rays, slot, make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, -1.f));
+    keys[slot] = key;
+}
+
+cudaError_t launch_raygen_refract(const float4* spos, const float4* snrm, const rsh_ray* prev, const float eye[3],
+                                  uint32_t w, uint32_t h, float eps, float eta, const HashP& hp, rsh_ray* rays,
+                                  uint32_t* keys, cudaStream_t s) {
+    const uint32_t n = w * h;
+    if (n == 0) return cudaSuccess;
+    k_raygen_refract<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, prev, v3{eye[0], eye[1], eye[2]}, n, eps, eta,
+                                                     hp, rays, keys);
+    note_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ hash of given rays
 __global__ void k_hash(const rsh_ray* __restrict__ rays, uint32_t n, HashP hp, uint32_t tag,
                        uint32_t* keys) {

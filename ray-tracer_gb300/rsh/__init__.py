@@ -169,6 +169,7 @@ SIGNATURES = {
     "rsh_raygen_primary": (C.c_int, [_P, _U32, _U32, _P, _P, _P]),
     "rsh_raygen_shadow": (C.c_int, [_P, _P, _U32, _U32, _P, _U32, _F, _P, _P, _P, _P]),
     "rsh_raygen_soft_shadow": (C.c_int, [_P, _P, _U32, _U32, _P, _U32, _F, _P, _P, _P, _P]),
+    "rsh_raygen_refract": (C.c_int, [_P, _P, _P, _P, _U32, _U32, _F, _F, _P, _P, _P, _P]),
     "rsh_raygen_reflect": (C.c_int, [_P, _P, _P, _P, _U32, _U32, _F, _F, _U32, _U32, _P, _P, _P, _P]),
     "rsh_hash": (C.c_int, [_P, _U32, _P, _U32, _P, _P]),
     "rsh_compress": (C.c_int, [_P, _P, _U32, _P, _P, _P, _P, _P, _P]),

@@ -122,6 +122,46 @@ def test_raygen_soft_shadow_bitexact(cornell):
                                                    d_keys.ptr, None), "soft shadow tag bits")
 
 
+def test_raygen_refract_bitexact(ctx, cornell):
+    """Refraction rays (CreateRefractionRays, RayTracer.cu:793-842): from the eye at eta = 1/1.52, then from
+    those rays at eta = 1.52 where grazing rays meet total internal reflection (no ray); same rays and keys
+    as the oracle, and the refracted rays trace to the brute-force closest hits."""
+    s = cornell
+    W, H = 96, 80
+    cam, spos, snrm = _primary_surface(s, W, H)
+    lo, hi = _lohi(s)
+    hp = rsh.hash_params(lo, hi, 5, 4, 0)
+    d_spos, d_snrm = rsh.DeviceArray.from_numpy(spos), rsh.DeviceArray.from_numpy(snrm)
+    m = W * H
+    d_r = rsh.DeviceArray(m, rsh.RAY_DTYPE, zero=True)
+    d_k = rsh.DeviceArray(m, np.uint32)
+    eye = (C.c_float * 3)(*cam.eye)
+    rsh.check(rsh.lib().rsh_raygen_refract(d_spos.ptr, d_snrm.ptr, None, eye, W, H, 0.01, 1.0 / 1.52, C.byref(hp),
+                                           d_r.ptr, d_k.ptr, None), "refract")
+    o_r, o_k = oracle.raygen_refract(spos, snrm, None, cam.as_array()[:3], W, H, 0.01, 1.0 / 1.52, lo,
+                                     np.array(hp.scale[:]), 5, 4)
+    assert np.array_equal(d_k.numpy(), o_k)
+    v = o_k != rsh.KEY_NONE
+    assert v.sum() > 1000
+    assert d_r.numpy()[v].tobytes() == o_r[v].tobytes()
+    d_r2 = rsh.DeviceArray(m, rsh.RAY_DTYPE, zero=True)
+    rsh.check(rsh.lib().rsh_raygen_refract(d_spos.ptr, d_snrm.ptr, d_r.ptr, None, W, H, 0.01, 1.52, C.byref(hp),
+                                           d_r2.ptr, d_k.ptr, None), "refract2")
+    o_r2, o_k2 = oracle.raygen_refract(spos, snrm, o_r, None, W, H, 0.01, 1.52, lo, np.array(hp.scale[:]), 5, 4)
+    assert np.array_equal(d_k.numpy(), o_k2)
+    v2 = o_k2 != rsh.KEY_NONE
+    assert d_r2.numpy()[v2].tobytes() == o_r2[v2].tobytes()
+    assert (v & ~v2).sum() > 0  # total internal reflection: no refracted ray
+    sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+    rays = o_r[v]
+    assert np.array_equal(ctx.trace(sc, rays, False), oracle.brute(s.positions, rays, False))
+    assert np.array_equal(ctx.trace(sc, rays, False, fused=True), oracle.brute(s.positions, rays, False))
+    sc.destroy()
+    with pytest.raises(rsh.RshError):
+        rsh.check(rsh.lib().rsh_raygen_refract(d_spos.ptr, d_snrm.ptr, None, eye, W, H, 0.01, 0.0, C.byref(hp),
+                                               d_r.ptr, d_k.ptr, None), "refract eta 0")
+
+
 @pytest.mark.parametrize("jitter", [0.0, 1.0])
 def test_raygen_secondary_bitexact(cornell, jitter):
     s = cornell
