@@ -123,9 +123,9 @@ def test_raygen_soft_shadow_bitexact(cornell):
 
 
 def test_raygen_refract_bitexact(ctx, cornell):
-    """Refraction rays (CreateRefractionRays, RayTracer.cu:793-842): from the eye at eta = 1/1.52, then from
-    those rays at eta = 1.52 where grazing rays meet total internal reflection (no ray); same rays and keys
-    as the oracle, and the refracted rays trace to the brute-force closest hits."""
+    """Refraction rays (CreateRefractionRays, RayTracer.cu:793-842): from the eye at eta = 1/1.52, from
+    those rays again, and from the eye at eta = 1.52 where grazing view rays meet total internal reflection
+    (no ray); same rays and keys as the oracle, and the refracted rays trace to the brute-force hits."""
     s = cornell
     W, H = 96, 80
     cam, spos, snrm = _primary_surface(s, W, H)
@@ -151,7 +151,15 @@ def test_raygen_refract_bitexact(ctx, cornell):
     assert np.array_equal(d_k.numpy(), o_k2)
     v2 = o_k2 != rsh.KEY_NONE
     assert d_r2.numpy()[v2].tobytes() == o_r2[v2].tobytes()
-    assert (v & ~v2).sum() > 0  # total internal reflection: no refracted ray
+    d_r3 = rsh.DeviceArray(m, rsh.RAY_DTYPE, zero=True)
+    rsh.check(rsh.lib().rsh_raygen_refract(d_spos.ptr, d_snrm.ptr, None, eye, W, H, 0.01, 1.52, C.byref(hp),
+                                           d_r3.ptr, d_k.ptr, None), "refract3")
+    o_r3, o_k3 = oracle.raygen_refract(spos, snrm, None, cam.as_array()[:3], W, H, 0.01, 1.52, lo,
+                                       np.array(hp.scale[:]), 5, 4)
+    assert np.array_equal(d_k.numpy(), o_k3)
+    v3 = o_k3 != rsh.KEY_NONE
+    assert d_r3.numpy()[v3].tobytes() == o_r3[v3].tobytes()
+    assert (v & ~v3).sum() > 0 and v3.sum() > 0  # grazing view rays: total internal reflection, no ray
     sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
     rays = o_r[v]
     assert np.array_equal(ctx.trace(sc, rays, False), oracle.brute(s.positions, rays, False))
