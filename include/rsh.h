@@ -193,6 +193,13 @@ rsh_status rsh_set_config(rsh_ctx* ctx, const rsh_config* cfg);
 const char* rsh_last_error_string(void);
 /* Device error word (bounded waits that timed out, buffer overflows) raised since the last reset. */
 rsh_status rsh_check_device_errors(rsh_ctx* ctx, rsh_stream_t stream);
+
+/* Self-test of the device-side wait limit: runs one sort pass whose first tile never publishes its
+ * look-back status, so the second tile's wait can only end by giving up after spin_limit polls
+ * (1..4,194,304; a few thousand take a few milliseconds). Returns RSH_ERR_TIMEOUT when the wait gave up
+ * and reported it as designed (the context stays usable, the error word is cleared), anything else on a
+ * failure of the mechanism. No counterpart in the reference, whose kernels never wait on each other. */
+rsh_status rsh_selftest_wait_timeout(rsh_ctx* ctx, uint32_t spin_limit, rsh_stream_t stream);
 uint64_t rsh_bytes_allocated(const rsh_ctx* ctx);
 
 /* Small helpers so that callers without a CUDA runtime binding can move data. */

@@ -370,6 +370,16 @@ rsh_status rsh_set_config(rsh_ctx* ctx, const rsh_config* cfg) {
     return RSH_OK;
 }
 
+rsh_status rsh_selftest_wait_timeout(rsh_ctx* ctx, uint32_t spin_limit, rsh_stream_t stream) {
+    if (!ctx || spin_limit == 0 || spin_limit > (1u << 22)) return RSH_ERR_INVALID;  // at most the kernels' own limit
+    // start from a clean error word, so the bit read back below is this test's
+    RSH_TRY(rsh_check_device_errors(ctx, stream));
+    void* scr = nullptr;
+    RSH_TRY(ensure(ctx, "selftest", sort_selftest_scratch_bytes(), &scr));
+    RSH_CUDA(sort_selftest_timeout(scr, ctx->d_err, spin_limit, stream));
+    return rsh_check_device_errors(ctx, stream);  // RSH_ERR_TIMEOUT: the wait gave up as designed
+}
+
 rsh_status rsh_check_device_errors(rsh_ctx* ctx, rsh_stream_t stream) {
     if (!ctx) return RSH_ERR_INVALID;
     uint32_t v = 0;

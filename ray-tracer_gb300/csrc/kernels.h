@@ -76,6 +76,8 @@ cudaError_t launch_chunk_sizes(const uint32_t* chunk_bases, const uint32_t* coun
 
 // ---- onesweep radix sort (sort.cu)
 size_t sort_scratch_bytes(uint32_t n_max, uint32_t key_bits);
+size_t sort_selftest_scratch_bytes();
+cudaError_t sort_selftest_timeout(void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                               uint32_t* vals_out, uint32_t n_max, const uint32_t* d_count,
                               uint32_t key_bits, void* scratch, uint32_t* err, cudaStream_t s);

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(SR_THREADS, 3)
 k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n_max,
            const uint32_t* __restrict__ d_count, uint32_t shift, const uint32_t* __restrict__ hist,
-           uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* err) {
+           uint32_t* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* err, uint32_t spin_limit) {
     __shared__ uint32_t s_wc[SR_WARPS][256];    // per-warp digit counts -> exclusive warp offsets
     __shared__ uint32_t s_keys[SR_TILE];
     __shared__ uint32_t s_vals[SR_TILE];
@@ -201,7 +201,7 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
             if (done) break;
             j -= used;
             if (stall) {
-                if (++spins > RSH_SPIN_LIMIT) {
+                if (++spins > spin_limit) {
                     raise_device_error(err, RSH_DEVERR_TIMEOUT);
                     break;
                 }
@@ -282,7 +282,7 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
         (void)last;
         const uint32_t grid = std::min<uint32_t>((uint32_t)(tiles - 1 > 0 ? tiles - 1 : 1), resident);
         k_onesweep<<<grid, SR_THREADS, 0, s>>>(ki, vi, ko, vo, n_max, d_count, 8u * p, hist + 256u * p,
-                                               status + p * tiles * 256, tickets + p, err);
+                                               status + p * tiles * 256, tickets + p, err, RSH_SPIN_LIMIT);
         note_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -290,6 +290,35 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
         vi = vo;
     }
     return cudaSuccess;
+}
+
+// Self-test of the bounded look-back wait: one sort pass over two tiles whose first tile is never run
+// (its ticket is taken before the launch), so the second tile waits on a status word that nothing
+// publishes. The wait must give up after `spin_limit` polls and raise RSH_DEVERR_TIMEOUT in *err
+// instead of hanging; every write stays in bounds. Buffers (2 tiles of keys in/out, status, tickets)
+// come from the caller's scratch of sort_selftest_scratch_bytes().
+size_t sort_selftest_scratch_bytes() { return (size_t)(4 * 2 * SR_TILE + 2 * 256 + 256 + 8) * 4 + 1024; }
+
+cudaError_t sort_selftest_timeout(void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+    uint32_t* w = static_cast<uint32_t*>(scratch);
+    const uint32_t n = 2 * SR_TILE;
+    uint32_t* keys_in = w;
+    uint32_t* vals_in = keys_in + n;
+    uint32_t* keys_out = vals_in + n;
+    uint32_t* vals_out = keys_out + n;
+    uint32_t* status = vals_out + n;      // 2 tiles x 256 digits, all "not yet published"
+    uint32_t* hist = status + 2 * 256;    // 256
+    uint32_t* ticket = hist + 256;
+    cudaError_t e = cudaMemsetAsync(w, 0, sort_selftest_scratch_bytes() - 1024, s);
+    if (e != cudaSuccess) return e;
+    const uint32_t one = 1u;  // tile 0's ticket is already gone: the one CTA gets tile 1
+    if ((e = cudaMemcpyAsync(ticket, &one, 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(hist, &n, 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;  // all keys digit 0
+    k_onesweep<<<1, SR_THREADS, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, nullptr, 0u, hist, status, ticket, err,
+                                        spin_limit);
+    note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
 }
 
 }  // namespace rsh

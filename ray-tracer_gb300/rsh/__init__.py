@@ -125,6 +125,7 @@ SIGNATURES = {
     "rsh_set_config": (C.c_int, [_P, _P]),
     "rsh_last_error_string": (C.c_char_p, []),
     "rsh_check_device_errors": (C.c_int, [_P, _P]),
+    "rsh_selftest_wait_timeout": (C.c_int, [_P, _U32, _P]),
     "rsh_bytes_allocated": (_U64, [_P]),
     "rsh_malloc": (C.c_int, [_P, C.c_size_t]),
     "rsh_free": (C.c_int, [_P]),
