@@ -249,6 +249,19 @@ rsh_status rsh_obj_load(const char* obj_path, rsh_obj_data** out);
 void rsh_obj_free(rsh_obj_data* data);
 rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* scene);
 /* Scene bounds (exact min/max over all vertices). */
+/* Per-frame object transforms: every vertex of object k (rsh_scene_desc.object_ids; objects = 1 + the
+ * largest id) is multiplied by model_matrices[16k..16k+15] and every normal by normal_matrices[16k..]
+ * (NULL: the model matrix; normals renormalised), row-major, out[i] = sum_j M[4i + j] v[j] -- UpdateVertex
+ * (RayTracer.cu:448-511) as main.cpp:1131-1196 drives it. Transforms apply to the pose uploaded first
+ * (the rest pose), not to the previous frame's; the scene bounds and the object-sphere hierarchy are then
+ * rebuilt on the GPU (replacing UpdateBoundingSphere, :513-570). */
+rsh_status rsh_scene_set_transforms(rsh_ctx* ctx, rsh_scene* scene, const float* model_matrices,
+                                    const float* normal_matrices, uint32_t object_count, rsh_stream_t stream);
+
+/* Rebuilds the scene's bounds and object-sphere hierarchy from its current triangles with the context's
+ * cluster_size (rsh_scene_upload and rsh_scene_set_transforms call it). Replaces the per-object
+ * BoundingSphere::calculateMiniball (BoundingSphere.cpp:9-63) of the engine's init. */
+rsh_status rsh_build_object_hierarchy(rsh_ctx* ctx, rsh_scene* scene, rsh_stream_t stream);
 rsh_status rsh_scene_bounds(const rsh_scene* scene, float lo[3], float hi[3]);
 uint32_t rsh_scene_triangle_count(const rsh_scene* scene);
 /* Object hierarchy inspection: level 0 = leaves (triangle clusters). */

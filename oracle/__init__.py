@@ -66,6 +66,7 @@ def lib():
             "orc_hierarchy_offsets": (U32, [U32, U32, P]),
             "orc_build_rsh": (None, [P, P, U32, U32, U32, P]),
             "orc_objh_build": (P, [P, U32, U32, P, P]),
+            "orc_transform": (None, [P, P, P, U32, U32, P, P, P, P]),
             "orc_objh_free": (None, [P]),
             "orc_objh_levels": (U32, [P]),
             "orc_objh_level_size": (U32, [P, U32]),
@@ -216,6 +217,20 @@ def build_rsh(rays, ids, n, P, max_rays=None):
     lib().orc_build_rsh(_p(np.ascontiguousarray(rays, RAY_DTYPE)), _p(None if ids is None else _u32(ids)), n,
                         max_rays, P, _p(nodes))
     return nodes, off
+
+
+def transform(positions, normals, object_ids, model, normal=None):
+    """UpdateVertex restated: positions / normals [T,3,4] moved by per-object row-major 4x4 matrices."""
+    pr = _f32(positions).reshape(-1, 3, 4)
+    nr = _f32(normals).reshape(-1, 3, 4)
+    T = pr.shape[0]
+    ob = _u32(object_ids)
+    md = _f32(np.asarray(model, np.float32).reshape(-1, 16))
+    nm = None if normal is None else _f32(np.asarray(normal, np.float32).reshape(-1, 16))
+    pos = np.empty_like(pr)
+    nrm = np.empty_like(nr)
+    lib().orc_transform(_p(pr), _p(nr), _p(ob), T, md.shape[0], _p(md), _p(nm), _p(pos), _p(nrm))
+    return pos, nrm
 
 
 class ObjH:

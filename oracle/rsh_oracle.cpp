@@ -1030,6 +1030,39 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
     }
 }
 
+// UpdateVertex (RayTracer.cu:448-511): per vertex of triangle t, the object obj[t]'s row-major model
+// matrix on the position (w kept) and normal matrix (NULL: the model matrix) on the normal, summed in j
+// order from 0, the normal renormalised with w = 0.
+void orc_transform(const float* pos_rest, const float* nrm_rest, const uint32_t* obj, uint32_t T, uint32_t nobj,
+                   const float* model, const float* normal, float* pos, float* nrm) {
+    auto apply = [](const float* m, const float* v, float* o) {
+        for (int i = 0; i < 4; ++i) {
+            float s = 0.0f;
+            s += m[4 * i + 0] * v[0];
+            s += m[4 * i + 1] * v[1];
+            s += m[4 * i + 2] * v[2];
+            s += m[4 * i + 3] * v[3];
+            o[i] = s;
+        }
+    };
+    for (uint64_t x = 0; x < 3ull * T; ++x) {
+        uint32_t id = obj[x / 3];
+        if (id >= nobj) id = 0;
+        float q[4];
+        apply(model + 16ull * id, pos_rest + 4 * x, q);
+        pos[4 * x] = q[0];
+        pos[4 * x + 1] = q[1];
+        pos[4 * x + 2] = q[2];
+        pos[4 * x + 3] = pos_rest[4 * x + 3];
+        apply((normal ? normal : model) + 16ull * id, nrm_rest + 4 * x, q);
+        const V3 u = normalize(V3{q[0], q[1], q[2]});
+        nrm[4 * x] = u.x;
+        nrm[4 * x + 1] = u.y;
+        nrm[4 * x + 2] = u.z;
+        nrm[4 * x + 3] = 0.0f;
+    }
+}
+
 // Builds the object-sphere hierarchy; returns a handle used by the traversal / intersection calls.
 void* orc_objh_build(const float* pos, uint32_t T, uint32_t cluster, const float lo[3], const float hi[3]) {
     ObjH* h = new ObjH();

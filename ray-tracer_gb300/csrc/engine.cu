@@ -575,6 +575,7 @@ rsh_status rsh_scene_upload(rsh_ctx* ctx, const rsh_scene_desc* d, rsh_scene** o
     if ((e = cudaMalloc(&sc->pos, tri_bytes)) != cudaSuccess ||
         (e = cudaMalloc(&sc->nrm, tri_bytes)) != cudaSuccess ||
         (e = cudaMalloc(&sc->mat, 4ull * (T ? T : 1))) != cudaSuccess ||
+        (e = cudaMalloc(&sc->obj, 4ull * (T ? T : 1))) != cudaSuccess ||
         (e = cudaMalloc(&sc->materials, sizeof(rsh_material) * sc->material_count)) != cudaSuccess) {
         rsh_scene_destroy(ctx, sc);
         return cuda_status(e, "rsh_scene_upload");
@@ -584,6 +585,12 @@ rsh_status rsh_scene_upload(rsh_ctx* ctx, const rsh_scene_desc* d, rsh_scene** o
     cudaMemcpy(sc->nrm, nrm, 48ull * T, cudaMemcpyHostToDevice);
     if (d->material_ids) cudaMemcpy(sc->mat, d->material_ids, 4ull * T, cudaMemcpyHostToDevice);
     else cudaMemset(sc->mat, 0, 4ull * (T ? T : 1));
+    if (d->object_ids) {
+        cudaMemcpy(sc->obj, d->object_ids, 4ull * T, cudaMemcpyHostToDevice);
+        for (uint32_t t = 0; t < T; ++t) sc->object_count = std::max(sc->object_count, d->object_ids[t] + 1);
+    } else {
+        cudaMemset(sc->obj, 0, 4ull * (T ? T : 1));
+    }
     cudaMemcpy(sc->materials, mats, sizeof(rsh_material) * sc->material_count, cudaMemcpyHostToDevice);
     void* scr = nullptr;
     const size_t scr_bytes = objh_scratch_bytes(T ? T : 1);
@@ -612,6 +619,9 @@ rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* sc) {
     if (sc->pos) cudaFree(sc->pos);
     if (sc->nrm) cudaFree(sc->nrm);
     if (sc->mat) cudaFree(sc->mat);
+    if (sc->obj) cudaFree(sc->obj);
+    if (sc->pos_rest) cudaFree(sc->pos_rest);
+    if (sc->nrm_rest) cudaFree(sc->nrm_rest);
     if (sc->materials) cudaFree(sc->materials);
     if (sc->h.spheres) cudaFree(sc->h.spheres);
     if (sc->h.kids) cudaFree(sc->h.kids);
@@ -620,6 +630,71 @@ rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* sc) {
     if (ctx && ctx->allocated >= sc->bytes) ctx->allocated -= sc->bytes;
     delete sc;
     return RSH_OK;
+}
+
+rsh_status rsh_build_object_hierarchy(rsh_ctx* ctx, rsh_scene* sc, rsh_stream_t stream) {
+    if (!ctx || !sc || sc->owner != ctx) return RSH_ERR_INVALID;
+    const uint32_t T = sc->tri_count;
+    cudaStream_t s = stream;
+    // exact bounds of the current positions (the hash and the Morton codes are built over them)
+    if (T) {
+        void* bscr = nullptr;
+        RSH_TRY(ensure(ctx, "bounds", bounds_scratch_bytes(), &bscr));
+        float* b6 = static_cast<float*>(bscr) + 6 * 608;
+        RSH_CUDA(launch_bounds(sc->pos, T, bscr, b6, s));
+        float hb[6];
+        RSH_CUDA(cudaMemcpyAsync(hb, b6, sizeof hb, cudaMemcpyDeviceToHost, s));
+        RSH_CUDA(cudaStreamSynchronize(s));
+        for (int a = 0; a < 3; ++a) {
+            if (!std::isfinite(hb[a]) || !std::isfinite(hb[3 + a])) {
+                set_error("non-finite vertex coordinate after the transform");
+                return RSH_ERR_INVALID;
+            }
+            sc->lo[a] = hb[a];
+            sc->hi[a] = hb[3 + a];
+        }
+    }
+    RSH_CUDA(cudaStreamSynchronize(s));
+    for (void* p : {(void*)sc->h.spheres, (void*)sc->h.kids, (void*)sc->h.tris, (void*)sc->h.order})
+        if (p) cudaFree(p);
+    sc->h = ObjHierarchy();
+    void* scr = nullptr;
+    const size_t scr_bytes = objh_scratch_bytes(T ? T : 1);
+    RSH_CUDA(cudaMalloc(&scr, scr_bytes));
+    const cudaError_t e = build_object_hierarchy(sc->pos, T, ctx->cfg.cluster_size, sc->lo, sc->hi, sc->h, scr,
+                                                 scr_bytes, ctx->d_err, s);
+    cudaFree(scr);
+    if (e != cudaSuccess) return cuda_status(e, "rsh_build_object_hierarchy");
+    return RSH_OK;
+}
+
+rsh_status rsh_scene_set_transforms(rsh_ctx* ctx, rsh_scene* sc, const float* model_matrices,
+                                    const float* normal_matrices, uint32_t object_count, rsh_stream_t stream) {
+    if (!ctx || !sc || sc->owner != ctx || !model_matrices || object_count < sc->object_count) return RSH_ERR_INVALID;
+    for (uint64_t i = 0; i < 16ull * object_count; ++i)
+        if (!std::isfinite(model_matrices[i]) || (normal_matrices && !std::isfinite(normal_matrices[i]))) {
+            set_error("non-finite transform");
+            return RSH_ERR_INVALID;
+        }
+    const uint32_t T = sc->tri_count;
+    cudaStream_t s = stream;
+    const size_t tri_bytes = 48ull * (T ? T : 1);
+    if (!sc->pos_rest) {  // the uploaded pose becomes the rest pose
+        RSH_CUDA(cudaMalloc(&sc->pos_rest, tri_bytes));
+        RSH_CUDA(cudaMalloc(&sc->nrm_rest, tri_bytes));
+        RSH_CUDA(cudaMemcpyAsync(sc->pos_rest, sc->pos, tri_bytes, cudaMemcpyDeviceToDevice, s));
+        RSH_CUDA(cudaMemcpyAsync(sc->nrm_rest, sc->nrm, tri_bytes, cudaMemcpyDeviceToDevice, s));
+    }
+    void* mbuf = nullptr;
+    RSH_TRY(ensure(ctx, "transforms", 2ull * 64 * object_count, &mbuf));
+    float* dm = static_cast<float*>(mbuf);
+    float* dn = dm + 16ull * object_count;
+    RSH_CUDA(cudaMemcpyAsync(dm, model_matrices, 64ull * object_count, cudaMemcpyHostToDevice, s));
+    if (normal_matrices)
+        RSH_CUDA(cudaMemcpyAsync(dn, normal_matrices, 64ull * object_count, cudaMemcpyHostToDevice, s));
+    RSH_CUDA(launch_transform(sc->pos_rest, sc->nrm_rest, sc->obj, T, object_count, dm,
+                              normal_matrices ? dn : nullptr, sc->pos, sc->nrm, s));
+    return rsh_build_object_hierarchy(ctx, sc, stream);
 }
 
 rsh_status rsh_scene_bounds(const rsh_scene* sc, float lo[3], float hi[3]) {

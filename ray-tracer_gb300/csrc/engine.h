@@ -41,6 +41,10 @@ struct rsh_scene {
     float4* pos = nullptr;       // original order, 3 per triangle
     float4* nrm = nullptr;       // original order, 3 per triangle
     uint32_t* mat = nullptr;     // per triangle
+    uint32_t* obj = nullptr;     // object id per triangle (transforms)
+    uint32_t object_count = 1;
+    float4* pos_rest = nullptr;  // rest pose for rsh_scene_set_transforms (kept from the first call on)
+    float4* nrm_rest = nullptr;
     rsh_material* materials = nullptr;
     uint32_t material_count = 0;
     rsh::ObjHierarchy h;

@@ -228,6 +228,13 @@ struct ShadeArgs {
 cudaError_t launch_shade(const ShadeArgs& a, cudaStream_t s);
 cudaError_t launch_pack_rgba(const float4* accum, uint32_t n, uint32_t* rgba, cudaStream_t s);
 
+// ---- object transforms and bounds (transform.cu)
+cudaError_t launch_transform(const float4* pos_rest, const float4* nrm_rest, const uint32_t* obj, uint32_t tri_count,
+                             uint32_t n_objects, const float* model, const float* normal, float4* pos, float4* nrm,
+                             cudaStream_t s);
+size_t bounds_scratch_bytes();
+cudaError_t launch_bounds(const float4* pos, uint32_t tri_count, void* scratch, float* out6, cudaStream_t s);
+
 // ---- misc (util kernels in raygen.cu)
 cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t s);
 cudaError_t launch_fill_u64(unsigned long long* p, unsigned long long v, size_t n, cudaStream_t s);

@@ -146,6 +146,8 @@ SIGNATURES = {
     "rsh_sm_count": (C.c_int, []),
     "rsh_kernel_launches": (_U64, []),
     "rsh_scene_upload": (C.c_int, [_P, _P, _P]),
+    "rsh_scene_set_transforms": (C.c_int, [_P, _P, _P, _P, _U32, _P]),
+    "rsh_build_object_hierarchy": (C.c_int, [_P, _P, _P]),
     "rsh_obj_load": (C.c_int, [C.c_char_p, _P]),
     "rsh_obj_free": (None, [_P]),
     "rsh_scene_destroy": (C.c_int, [_P, _P]),
@@ -362,7 +364,8 @@ def load_obj(path) -> dict:
 class Scene:
     """A device-resident scene (positions/normals float32 [T,3,4]; material ids uint32 [T])."""
 
-    def __init__(self, ctx: "Context", positions: np.ndarray, normals=None, material_ids=None, materials=None):
+    def __init__(self, ctx: "Context", positions: np.ndarray, normals=None, material_ids=None, materials=None,
+                 object_ids=None):
         self.ctx = ctx
         pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3, 4)
         self.positions = pos
@@ -374,7 +377,8 @@ class Scene:
         d.positions = pos.ctypes.data
         d.normals = self.normals.ctypes.data if self.normals is not None else None
         d.material_ids = self.material_ids.ctypes.data if self.material_ids is not None else None
-        d.object_ids = None
+        self.object_ids = None if object_ids is None else np.ascontiguousarray(object_ids, dtype=np.uint32)
+        d.object_ids = self.object_ids.ctypes.data if self.object_ids is not None else None
         d.materials = self.materials.ctypes.data
         d.triangle_count = pos.shape[0]
         d.material_count = self.materials.shape[0]
@@ -396,6 +400,25 @@ class Scene:
             a = np.empty(n, OBJNODE_DTYPE)
             check(lib().rsh_scene_get_level(self.handle, l, a.ctypes.data), "rsh_scene_get_level")
             out.append(a)
+        return out
+
+    def set_transforms(self, model, normal=None, stream=None):
+        """Per-object row-major 4x4 model (and normal) matrices, [K,16] or [K,4,4]; see rsh_scene_set_transforms."""
+        m = np.ascontiguousarray(np.asarray(model, np.float32).reshape(-1, 16))
+        n = None if normal is None else np.ascontiguousarray(np.asarray(normal, np.float32).reshape(-1, 16))
+        check(lib().rsh_scene_set_transforms(self.ctx.handle, self.handle, m.ctypes.data,
+                                             None if n is None else n.ctypes.data, m.shape[0], stream),
+              "rsh_scene_set_transforms")
+
+    def triangles(self) -> np.ndarray:
+        """The scene's current triangles in original order (float32 [T,3,4], w as uploaded)."""
+        T = self.tri_count
+        tris = np.empty((T, 3, 4), np.float32)
+        check(lib().rsh_memcpy_d2h(tris.ctypes.data, lib().rsh_scene_device_triangles(self.handle), 48 * T, None),
+              "d2h")
+        out = np.empty_like(tris)
+        out[self.order()] = tris
+        out[:, 0, 3] = self.positions[:, 0, 3]  # cluster order keeps the original id in v0.w
         return out
 
     def order(self) -> np.ndarray:
@@ -422,8 +445,8 @@ class Context:
             setattr(self.config, k, v)
         check(lib().rsh_set_config(self.handle, C.byref(self.config)), "rsh_set_config")
 
-    def scene(self, positions, normals=None, material_ids=None, materials=None) -> Scene:
-        return Scene(self, positions, normals, material_ids, materials)
+    def scene(self, positions, normals=None, material_ids=None, materials=None, object_ids=None) -> Scene:
+        return Scene(self, positions, normals, material_ids, materials, object_ids)
 
     def set_lights(self, lights):
         arr = make_lights(lights)
