@@ -511,6 +511,82 @@ def serving_bench(args):
 
 
 
+def batching_bench(args):
+    """The batching workload: 256 independent ray batches (sizes log-uniform in [4k, 2M]) over 16 resident
+    random soups (10k-1M triangles, log-uniform); rays leave triangle surfaces with uniform-sphere or mirror
+    directions (50/50); half the batches closest hit, half any hit. The autotuner picks grid bits, direction
+    bins and packet size on this batch; then one CUDA-graph launch traces the whole batch per step.
+    Mrays/s = rays per step / device time per step (CUDA events on the graph's stream)."""
+    import ctypes as C
+
+    import rsh
+    from rsh import scenes
+
+    lib = rsh.load()
+    sd, sizes, which, any_hit = scenes.batch_config(n_batches=args.batch_count, max_rays=args.batch_max_rays)
+    ctx = rsh.Context(rsh.default_config())
+    scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]
+    rng = np.random.default_rng([scenes.SEED_BASE + 3, 7])
+    segs = (rsh.BatchSegment * len(sizes))()
+    keep = []
+    total = 0
+    for i, (n, w, a) in enumerate(zip(sizes, which, any_hit)):
+        n = int(n)
+        r = scenes.surface_rays(sd[w], n, rng)
+        dr = rsh.DeviceArray.from_numpy(r)
+        out = rsh.DeviceArray(n, np.uint32 if a else np.uint64)
+        keep.append((dr, out))
+        segs[i].scene = scs[w].handle
+        segs[i].rays = dr.ptr
+        segs[i].n = n
+        segs[i].any_hit = int(a)
+        segs[i].hits = None if a else out.ptr
+        segs[i].flags = out.ptr if a else None
+        total += n
+    st = C.c_void_p()
+    rsh.check(lib.rsh_stream_create(C.byref(st)), "stream")
+    gb, db, ps = (C.c_uint32 * 2)(4, 5), (C.c_uint32 * 2)(5, 6), (C.c_uint32 * 2)(8, 16)
+    best = rsh.Config()
+    t0 = time.perf_counter()
+    rsh.check(lib.rsh_autotune(ctx.handle, segs, len(sizes), gb, 2, db, 2, ps, 2, st, C.byref(best)), "autotune")
+    tune_s = time.perf_counter() - t0
+    g = C.c_void_p()
+    rsh.check(lib.rsh_batch_graph_create(ctx.handle, segs, len(sizes), st, C.byref(g)), "graph")
+    for _ in range(args.warmup):
+        rsh.check(lib.rsh_batch_graph_launch(g, st), "launch")
+    rsh.check(lib.rsh_stream_synchronize(st), "sync")
+    e0, e1 = C.c_void_p(), C.c_void_p()
+    lib.rsh_event_create(C.byref(e0))
+    lib.rsh_event_create(C.byref(e1))
+    l0 = lib.rsh_kernel_launches()
+    clocks = ClockSampler()
+    clocks.start()
+    lib.rsh_event_record(e0, st)
+    for _ in range(args.steps):
+        rsh.check(lib.rsh_batch_graph_launch(g, st), "launch")
+    lib.rsh_event_record(e1, st)
+    rsh.check(lib.rsh_stream_synchronize(st), "sync")
+    clk = clocks.stop()
+    ms = C.c_float()
+    lib.rsh_event_elapsed(e0, e1, C.byref(ms))
+    ctx.check_device_errors(st)
+    lib.rsh_batch_graph_destroy(g)
+    lib.rsh_stream_destroy(st)
+    for s in scs:
+        s.destroy()
+    step_ms = ms.value / args.steps
+    out = {"metric": "batched secondary-ray Mrays/s (graph launch per step)", "value": round(total / step_ms / 1e3, 3),
+           "unit": "Mrays/s", "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3),
+           "rays_per_step": int(total), "batches": int(len(sizes)), "scenes": len(sd),
+           "scenes_tris": [int(s.tri_count) for s in sd],
+           "autotuned": {"grid_bits": best.grid_bits, "dir_log2": best.dir_log2, "packet_size": best.packet_size,
+                         "tuning_s": round(tune_s, 2)},
+           "kernels_per_step_launched_by_graph": "compress, sort, decompress, build, fused (one persistent launch)",
+           "clocks": clk, "data": "synthetic (seeded random soups, surface rays)"}
+    ctx.destroy()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -525,6 +601,9 @@ def main():
     ap.add_argument("--mode", default="all", choices=["all", "plain", "fused"],
                     help="all: plain + fused + e2e + stage timers; plain/fused: only that timed pass")
     ap.add_argument("--serving", action="store_true", help="run the serving benchmark instead")
+    ap.add_argument("--batching", action="store_true", help="run the batching benchmark (256 batches, 16 scenes)")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-max-rays", type=int, default=2_000_000)
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-scenes", type=int, default=8)
@@ -533,6 +612,9 @@ def main():
     args = ap.parse_args()
     if args.serving:
         print(json.dumps(serving_bench(args)))
+        return 0
+    if args.batching:
+        print(json.dumps(batching_bench(args)))
         return 0
     rank, world, td = dist_setup(args.gpus)
     s = make_workload(args.config)

@@ -42,6 +42,7 @@ struct PrepSeg {  // per-segment table of k_batch_prep
 }  // namespace
 
 __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, uint32_t total, uint32_t tag_shift,
+                             uint32_t hash_drop,
                              rsh_ray* __restrict__ rays_all, uint32_t* __restrict__ keys,
                              uint32_t* __restrict__ seg_cnt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -60,7 +61,7 @@ __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, ui
         store_ray(rays_all, i, o, d);
         uint32_t key = RSH_KEY_NONE;
         valid = d.w > o.w;
-        if (valid) key = (lo << tag_shift) | ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, sg.hp, 0u);
+        if (valid) key = (lo << tag_shift) | (ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, sg.hp, 0u) >> hash_drop);
         keys[i] = key;
         if (sg.any_hit) sg.flags[j] = 0u;
         else sg.hits[j] = RSH_HIT_NONE;
@@ -112,7 +113,7 @@ using namespace rsh;
 namespace {
 
 struct BatchPlan {
-    uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0;
+    uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0, hash_drop = 0;
     void *rays_all, *keys, *trimmed, *ckeys, *cbases, *counts, *skeys, *svals, *sorted_keys, *sorted_ids, *scr;
     void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work, *sched, *seg_delta;
     std::vector<PrepSeg> h_prep;
@@ -137,12 +138,16 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     pl.total = (uint32_t)total;
     uint32_t tag_bits = 0;
     while ((1u << tag_bits) < count) ++tag_bits;
-    pl.tag_shift = 3 * ctx->cfg.grid_bits + 2 * ctx->cfg.dir_log2;
-    pl.key_bits = pl.tag_shift + tag_bits;
-    if (pl.key_bits > 31) {
-        set_error("segment tag + hash exceed 31 key bits: lower grid_bits / dir_log2");
+    // segment tag above the hash; when both do not fit in 31 bits, the hash's lowest bits are dropped (the
+    // hash only orders rays for coherence, no result depends on it)
+    const uint32_t hash_bits = 3 * ctx->cfg.grid_bits + 2 * ctx->cfg.dir_log2;
+    pl.hash_drop = (hash_bits + tag_bits > 31) ? hash_bits + tag_bits - 31 : 0u;
+    if (pl.hash_drop > hash_bits) {
+        set_error("too many batch segments for a 31-bit key");
         return RSH_ERR_INVALID;
     }
+    pl.tag_shift = hash_bits - pl.hash_drop;
+    pl.key_bits = pl.tag_shift + tag_bits;
     pl.P = ctx->cfg.packet_size;
     pl.unit_rays = 8 * pl.P;
     pl.max_padded = pl.total + count * pl.unit_rays;
@@ -290,7 +295,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     uint32_t* totals = static_cast<uint32_t*>(pl.totals);
     RSH_CUDA(cudaMemsetAsync(pl.seg_cnt, 0, 4ull * pl.nseg, s));
     k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
-                                                       pl.tag_shift, static_cast<rsh_ray*>(pl.rays_all),
+                                                       pl.tag_shift, pl.hash_drop, static_cast<rsh_ray*>(pl.rays_all),
                                                        static_cast<uint32_t*>(pl.keys), static_cast<uint32_t*>(pl.seg_cnt));
     note_launch();
     RSH_CUDA(cudaGetLastError());

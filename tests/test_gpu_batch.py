@@ -117,3 +117,39 @@ def test_autotune_picks_a_valid_config(ctx):
     assert np.array_equal(out.numpy(), oracle.brute(s.positions, rays, False))
     ctx.set_config(grid_bits=5, dir_log2=4, packet_size=8)
     sc.destroy()
+
+
+def test_many_segments_drop_low_hash_bits():
+    """300 segments need 9 tag bits: with a 27-bit hash (grid 5, dir 6) the key would need 36 bits, so the
+    batch drops the hash's 5 lowest bits (ordering only); every segment's results still equal brute force."""
+    ctx = rsh.Context(grid_bits=5, dir_log2=6, packet_size=8, cluster_size=6)
+    rng = np.random.default_rng(31)
+    sd = [scenes.random_soup(int(t), np.random.default_rng(300 + i)) for i, t in enumerate([4_000, 9_000, 15_000])]
+    scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]
+    nseg = 300
+    sizes = rng.integers(0, 700, nseg)
+    which = rng.integers(0, 3, nseg)
+    anyh = rng.random(nseg) < 0.5
+    segs = (rsh.BatchSegment * nseg)()
+    keep = []
+    for i in range(nseg):
+        n = int(sizes[i])
+        r = scenes.surface_rays(sd[which[i]], max(n, 1), rng)[:n]
+        dr = rsh.DeviceArray.from_numpy(r) if n else rsh.DeviceArray(1, rsh.RAY_DTYPE)
+        out = rsh.DeviceArray(max(n, 1), np.uint32 if anyh[i] else np.uint64)
+        keep.append((r, dr, out))
+        segs[i].scene = scs[which[i]].handle
+        segs[i].rays = dr.ptr
+        segs[i].n = n
+        segs[i].any_hit = int(anyh[i])
+        segs[i].hits = None if anyh[i] else out.ptr
+        segs[i].flags = out.ptr if anyh[i] else None
+    rsh.check(rsh.lib().rsh_batch_trace(ctx.handle, segs, nseg, None), "batch")
+    ctx.check_device_errors()
+    for i in range(nseg):
+        r, _, out = keep[i]
+        if len(r):
+            assert np.array_equal(out.numpy(len(r)), oracle.brute(sd[which[i]].positions, r, bool(anyh[i]))), i
+    for sc in scs:
+        sc.destroy()
+    ctx.destroy()
