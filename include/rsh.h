@@ -464,7 +464,9 @@ rsh_status rsh_batch_graph_create(rsh_ctx* ctx, const rsh_batch_segment* segment
                                   rsh_stream_t stream, void** graph_exec);
 rsh_status rsh_batch_graph_launch(void* graph_exec, rsh_stream_t stream);
 rsh_status rsh_batch_graph_destroy(void* graph_exec);
-/* Statistics of the last rsh_batch_trace (synchronises). */
+/* Statistics of the last rsh_batch_trace (synchronises): reflection_rays = rays traced, chunks, node and
+ * triangle tests, and with RSH_FLAG_STAGE_TIMERS stage_ms (RAYGEN = gather + hash, COMPRESS, SORT,
+ * DECOMPRESS, BUILD, TRAVERSE = the fused traversal + intersection launch). */
 rsh_status rsh_batch_stats_get(rsh_ctx* ctx, rsh_frame_stats* out);
 
 /* Autotuner: times rsh_batch_trace on `segments` for each (grid_bits, dir_log2, packet_size) in the
@@ -473,6 +475,37 @@ rsh_status rsh_autotune(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_
                         const uint32_t* grid_bits, uint32_t n_grid, const uint32_t* dir_log2,
                         uint32_t n_dir, const uint32_t* packet_sizes, uint32_t n_packet,
                         rsh_stream_t stream, rsh_config* best);
+
+/* Per-scene tuning of the batched form (rsh_batch_trace, its graphs and the server): origin-grid bits,
+ * direction bins (dir_log2) and the object-tree level at which rays leave their packets. A field equal
+ * to RSH_TUNE_DEFAULT takes the context's value. The plain per-frame path ignores it. No counterpart in
+ * the reference (its hash has no parameters, RayTracer.cu:147-198). */
+#define RSH_TUNE_DEFAULT 0xFFFFFFFFu
+typedef struct rsh_scene_tuning {
+    uint32_t grid_bits;   /* 1..10 */
+    uint32_t dir_log2;    /* 1..6 */
+    uint32_t ray_level;   /* 0..15 */
+} rsh_scene_tuning;
+rsh_status rsh_scene_set_tuning(rsh_scene* scene, const rsh_scene_tuning* tuning);
+rsh_status rsh_scene_get_tuning(const rsh_scene* scene, rsh_scene_tuning* out);
+
+/* Search space of rsh_autotune_scenes. Any list may be empty (that parameter stays as it is). */
+typedef struct rsh_tune_space {
+    const uint32_t* grid_bits;    uint32_t n_grid;
+    const uint32_t* dir_log2;     uint32_t n_dir;
+    const uint32_t* ray_levels;   uint32_t n_ray_level;
+    const uint32_t* packet_sizes; uint32_t n_packet;
+    uint32_t reps;                /* timed repetitions per point after one warm-up (0: 2) */
+} rsh_tune_space;
+/* Per-scene autotuner: coordinate descent over the space. The packet size (shared by every segment of a
+ * batch) is chosen on the whole batch; then, for each distinct scene, grid bits, direction bins and the
+ * switch level are chosen on that scene's segments alone, one parameter at a time, and stored in the
+ * scene (rsh_scene_set_tuning); last, the packet size is chosen again with the scenes tuned. Points whose
+ * hash is wider than 31 bits are skipped. *best_ms (optional) is the whole batch's time with the final
+ * choice, *untuned_ms (optional) its time with the context's configuration and no scene tuning. */
+rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count,
+                               const rsh_tune_space* space, rsh_stream_t stream, float* best_ms,
+                               float* untuned_ms);
 
 /* Ray-by-ray trace through the fused persistent kernel (one segment); same outputs as
  * rsh_trace_rays. */

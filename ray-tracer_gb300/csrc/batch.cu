@@ -121,6 +121,16 @@ struct BatchPlan {
     std::vector<uint32_t> h_sched;  // schedule position -> segment index
 };
 
+// The context's configuration with a scene's own tuning (rsh_scene_set_tuning) applied.
+rsh_config tuned_config(const rsh_config& base, const rsh_scene* sc) {
+    rsh_config c = base;
+    if (!sc) return c;
+    if (sc->tune.grid_bits != RSH_TUNE_DEFAULT) c.grid_bits = sc->tune.grid_bits;
+    if (sc->tune.dir_log2 != RSH_TUNE_DEFAULT) c.dir_log2 = sc->tune.dir_log2;
+    if (sc->tune.ray_level != RSH_TUNE_DEFAULT) c.ray_level = sc->tune.ray_level;
+    return c;
+}
+
 rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count, BatchPlan& pl) {
     if (!ctx || (!segs && count)) return RSH_ERR_INVALID;
     if (count > 1024) {
@@ -139,8 +149,13 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     uint32_t tag_bits = 0;
     while ((1u << tag_bits) < count) ++tag_bits;
     // segment tag above the hash; when both do not fit in 31 bits, the hash's lowest bits are dropped (the
-    // hash only orders rays for coherence, no result depends on it)
-    const uint32_t hash_bits = 3 * ctx->cfg.grid_bits + 2 * ctx->cfg.dir_log2;
+    // hash only orders rays for coherence, no result depends on it). Scenes may tune their own hash width:
+    // the tag sits above the widest.
+    uint32_t hash_bits = 0;
+    for (uint32_t s = 0; s < count; ++s) {
+        const rsh_config c = tuned_config(ctx->cfg, segs[s].scene);
+        hash_bits = std::max(hash_bits, 3 * c.grid_bits + 2 * c.dir_log2);
+    }
     pl.hash_drop = (hash_bits + tag_bits > 31) ? hash_bits + tag_bits - 31 : 0u;
     if (pl.hash_drop > hash_bits) {
         set_error("too many batch segments for a 31-bit key");
@@ -190,7 +205,8 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         p.any_hit = g.any_hit ? 1u : 0u;
         p.flags = g.flags;
         p.hits = reinterpret_cast<unsigned long long*>(g.hits);
-        RSH_TRY(make_hash_params(sc, ctx->cfg, 0, p.hp));
+        const rsh_config tc = tuned_config(ctx->cfg, sc);
+        RSH_TRY(make_hash_params(sc, tc, 0, p.hp));
         // per-ray job words and packet stack entries hold an object-node index of level >= 1 in 20 bits;
         // cluster triangles are staged in shared memory (at most 32)
         if ((sc->h.levels > 1 && sc->h.level_size[1] > (1u << 20)) || sc->h.cluster > 32) {
@@ -210,6 +226,7 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
             f.lvl_size[l] = sc->h.level_size[l];
         }
         f.any_hit = p.any_hit;
+        f.ray_level = tc.ray_level;
         f.flags = g.flags;
         f.hits = reinterpret_cast<unsigned long long*>(g.hits);
         f.slot_base = start;
@@ -293,6 +310,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     if (pl.total == 0) return RSH_OK;
     uint32_t* cnt = static_cast<uint32_t*>(pl.counts);
     uint32_t* totals = static_cast<uint32_t*>(pl.totals);
+    int th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);  // gather + hash + per-segment counts
     RSH_CUDA(cudaMemsetAsync(pl.seg_cnt, 0, 4ull * pl.nseg, s));
     k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
                                                        pl.tag_shift, pl.hash_drop, static_cast<rsh_ray*>(pl.rays_all),
@@ -306,7 +324,8 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
                                       pl.max_padded);
     note_launch();
     RSH_CUDA(cudaGetLastError());
-    int th = stage_begin(ctx, RSH_STAGE_COMPRESS, s);
+    stage_end(ctx, th, s);
+    th = stage_begin(ctx, RSH_STAGE_COMPRESS, s);
     RSH_CUDA(launch_compress(static_cast<uint32_t*>(pl.keys), pl.total, static_cast<uint32_t*>(pl.trimmed),
                              static_cast<uint32_t*>(pl.ckeys), static_cast<uint32_t*>(pl.cbases), cnt, pl.scr,
                              ctx->d_err, s));
@@ -341,7 +360,6 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     fa.units_max = pl.max_padded / pl.unit_rays;
     fa.d_units = totals + 1;
     fa.work = static_cast<uint32_t*>(pl.work);
-    fa.ray_level = ctx->cfg.ray_level;
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;
@@ -361,6 +379,16 @@ struct GraphExec {
 }  // namespace
 
 namespace rsh {
+// rsh_batch_trace without resetting the stage timers (a fused frame keeps its own).
+rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream) {
+    BatchPlan pl;
+    RSH_TRY(batch_prepare(ctx, segments, count, pl));
+    ctx->last_stream = stream;
+    RSH_TRY(batch_enqueue(ctx, pl, stream));
+    ctx->batch_counts_host.assign(1, pl.total);
+    return RSH_OK;
+}
+
 // Frees the context's staging ring (called by rsh_destroy).
 void batch_release_ctx(const rsh_ctx* ctx) {
     std::lock_guard<std::mutex> lk(g_stage_mu);
@@ -377,12 +405,10 @@ void batch_release_ctx(const rsh_ctx* ctx) {
 extern "C" {
 
 rsh_status rsh_batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, rsh_stream_t stream) {
-    BatchPlan pl;
-    RSH_TRY(batch_prepare(ctx, segments, count, pl));
-    ctx->last_stream = stream;
-    RSH_TRY(batch_enqueue(ctx, pl, stream));
-    ctx->batch_counts_host.assign(1, pl.total);
-    return RSH_OK;
+    if (!ctx) return RSH_ERR_INVALID;
+    ctx->tev_used = 0;  // stage timers (RSH_FLAG_STAGE_TIMERS) cover this call only
+    ctx->tmarks.clear();
+    return batch_trace(ctx, segments, count, stream);
 }
 
 rsh_status rsh_batch_graph_create(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count,
@@ -464,6 +490,12 @@ rsh_status rsh_batch_stats_get(rsh_ctx* ctx, rsh_frame_stats* out) {
     st.chunks = cnt[1];
     st.node_tests = d[0];
     st.tri_tests = d[1];
+    for (const auto& m : ctx->tmarks) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ctx->tev[m.second], ctx->tev[m.second + 1]) == cudaSuccess && m.first < 12)
+            st.stage_ms[m.first] += ms;
+    }
+    cudaGetLastError();
     *out = st;
     return RSH_OK;
 }
@@ -523,4 +555,126 @@ rsh_status rsh_autotune(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_
     return best_ms < 1e30f ? RSH_OK : RSH_ERR_INVALID;
 }
 
+rsh_status rsh_scene_set_tuning(rsh_scene* sc, const rsh_scene_tuning* t) {
+    if (!sc || !t) return RSH_ERR_INVALID;
+    const uint32_t D = RSH_TUNE_DEFAULT;
+    if ((t->grid_bits != D && (t->grid_bits < 1 || t->grid_bits > 10)) ||
+        (t->dir_log2 != D && (t->dir_log2 < 1 || t->dir_log2 > 6)) || (t->ray_level != D && t->ray_level > 15)) {
+        set_error("scene tuning out of range");
+        return RSH_ERR_INVALID;
+    }
+    sc->tune = *t;
+    return RSH_OK;
+}
+
+rsh_status rsh_scene_get_tuning(const rsh_scene* sc, rsh_scene_tuning* out) {
+    if (!sc || !out) return RSH_ERR_INVALID;
+    *out = sc->tune;
+    return RSH_OK;
+}
+
 }  // extern "C"
+
+namespace {
+// Mean time of one batch after a warm-up (CUDA events on the stream).
+rsh_status time_batch(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count, uint32_t reps,
+                      cudaStream_t stream, float* ms_out) {
+    BatchPlan pl;
+    RSH_TRY(batch_prepare(ctx, segs, count, pl));
+    RSH_TRY(batch_enqueue(ctx, pl, stream));
+    cudaEvent_t e0, e1;
+    RSH_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return RSH_ERR_CUDA;
+    }
+    rsh_status st = RSH_OK;
+    cudaEventRecord(e0, stream);
+    for (uint32_t r = 0; r < reps && st == RSH_OK; ++r) st = batch_enqueue(ctx, pl, stream);
+    cudaEventRecord(e1, stream);
+    const cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != RSH_OK) return st;
+    if (e != cudaSuccess) return RSH_ERR_CUDA;
+    *ms_out = ms / (float)reps;
+    return RSH_OK;
+}
+
+// Packet size on the whole batch: keeps the context's value unless another one is faster than cur_ms.
+float tune_packet(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count, const rsh_tune_space& sp,
+                  uint32_t reps, cudaStream_t stream, float cur_ms) {
+    const rsh_config base = ctx->cfg;
+    rsh_config best = base;
+    for (uint32_t i = 0; i < sp.n_packet; ++i) {
+        rsh_config c = base;
+        c.packet_size = sp.packet_sizes[i];
+        if (c.packet_size == base.packet_size || rsh_set_config(ctx, &c) != RSH_OK) continue;
+        float ms;
+        if (time_batch(ctx, segs, count, reps, stream, &ms) == RSH_OK && ms < cur_ms) {
+            cur_ms = ms;
+            best = c;
+        }
+    }
+    rsh_set_config(ctx, &best);
+    return cur_ms;
+}
+}  // namespace
+
+extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count,
+                                          const rsh_tune_space* space, rsh_stream_t stream, float* best_ms,
+                                          float* untuned_ms) {
+    if (!ctx || !space || !segs || !count) return RSH_ERR_INVALID;
+    if ((space->n_grid && !space->grid_bits) || (space->n_dir && !space->dir_log2) ||
+        (space->n_ray_level && !space->ray_levels) || (space->n_packet && !space->packet_sizes))
+        return RSH_ERR_INVALID;
+    const uint32_t reps = space->reps ? space->reps : 2u;
+    std::vector<rsh_scene*> scenes;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (!segs[i].scene) return RSH_ERR_INVALID;
+        rsh_scene* sc = const_cast<rsh_scene*>(segs[i].scene);
+        if (std::find(scenes.begin(), scenes.end(), sc) == scenes.end()) scenes.push_back(sc);
+    }
+    const rsh_scene_tuning none{RSH_TUNE_DEFAULT, RSH_TUNE_DEFAULT, RSH_TUNE_DEFAULT};
+    for (rsh_scene* sc : scenes) sc->tune = none;
+    float ms;
+    RSH_TRY(time_batch(ctx, segs, count, reps, stream, &ms));
+    if (untuned_ms) *untuned_ms = ms;
+    ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
+    // each scene on its own segments, one parameter at a time
+    for (rsh_scene* sc : scenes) {
+        std::vector<rsh_batch_segment> sub;
+        for (uint32_t i = 0; i < count; ++i)
+            if (segs[i].scene == sc) sub.push_back(segs[i]);
+        rsh_scene_tuning t{ctx->cfg.grid_bits, ctx->cfg.dir_log2, ctx->cfg.ray_level};
+        sc->tune = t;
+        float cur;
+        if (time_batch(ctx, sub.data(), (uint32_t)sub.size(), reps, stream, &cur) != RSH_OK) {
+            sc->tune = none;
+            continue;
+        }
+        for (int param = 0; param < 3; ++param) {
+            const uint32_t* vals = param == 0 ? space->grid_bits : param == 1 ? space->dir_log2 : space->ray_levels;
+            const uint32_t nv = param == 0 ? space->n_grid : param == 1 ? space->n_dir : space->n_ray_level;
+            for (uint32_t k = 0; k < nv; ++k) {
+                rsh_scene_tuning trial = t;
+                uint32_t& field = param == 0 ? trial.grid_bits : param == 1 ? trial.dir_log2 : trial.ray_level;
+                if (field == vals[k]) continue;
+                field = vals[k];
+                if (rsh_scene_set_tuning(sc, &trial) != RSH_OK) continue;
+                float m2;
+                if (time_batch(ctx, sub.data(), (uint32_t)sub.size(), reps, stream, &m2) == RSH_OK && m2 < cur) {
+                    cur = m2;
+                    t = trial;
+                }
+            }
+            sc->tune = t;
+        }
+    }
+    RSH_TRY(time_batch(ctx, segs, count, reps, stream, &ms));
+    ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
+    if (best_ms) *best_ms = ms;
+    return RSH_OK;
+}

@@ -1157,7 +1157,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
             rsh_batch_segment segs[2] = {
                 {sc, srays, npix * LS, 1, nullptr, sflags},
                 {sc, rrays, npix, 0, reinterpret_cast<uint64_t*>(rhits), nullptr}};
-            RSH_TRY(rsh_batch_trace(ctx, segs, 2, s));
+            RSH_TRY(batch_trace(ctx, segs, 2, s));
             const uint32_t* seg_cnt = static_cast<const uint32_t*>(ctx->bufs["b_seg_cnt"].ptr);
             const uint32_t* bcnt = static_cast<const uint32_t*>(ctx->bufs["b_counts"].ptr);
             RSH_CUDA(cudaMemcpyAsync(fc + 4 * b, seg_cnt, 4, cudaMemcpyDeviceToDevice, s));

@@ -49,6 +49,7 @@ struct rsh_scene {
     uint32_t material_count = 0;
     rsh::ObjHierarchy h;
     size_t bytes = 0;
+    rsh_scene_tuning tune{RSH_TUNE_DEFAULT, RSH_TUNE_DEFAULT, RSH_TUNE_DEFAULT};  // batched form only
 };
 
 struct BounceBufs {
@@ -95,6 +96,8 @@ rsh_status ensure_buf(rsh_ctx* ctx, DevBuf& b, size_t bytes);
 void release_buf(rsh_ctx* ctx, DevBuf& b);
 rsh_status make_hash_params(const rsh_scene* sc, const rsh_config& cfg, uint32_t tag_bits, HashP& out);
 void batch_release_ctx(const rsh_ctx* ctx);
+// rsh_batch_trace without resetting the stage timers (used inside a fused frame).
+rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream);
 
 // One secondary batch through compress -> sort -> decompress -> build -> traverse -> intersect.
 // keys: per slot (RSH_KEY_NONE = no ray); rays indexed by slot. Output flags/hits indexed by slot

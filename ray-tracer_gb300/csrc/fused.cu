@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
                 if (m == 0) continue;
                 // rays of these packets leave the packet and descend this subtree one by one: below the
                 // switch level, and at once for packets whose cone is wider than a half-space
-                const uint32_t m_ray = (L <= a.ray_level) ? m : (m & fullmask);
+                const uint32_t m_ray = (L <= sg.ray_level) ? m : (m & fullmask);
                 if (m_ray) {
                     // queue one job per live ray of these packets; run the queue once it is long enough
                     // to keep every lane busy (or would overflow)

@@ -182,6 +182,7 @@ struct FusedSeg {
     uint32_t ray_begin, ray_end;   // sorted ray range of this segment
     uint32_t unit_begin;           // first work unit (level-1 node) of this segment
     uint32_t any_hit;
+    uint32_t ray_level;            // object-tree level at and below which rays descend individually
     uint32_t* flags;               // indexed by slot - slot_base
     unsigned long long* hits;
     uint32_t slot_base;
@@ -198,7 +199,6 @@ struct FusedArgs {
     uint32_t units_max;
     const uint32_t* d_units;       // device count of units
     uint32_t* work;
-    uint32_t ray_level;            // object-tree level at and below which rays descend individually
     unsigned long long* node_tests;
     unsigned long long* tri_tests;
     uint32_t* err;

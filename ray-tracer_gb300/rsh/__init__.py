@@ -98,6 +98,19 @@ class BatchSegment(C.Structure):
                 ("hits", C.c_void_p), ("flags", C.c_void_p)]
 
 
+TUNE_DEFAULT = 0xFFFFFFFF
+
+
+class SceneTuning(C.Structure):
+    _fields_ = [("grid_bits", C.c_uint32), ("dir_log2", C.c_uint32), ("ray_level", C.c_uint32)]
+
+
+class TuneSpace(C.Structure):
+    _fields_ = [("grid_bits", C.c_void_p), ("n_grid", C.c_uint32), ("dir_log2", C.c_void_p), ("n_dir", C.c_uint32),
+                ("ray_levels", C.c_void_p), ("n_ray_level", C.c_uint32), ("packet_sizes", C.c_void_p),
+                ("n_packet", C.c_uint32), ("reps", C.c_uint32)]
+
+
 class Request(C.Structure):
     _fields_ = [("scene_index", C.c_uint32), ("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("depth", C.c_uint32), ("light_count", C.c_uint32), ("lights", Light * 8)]
@@ -193,6 +206,9 @@ SIGNATURES = {
     "rsh_batch_stats_get": (C.c_int, [_P, _P]),
     "rsh_autotune": (C.c_int, [_P, _P, _U32, _P, _U32, _P, _U32, _P, _U32, _P, _P]),
     "rsh_trace_rays_fused": (C.c_int, [_P, _P, _P, _U32, C.c_int, _P, _P, _P]),
+    "rsh_scene_set_tuning": (C.c_int, [_P, _P]),
+    "rsh_scene_get_tuning": (C.c_int, [_P, _P]),
+    "rsh_autotune_scenes": (C.c_int, [_P, _P, _U32, _P, _P, _P, _P]),
     "rsh_server_create": (C.c_int, [_P, _P, _U32, _U64, _U32, _P]),
     "rsh_server_submit": (C.c_int, [_P, _P, _P]),
     "rsh_server_wait": (C.c_int, [_P, _U64, _U32, _P, _P, _P]),
@@ -410,6 +426,16 @@ class Scene:
                                              None if n is None else n.ctypes.data, m.shape[0], stream),
               "rsh_scene_set_transforms")
 
+    def set_tuning(self, grid_bits=TUNE_DEFAULT, dir_log2=TUNE_DEFAULT, ray_level=TUNE_DEFAULT):
+        """This scene's own hash width and switch level in the batched form (TUNE_DEFAULT: the context's)."""
+        t = SceneTuning(grid_bits, dir_log2, ray_level)
+        check(lib().rsh_scene_set_tuning(self.handle, C.byref(t)), "rsh_scene_set_tuning")
+
+    def tuning(self) -> dict:
+        t = SceneTuning()
+        check(lib().rsh_scene_get_tuning(self.handle, C.byref(t)), "rsh_scene_get_tuning")
+        return {"grid_bits": t.grid_bits, "dir_log2": t.dir_log2, "ray_level": t.ray_level}
+
     def triangles(self) -> np.ndarray:
         """The scene's current triangles in original order (float32 [T,3,4], w as uploaded)."""
         T = self.tri_count
@@ -444,6 +470,20 @@ class Context:
         for k, v in kw.items():
             setattr(self.config, k, v)
         check(lib().rsh_set_config(self.handle, C.byref(self.config)), "rsh_set_config")
+
+    def autotune_scenes(self, segments, count: int, grid_bits=(), dir_log2=(), ray_levels=(), packet_sizes=(),
+                        reps: int = 2, stream=None) -> tuple:
+        """rsh_autotune_scenes over a BatchSegment array; returns (tuned ms, untuned ms) of the whole batch.
+        The chosen packet size lands in this context, the rest in each scene (Scene.tuning())."""
+        lists = [(C.c_uint32 * max(1, len(v)))(*v) for v in (grid_bits, dir_log2, ray_levels, packet_sizes)]
+        sp = TuneSpace(C.cast(lists[0], C.c_void_p), len(grid_bits), C.cast(lists[1], C.c_void_p), len(dir_log2),
+                       C.cast(lists[2], C.c_void_p), len(ray_levels), C.cast(lists[3], C.c_void_p),
+                       len(packet_sizes), reps)
+        best, untuned = C.c_float(), C.c_float()
+        check(lib().rsh_autotune_scenes(self.handle, segments, count, C.byref(sp), stream, C.byref(best),
+                                        C.byref(untuned)), "rsh_autotune_scenes")
+        check(lib().rsh_get_config(self.handle, C.byref(self.config)), "rsh_get_config")
+        return best.value, untuned.value
 
     def scene(self, positions, normals=None, material_ids=None, materials=None, object_ids=None) -> Scene:
         return Scene(self, positions, normals, material_ids, materials, object_ids)

@@ -153,3 +153,77 @@ def test_many_segments_drop_low_hash_bits():
     for sc in scs:
         sc.destroy()
     ctx.destroy()
+
+
+def _segments(ctx, sd, scs, sizes, which, anyh, rng):
+    segs = (rsh.BatchSegment * len(sizes))()
+    keep = []
+    for i, (n, w, a) in enumerate(zip(sizes, which, anyh)):
+        r = scenes.surface_rays(sd[w], n, rng)
+        if a:
+            r["tmax"] = rng.uniform(0.1, 10.0, n).astype(np.float32)
+        dr = rsh.DeviceArray.from_numpy(r)
+        out = rsh.DeviceArray(n, np.uint32 if a else np.uint64)
+        keep.append((r, dr, out))
+        segs[i].scene = scs[w].handle
+        segs[i].rays = dr.ptr
+        segs[i].n = n
+        segs[i].any_hit = int(a)
+        segs[i].hits = None if a else out.ptr
+        segs[i].flags = out.ptr if a else None
+    return segs, keep
+
+
+def _check_segments(sd, which, anyh, keep):
+    for i, (r, _, out) in enumerate(keep):
+        assert np.array_equal(out.numpy(len(r)), oracle.brute(sd[which[i]].positions, r, bool(anyh[i]))), i
+
+
+def test_scene_tuning_mixed_widths_and_levels():
+    """Scenes of one batch with their own hash widths (8 and 30 bits) and switch levels (0 and 15): the tag
+    sits above the widest hash, each segment keeps its own level, and results equal brute force."""
+    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=6)
+    sd = [scenes.random_soup(t, np.random.default_rng(400 + i)) for i, t in enumerate([8_000, 30_000])]
+    scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]
+    scs[0].set_tuning(grid_bits=8, dir_log2=3, ray_level=0)
+    scs[1].set_tuning(grid_bits=2, dir_log2=1, ray_level=15)
+    assert scs[0].tuning() == {"grid_bits": 8, "dir_log2": 3, "ray_level": 0}
+    assert scs[1].tuning()["ray_level"] == 15
+    which, anyh = [0, 1, 0, 1, 1], [False, False, True, True, False]
+    segs, keep = _segments(ctx, sd, scs, [9_000, 12_001, 5_000, 7_000, 64], which, anyh, np.random.default_rng(41))
+    rsh.check(rsh.lib().rsh_batch_trace(ctx.handle, segs, len(which), None), "batch")
+    ctx.check_device_errors()
+    _check_segments(sd, which, anyh, keep)
+    for bad in ({"grid_bits": 11}, {"dir_log2": 0}, {"ray_level": 16}):
+        with pytest.raises(rsh.RshError):
+            scs[0].set_tuning(**bad)
+    scs[0].set_tuning()  # back to the context's
+    assert scs[0].tuning() == {"grid_bits": rsh.TUNE_DEFAULT, "dir_log2": rsh.TUNE_DEFAULT,
+                               "ray_level": rsh.TUNE_DEFAULT}
+    for sc in scs:
+        sc.destroy()
+    ctx.destroy()
+
+
+def test_autotune_scenes_per_scene_choice():
+    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=6)
+    sd = [scenes.random_soup(t, np.random.default_rng(500 + i)) for i, t in enumerate([6_000, 25_000, 60_000])]
+    scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]
+    which, anyh = [0, 1, 2, 2, 1, 0], [False, True, False, True, False, True]
+    segs, keep = _segments(ctx, sd, scs, [20_000, 30_000, 50_000, 20_000, 4_000, 9_000], which, anyh,
+                           np.random.default_rng(51))
+    best_ms, untuned_ms = ctx.autotune_scenes(segs, len(which), grid_bits=(4, 6), dir_log2=(3, 5),
+                                              ray_levels=(2, 4), packet_sizes=(8, 16))
+    assert best_ms > 0 and untuned_ms > 0
+    assert ctx.config.packet_size in (8, 16)
+    for sc in scs:
+        t = sc.tuning()
+        assert t["grid_bits"] in (4, 5, 6) and t["dir_log2"] in (3, 4, 5) and t["ray_level"] in (2, 4)
+    for _, _, out in keep:
+        out.fill_bytes(0x5A)
+    rsh.check(rsh.lib().rsh_batch_trace(ctx.handle, segs, len(which), None), "batch")
+    ctx.check_device_errors()
+    _check_segments(sd, which, anyh, keep)
+    for sc in scs:
+        sc.destroy()
+    ctx.destroy()
