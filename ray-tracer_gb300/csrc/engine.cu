@@ -23,7 +23,7 @@ static std::atomic<uint64_t> g_launches{0};
 void note_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 int stage_begin(rsh_ctx* ctx, int stage, cudaStream_t s) {
-    if (!(ctx->cfg.flags & RSH_FLAG_STAGE_TIMERS)) return -1;
+    if (!(ctx->cfg.flags & RSH_FLAG_STAGE_TIMERS) || ctx->timers_paused) return -1;
     while (ctx->tev.size() < ctx->tev_used + 2) {
         cudaEvent_t ev;
         if (cudaEventCreate(&ev) != cudaSuccess) return -1;
@@ -1111,10 +1111,16 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     RSH_CUDA(launch_raygen_primary(to_camp(ctx->cam), W, H, prays, ppix, s));
     if (fused) {
         rsh_batch_segment seg{sc, prays, np, 0, reinterpret_cast<uint64_t*>(phits), nullptr};
-        RSH_TRY(rsh_batch_trace(ctx, &seg, 1, s));
+        ctx->timers_paused = true;  // the primary window times the whole primary pass
+        const rsh_status pst = batch_trace(ctx, &seg, 1, s);
+        ctx->timers_paused = false;
+        RSH_TRY(pst);
     } else {
         RSH_CUDA(launch_fill_u64(phits, RSH_HIT_NONE, np, s));
-        RSH_TRY(trace_ordered(ctx, sc, prays, np, false, nullptr, phits, s));
+        ctx->timers_paused = true;
+        const rsh_status pst = trace_ordered(ctx, sc, prays, np, false, nullptr, phits, s);
+        ctx->timers_paused = false;
+        RSH_TRY(pst);
     }
     RSH_CUDA(launch_resolve(sc->pos, sc->nrm, sc->mat, prays, phits, ppix, np,
                             static_cast<float4*>(ctx->surf0_pos.ptr), static_cast<float4*>(ctx->surf0_nrm.ptr), s));

@@ -84,6 +84,7 @@ struct rsh_ctx {
     std::vector<cudaEvent_t> tev;
     std::vector<std::pair<int, uint32_t>> tmarks;
     uint32_t tev_used = 0;
+    bool timers_paused = false;  // stages inside an already-timed window record no marks of their own
 };
 
 namespace rsh {

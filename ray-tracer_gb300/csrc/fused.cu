@@ -140,7 +140,12 @@ RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t la
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, has)) break;
+        if (!__any_sync(0xffffffffu, has)) {
+            // every lane is idle: the queue is done only once it is exhausted (a job whose ray was occluded
+            // after it was queued is skipped at fetch and takes no lane, so a whole round can come up empty)
+            if (qh >= qn) break;
+            continue;
+        }
         if (!has) continue;
         // what other jobs of this ray found so far
         if (any) {
@@ -182,32 +187,44 @@ RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t la
                 uint32_t first, cnt;
                 node_children(sg.kids, sg.lvl_off, sg.lvl_size, sg.levels, L, idx, first, cnt);
                 const float4* sb = sg.spheres + sg.lvl_off[cl] + first;
-                float te[8];
-                uint32_t ci[8];
-                uint32_t nh = 0;
-                for (uint32_t c = 0; c < cnt; ++c) {
-                    const float4 q = __ldg(sb + c);
-                    ++ntests;
-                    float tc;
-                    if (!job_hits_sphere(ox, oy, oz, dx, dy, dz, tmin, tcur, q, tc)) continue;
-                    if (any) {  // any hit: the order of the subtrees does not change the result, skip sorting
-                        ci[nh++] = first + c;
-                        continue;
+                // children (at most 8, an invariant of the object tree) tested into registers; hits pushed
+                // farthest first by selection, so the nearest pops first
+                if (cnt > 8u) raise_device_error(err, RSH_DEVERR_OVERFLOW);
+                float tcs[8];
+                uint32_t hm = 0;
+#pragma unroll
+                for (uint32_t c = 0; c < 8; ++c) {
+                    tcs[c] = 0.0f;
+                    if (c < cnt) {
+                        const float4 q = __ldg(sb + c);
+                        ++ntests;
+                        float tc;
+                        if (job_hits_sphere(ox, oy, oz, dx, dy, dz, tmin, tcur, q, tc)) {
+                            hm |= 1u << c;
+                            tcs[c] = tc;
+                        }
                     }
-                    uint32_t k = nh++;  // keep te[] sorted descending (farthest first)
-                    while (k > 0 && te[k - 1] < tc) {
-                        te[k] = te[k - 1];
-                        ci[k] = ci[k - 1];
-                        --k;
-                    }
-                    te[k] = tc;
-                    ci[k] = first + c;
                 }
-                if (sp + (int)nh > J_STACK) {
+                if (sp + __popc(hm) > J_STACK) {
                     raise_device_error(err, RSH_DEVERR_OVERFLOW);
-                    nh = 0;
+                    hm = 0;
                 }
-                for (uint32_t k = 0; k < nh; ++k) stk[sp++] = (cl << 24) | ci[k];
+                while (hm) {
+                    uint32_t bc = 0;
+                    float bt = -INFINITY;
+                    if (!any) {
+#pragma unroll
+                        for (uint32_t c = 0; c < 8; ++c)
+                            if (((hm >> c) & 1u) && tcs[c] >= bt) {
+                                bt = tcs[c];
+                                bc = c;
+                            }
+                    } else {
+                        bc = __ffs(hm) - 1u;
+                    }
+                    hm &= ~(1u << bc);
+                    stk[sp++] = (cl << 24) | (first + bc);
+                }
             }
         }
         if (sp == 0) has = false;
