@@ -218,6 +218,7 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         f.spheres = sc->h.spheres;
         f.kids = sc->h.kids;
         f.tris = sc->h.tris;
+        f.boxes = sc->h.boxes;
         f.tri_count = sc->tri_count;
         f.cluster = sc->h.cluster;
         f.levels = sc->h.levels;

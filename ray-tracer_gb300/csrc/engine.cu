@@ -607,7 +607,8 @@ rsh_status rsh_scene_upload(rsh_ctx* ctx, const rsh_scene_desc* d, rsh_scene** o
     }
     uint32_t total = 0;
     for (uint32_t l = 0; l < sc->h.levels; ++l) total += sc->h.level_size[l];
-    sc->bytes = tri_bytes * 3 + 8ull * T + 16ull * total + sizeof(rsh_material) * sc->material_count;
+    sc->bytes = tri_bytes * 3 + 8ull * T + 48ull * total +
+                sizeof(rsh_material) * sc->material_count;
     ctx->allocated += sc->bytes;
     *out = sc;
     return RSH_OK;
@@ -627,6 +628,7 @@ rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* sc) {
     if (sc->h.kids) cudaFree(sc->h.kids);
     if (sc->h.tris) cudaFree(sc->h.tris);
     if (sc->h.order) cudaFree(sc->h.order);
+    if (sc->h.boxes) cudaFree(sc->h.boxes);
     if (ctx && ctx->allocated >= sc->bytes) ctx->allocated -= sc->bytes;
     delete sc;
     return RSH_OK;
@@ -655,7 +657,8 @@ rsh_status rsh_build_object_hierarchy(rsh_ctx* ctx, rsh_scene* sc, rsh_stream_t 
         }
     }
     RSH_CUDA(cudaStreamSynchronize(s));
-    for (void* p : {(void*)sc->h.spheres, (void*)sc->h.kids, (void*)sc->h.tris, (void*)sc->h.order})
+    for (void* p : {(void*)sc->h.spheres, (void*)sc->h.kids, (void*)sc->h.tris, (void*)sc->h.order,
+                    (void*)sc->h.boxes})
         if (p) cudaFree(p);
     sc->h = ObjHierarchy();
     void* scr = nullptr;

@@ -121,8 +121,9 @@ __global__ void k_level_nodes(const uint32_t* __restrict__ firsts, uint32_t nn, 
 
 // One warp per node: the sphere over every vertex of the node's triangle range. Min/max and max
 // reductions are exact in any order.
+// Also the node's box, widened by `pad` on every side.
 __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t* __restrict__ tstart, uint32_t nnodes,
-                                float4* __restrict__ sph) {
+                                float4* __restrict__ sph, float4* __restrict__ box, float pad) {
     const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (j >= nnodes) return;
@@ -146,6 +147,10 @@ __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t*
         mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
         mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
         mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+    }
+    if (lane == 0) {
+        box[2 * j] = make_float4(mnx - pad, mny - pad, mnz - pad, 0.f);
+        box[2 * j + 1] = make_float4(mxx + pad, mxy + pad, mxz + pad, 0.f);
     }
     const v3 c = v3{(mnx + mxx) * 0.5f, (mny + mxy) * 0.5f, (mnz + mxz) * 0.5f};
     float r2 = 0.f;
@@ -182,6 +187,7 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     if ((e = cudaMalloc(&h.kids, sizeof(uint32_t) * (node_cap + 16))) != cudaSuccess) return e;
     if ((e = cudaMalloc(&h.tris, sizeof(float4) * 3ull * n)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&h.order, sizeof(uint32_t) * n)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h.boxes, 2 * sizeof(float4) * node_cap)) != cudaSuccess) return e;
 
     char* b = static_cast<char*>(scratch);
     uint32_t* codes = reinterpret_cast<uint32_t*>(b);
@@ -227,6 +233,11 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
         cudaFree(perm_tmp);
         return e;
     }
+    // cluster boxes are widened by 1e-5 of the scene's largest coordinate magnitude: far more than the
+    // rounding of a float slab test over the scene, so the box cull never drops a hit of the watertight test
+    float smax = 0.0f;
+    for (int a = 0; a < 3; ++a) smax = fmaxf(smax, fmaxf(fabsf(lo[a]), fabsf(hi[a])));
+    const float box_pad = 1e-5f * smax + 1e-30f;
     // levels, bottom up; each level's size is read back (a scene build, not a per-frame step)
     uint32_t items = n, total = 0;
     const uint32_t* start = nullptr;  // items of level 0 are the triangles
@@ -255,7 +266,8 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
         k_level_nodes<<<(nn + 256) / 256, 256, 0, s>>>(firsts, nn, items, start, n, l == 0,
                                                        h.kids + total + l, nstart);
         note_launch();
-        k_level_spheres<<<(nn * 32 + 127) / 128, 128, 0, s>>>(h.tris, nstart, nn, h.spheres + total);
+        k_level_spheres<<<(nn * 32 + 127) / 128, 128, 0, s>>>(h.tris, nstart, nn, h.spheres + total,
+                                                              h.boxes + 2ull * total, box_pad);
         note_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) break;
         total += nn;
