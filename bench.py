@@ -188,7 +188,7 @@ def cpu_baseline(s, crop=(240, 136), threads=None, steps=1):
     hi = s.positions[..., :3].reshape(-1, 3).max(0)
     # the GPU path's default configuration (grid bits, direction bits, packet, cluster, ray level)
     dc = rsh.default_config()
-    g, b, P, K, rl = dc.grid_bits, dc.dir_log2, dc.packet_size, dc.cluster_size, dc.ray_level
+    g, b, P, K, rl = dc.grid_bits, dc.dir_log2, dc.packet_size, dc.cluster_size, dc.plain_ray_level
     t0 = time.perf_counter()
     oh = oracle.ObjH(s.positions, K, lo, hi)
     build_s = time.perf_counter() - t0
@@ -403,7 +403,7 @@ def gpu_arm(args, s, rank, world, td):
                    "path": "rsh_render_frame " + ("batched form (RSH_FLAG_FUSED)" if head["flags"] == 2 else "plain"),
                    "triangles": s.tri_count, "width": W, "height": H, "lights": len(s.lights), "depth": depth,
                    "grid_bits": cfg.grid_bits, "dir_log2": cfg.dir_log2, "packet_size": cfg.packet_size,
-                   "cluster_size": cfg.cluster_size, "ray_level": cfg.ray_level,
+                   "cluster_size": cfg.cluster_size, "ray_level": cfg.ray_level, "plain_ray_level": cfg.plain_ray_level,
                    "l2": "inputs larger than L2 (scene + per-frame rays > 129 MB)", "parallelism": f"replicas x{world}"},
         "secondary_rays_per_step": round(sec_rays / args.steps),
         "secondary_ms_per_step": round(sec_ms / args.steps, 3),
@@ -546,10 +546,11 @@ def batching_bench(args):
     st = C.c_void_p()
     rsh.check(lib.rsh_stream_create(C.byref(st)), "stream")
     # per-scene autotuner over origin-grid bits 4..10, direction bins 16..4096 (dir_log2 2..6), switch levels
-    # 2..6 and packet sizes 8/16/32 (coordinate descent; points whose hash exceeds 31 bits are skipped)
+    # 3..7 and 15 (rays alone from the root) and packet sizes 8/16/32 (coordinate descent; points whose hash
+    # exceeds 31 bits are skipped)
     t0 = time.perf_counter()
     tuned_ms, untuned_ms = ctx.autotune_scenes(segs, len(sizes), grid_bits=range(4, 11), dir_log2=range(2, 7),
-                                               ray_levels=range(2, 7), packet_sizes=(8, 16, 32), stream=st)
+                                               ray_levels=(3, 4, 5, 6, 7, 15), packet_sizes=(8, 16, 32), stream=st)
     tune_s = time.perf_counter() - t0
     best = ctx.config
     scene_tuning = [sc.tuning() for sc in scs]

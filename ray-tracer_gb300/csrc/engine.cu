@@ -132,7 +132,7 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ta.capacity = cap;
     ta.cand_count = cc;
     ta.work = w;
-    ta.ray_level = ctx->cfg.ray_level;
+    ta.ray_level = ctx->cfg.plain_ray_level;
     ta.rays = rays;
     ta.sorted_ids = sorted_ids;
     ta.node_tests = ctx->d_stats + 0;
@@ -154,7 +154,7 @@ static rsh_status traverse_and_intersect(rsh_ctx* ctx, const rsh_scene* sc, cons
     ia.flags = flags;
     ia.hits = hits;
     ia.tri_tests = ctx->d_stats + 1;
-    ia.per_ray = ctx->cfg.ray_level > 0 ? 1u : 0u;
+    ia.per_ray = ctx->cfg.plain_ray_level > 0 ? 1u : 0u;
     // Passes over a window of work units [start, start + window). Without overflow the first pass covers
     // every unit. After an overflow the window restarts at the first unfinished unit; if a pass made no
     // progress the window shrinks (units of one pass race for the buffer), down to a single unit, which
@@ -284,7 +284,8 @@ void rsh_config_default(rsh_config* c) {
     c->flags = 0;
     c->reflect_jitter = 0.0f;
     c->seed = 0x5EED0000u;
-    c->ray_level = 4;
+    c->ray_level = 6;
+    c->plain_ray_level = 3;
 }
 
 static rsh_status validate_config(const rsh_config* c) {
@@ -293,7 +294,7 @@ static rsh_status validate_config(const rsh_config* c) {
     if (c->packet_size != 8 && c->packet_size != 16 && c->packet_size != 32) return RSH_ERR_INVALID;
     if (c->cluster_size < 1 || c->cluster_size > 64) return RSH_ERR_INVALID;
     if (!(c->epsilon >= 0.0f)) return RSH_ERR_INVALID;
-    if (c->ray_level > 15) return RSH_ERR_INVALID;
+    if (c->ray_level > 15 || c->plain_ray_level > 15) return RSH_ERR_INVALID;
     return RSH_OK;
 }
 

@@ -46,7 +46,7 @@ class Config(C.Structure):
     _fields_ = [("grid_bits", C.c_uint32), ("dir_log2", C.c_uint32), ("packet_size", C.c_uint32),
                 ("cluster_size", C.c_uint32), ("epsilon", C.c_float), ("hbm_budget", C.c_uint64),
                 ("candidate_capacity", C.c_uint64), ("flags", C.c_uint32), ("reflect_jitter", C.c_float),
-                ("seed", C.c_uint32), ("ray_level", C.c_uint32)]
+                ("seed", C.c_uint32), ("ray_level", C.c_uint32), ("plain_ray_level", C.c_uint32)]
 
 
 class HashParams(C.Structure):

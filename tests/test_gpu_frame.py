@@ -82,7 +82,7 @@ def _check_frame(ctx, s, sc, W, H, depth, jitter, samples=1):
 @pytest.mark.parametrize("jitter", [0.0, 1.0])
 def test_frame_cornell(cornell, jitter, ray_level):
     ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, reflect_jitter=jitter,
-                      ray_level=ray_level)
+                      ray_level=ray_level, plain_ray_level=ray_level)
     sc = ctx.scene(cornell.positions, cornell.normals, cornell.material_ids, cornell.materials)
     st = _check_frame(ctx, cornell, sc, 128, 96, 2, jitter)
     assert st["secondary_ms"] > 0
@@ -134,7 +134,8 @@ def test_rah_ablation_same_results_more_work(cornell, ray_level):
     W, H = 128, 128
     res = {}
     for flags in (0, rsh.FLAG_RAH):
-        ctx = rsh.Context(grid_bits=5, dir_log2=5, packet_size=8, cluster_size=8, flags=flags, ray_level=ray_level)
+        ctx = rsh.Context(grid_bits=5, dir_log2=5, packet_size=8, cluster_size=8, flags=flags, ray_level=ray_level,
+                          plain_ray_level=ray_level)
         sc = ctx.scene(cornell.positions, cornell.normals, cornell.material_ids, cornell.materials)
         ctx.set_camera(rsh.camera_look_at(cornell.eye, cornell.target, cornell.up, cornell.fov, W, H))
         ctx.set_lights(cornell.lights)

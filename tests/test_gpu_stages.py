@@ -472,7 +472,7 @@ def test_pipeline_stages_bitexact_and_vs_brute(ctx, which, any_hit, cornell, sou
 @pytest.mark.parametrize("any_hit", [False, True])
 def test_trace_rays_vs_brute(ctx, any_hit, soup_scene, ray_level):
     s = soup_scene
-    ctx.set_config(ray_level=ray_level)
+    ctx.set_config(ray_level=ray_level, plain_ray_level=ray_level)
     sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
     rng = np.random.default_rng(8)
     rays = scenes.surface_rays(s, 100_000, rng)
@@ -481,14 +481,14 @@ def test_trace_rays_vs_brute(ctx, any_hit, soup_scene, ray_level):
     out = ctx.trace(sc, rays, any_hit)
     bf = oracle.brute(s.positions, rays, any_hit)
     assert np.array_equal(out, bf)
-    ctx.set_config(ray_level=3)
+    ctx.set_config(ray_level=6, plain_ray_level=3)
     sc.destroy()
 
 
 @pytest.mark.parametrize("ray_level", [0, 3])
 def test_overflow_resume_matches_brute(cornell, ray_level):
     c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, candidate_capacity=5000,
-                    ray_level=ray_level)
+                    ray_level=ray_level, plain_ray_level=ray_level)
     s = cornell
     sc = c.scene(s.positions, s.normals, s.material_ids, s.materials)
     rays = scenes.surface_rays(s, 20_000, np.random.default_rng(4))
