@@ -285,7 +285,7 @@ void rsh_config_default(rsh_config* c) {
     c->reflect_jitter = 0.0f;
     c->seed = 0x5EED0000u;
     c->ray_level = 6;
-    c->plain_ray_level = 3;
+    c->plain_ray_level = 4;
 }
 
 static rsh_status validate_config(const rsh_config* c) {

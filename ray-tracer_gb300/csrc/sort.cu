@@ -4,11 +4,14 @@
 // (RayTracer.cu:2385-2409, temp storage sized at :2127-2139). Here: our own kernels, and only the
 // ceil(key_bits / 8) digit passes the hash actually uses.
 //
-//  1. one histogram kernel reads the keys once and builds all passes' 256-bin digit histograms;
+//  1. one histogram kernel reads the keys once and builds all passes' 256-bin digit histograms; its last
+//     CTA turns them into per-pass exclusive digit offsets;
 //  2. one kernel per 8-bit digit pass: each CTA takes a 3840-key tile by atomic ticket, ranks its keys
-//     stably (warp match_any + per-warp digit counters), publishes its per-digit counts, resolves the
-//     per-digit exclusive prefix over earlier tiles by decoupled look-back (bounded spin), then
-//     scatters through shared memory so that global writes are runs of one digit.
+//     stably (warp peer masks from 8 ballots + per-warp digit counters), publishes its per-digit counts,
+//     resolves the per-digit exclusive prefix over earlier tiles by decoupled look-back (bounded spin),
+//     then scatters through shared memory so that global writes are runs of one digit. A status word
+//     holds flag and count together and nothing else is read through it, so it is published and read
+//     with relaxed (not release / acquire) accesses: no memory barrier per tile.
 #include <algorithm>
 
 #include "common.cuh"
@@ -32,8 +35,10 @@ inline uint32_t num_passes(uint32_t key_bits) { return key_bits == 0 ? 1u : (key
 // the passes will use (ceil(n / SR_TILE) rows of 256 words per pass, pass stride `stride` words)
 __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
                             const uint32_t* __restrict__ d_count, uint32_t passes,
-                            uint32_t* __restrict__ hist, uint32_t* __restrict__ status, size_t stride) {
+                            uint32_t* __restrict__ hist, uint32_t* __restrict__ status, size_t stride,
+                            uint32_t* __restrict__ done) {
     __shared__ uint32_t sh[4][256];
+    __shared__ uint32_t s_last;
     for (uint32_t i = threadIdx.x; i < 4u * 256u; i += blockDim.x) (&sh[0][0])[i] = 0u;
     __syncthreads();
     const uint32_t n = dev_count(d_count, n_max);
@@ -53,6 +58,22 @@ __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
     for (uint32_t i = threadIdx.x; i < passes * 256u; i += blockDim.x) {
         const uint32_t v = (&sh[0][0])[i];
         if (v) atomicAdd(hist + i, v);
+    }
+    // the last CTA to finish turns the counts into exclusive digit offsets, in place
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(done, 1u) == gridDim.x - 1u) ? 1u : 0u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (threadIdx.x < passes) {
+        uint32_t* h = hist + 256u * threadIdx.x;
+        uint32_t acc = 0u;
+        for (uint32_t d = 0; d < 256u; ++d) {
+            const uint32_t v = __ldcg(h + d);
+            h[d] = acc;
+            acc += v;
+        }
     }
 }
 
@@ -100,7 +121,13 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
         const uint32_t idx = wbase + j * 32u + lane;
         const bool valid = idx < n;
         const uint32_t d = valid ? ((key[j] >> shift) & 255u) : 256u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t peers = 0xffffffffu;  // lanes holding the same digit (or also invalid)
+#pragma unroll
+        for (int b = 0; b < 9; ++b) {
+            const bool bit = (d >> b) & 1u;
+            const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? bal : ~bal;
+        }
         const uint32_t before = __popc(peers & lanemask_lt());
         uint32_t cnt = 0u;
         if (valid) cnt = s_wc[warp][d];
@@ -121,8 +148,8 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
     }
     // publish the tile's count for this digit early so successors can proceed
     uint32_t* st = status + (size_t)tile * 256u + dg;
-    if (tile == 0) st_release_u32(st, FLAG_PRE | tcount);
-    else st_release_u32(st, FLAG_AGG | tcount);
+    if (tile == 0) st_relaxed_u32(st, FLAG_PRE | tcount);
+    else st_relaxed_u32(st, FLAG_AGG | tcount);
     // exclusive scan over digits of tcount -> s_start
     {
         uint32_t x = tcount;
@@ -142,32 +169,13 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
             }
         }
         __syncthreads();
-        s_start[dg] = s_scan[warp] + x - tcount;
-    }
-    // global digit offset of this pass: exclusive scan of hist over digits
-    uint32_t gex;
-    {
-        const uint32_t hv = __ldg(hist + dg);
-        uint32_t x = hv;
+        const uint32_t start = s_scan[warp] + x - tcount;
+        s_start[dg] = start;
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-            if (lane >= (uint32_t)d) x += y;
-        }
-        __syncthreads();
-        if (lane == 31) s_scan[warp] = x;
-        __syncthreads();
-        if (tid == 0) {
-            uint32_t r = 0;
-            for (int w = 0; w < SR_WARPS; ++w) {
-                const uint32_t t = s_scan[w];
-                s_scan[w] = r;
-                r += t;
-            }
-        }
-        __syncthreads();
-        gex = s_scan[warp] + x - hv;
+        for (int w = 0; w < SR_WARPS; ++w) s_wc[w][dg] += start;  // tile-local position of each warp's run
     }
+    // global digit offset of this pass (exclusive, from the histogram kernel)
+    const uint32_t gex = __ldg(hist + dg);
     // decoupled look-back for this digit, LB predecessors per step: their status words are loaded
     // together (flag and count share one word, so relaxed loads suffice) and folded newest first up to
     // the first one holding an inclusive prefix; a not-yet-published word restarts the step there
@@ -208,7 +216,7 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
                 if (spins > 16) __nanosleep(32);
             }
         }
-        st_release_u32(st, FLAG_PRE | (excl + tcount));
+        st_relaxed_u32(st, FLAG_PRE | (excl + tcount));
     }
     s_gbase[dg] = gex + excl - s_start[dg];
     __syncthreads();
@@ -218,7 +226,7 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
         const uint32_t idx = wbase + j * 32u + lane;
         if (idx < n) {
             const uint32_t d = (key[j] >> shift) & 255u;
-            const uint32_t pos = s_start[d] + s_wc[warp][d] + rank[j];
+            const uint32_t pos = s_wc[warp][d] + rank[j];
             s_keys[pos] = key[j];
             s_vals[pos] = val[j];
         }
@@ -241,7 +249,7 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
 size_t sort_scratch_bytes(uint32_t n_max, uint32_t key_bits) {
     const size_t passes = num_passes(key_bits);
     const size_t tiles = (n_max + SR_TILE - 1) / SR_TILE + 1;
-    const size_t words = 4 * 256 + 8 + passes * tiles * 256;
+    const size_t words = 4 * 256 + 16 + passes * tiles * 256;
     return words * 4 + 2 * (size_t)n_max * 4 + 1024;
 }
 
@@ -253,14 +261,14 @@ cudaError_t launch_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
     const size_t tiles = (n_max + SR_TILE - 1) / SR_TILE + 1;
     uint32_t* w = static_cast<uint32_t*>(scratch);
     uint32_t* hist = w;                       // passes * 256 (room for 4)
-    uint32_t* tickets = w + 4 * 256;          // 8
-    uint32_t* status = tickets + 8;           // passes * tiles * 256
+    uint32_t* tickets = w + 4 * 256;          // 16: one per pass, [8] = histogram CTAs done
+    uint32_t* status = tickets + 16;          // passes * tiles * 256
     uint32_t* alt_keys = status + passes * tiles * 256;
     alt_keys = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(alt_keys) + 255) & ~uintptr_t(255));
     uint32_t* alt_vals = alt_keys + n_max;
-    cudaError_t e = cudaMemsetAsync(w, 0, (4 * 256 + 8) * sizeof(uint32_t), s);
+    cudaError_t e = cudaMemsetAsync(w, 0, (4 * 256 + 16) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    k_sort_hist<<<152 * 2, 256, 0, s>>>(keys_in, n_max, d_count, passes, hist, status, tiles * 256);
+    k_sort_hist<<<152 * 2, 256, 0, s>>>(keys_in, n_max, d_count, passes, hist, status, tiles * 256, tickets + 8);
     // at most the CTAs resident at once: tiles beyond the device count cost nothing, and every ticket
     // below a CTA's tile is held by a running CTA (forward progress of the look-back)
     int dev = 0, sms = 152, per_sm = 1;
@@ -307,13 +315,12 @@ cudaError_t sort_selftest_timeout(void* scratch, uint32_t* err, uint32_t spin_li
     uint32_t* keys_out = vals_in + n;
     uint32_t* vals_out = keys_out + n;
     uint32_t* status = vals_out + n;      // 2 tiles x 256 digits, all "not yet published"
-    uint32_t* hist = status + 2 * 256;    // 256
+    uint32_t* hist = status + 2 * 256;    // 256 exclusive digit offsets: all 0 (every key is digit 0)
     uint32_t* ticket = hist + 256;
     cudaError_t e = cudaMemsetAsync(w, 0, sort_selftest_scratch_bytes() - 1024, s);
     if (e != cudaSuccess) return e;
     const uint32_t one = 1u;  // tile 0's ticket is already gone: the one CTA gets tile 1
     if ((e = cudaMemcpyAsync(ticket, &one, 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(hist, &n, 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;  // all keys digit 0
     k_onesweep<<<1, SR_THREADS, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, nullptr, 0u, hist, status, ticket, err,
                                         spin_limit);
     note_launch();
