@@ -145,7 +145,7 @@ typedef struct rsh_config {
     uint32_t ray_level;        /* batched form: object-tree level at and below which rays leave their packet
                                   and descend one by one (0: packets down to the clusters; default 6) */
     uint32_t plain_ray_level;  /* plain per-frame path: object-tree level at and below which the traversal
-                                  emits per-ray candidates (0: packet candidates only; default 3) */
+                                  emits per-ray candidates (0: packet candidates only; default 4) */
 } rsh_config;
 
 #define RSH_FLAG_STAGE_TIMERS 1u   /* record per-stage CUDA events (TestManager timers) */

@@ -278,7 +278,7 @@ class ObjH:
                             int(any_hit), _p(flags), _p(hits))
         return flags if any_hit else hits
 
-    def trace_keyed(self, rays, keys, key_bits, P, any_hit, ray_level=3):
+    def trace_keyed(self, rays, keys, key_bits, P, any_hit, ray_level=4):
         rays = np.ascontiguousarray(rays, RAY_DTYPE)
         keys = _u32(keys)
         n = len(keys)

@@ -481,7 +481,7 @@ def test_trace_rays_vs_brute(ctx, any_hit, soup_scene, ray_level):
     out = ctx.trace(sc, rays, any_hit)
     bf = oracle.brute(s.positions, rays, any_hit)
     assert np.array_equal(out, bf)
-    ctx.set_config(ray_level=6, plain_ray_level=3)
+    ctx.set_config(ray_level=6, plain_ray_level=4)
     sc.destroy()
 
 
