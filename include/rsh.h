@@ -143,7 +143,8 @@ typedef struct rsh_config {
     float reflect_jitter;      /* 0: mirror reflections; >0: cosine-lobe perturbation weight */
     uint32_t seed;             /* seed of the reflection perturbation */
     uint32_t ray_level;        /* batched form: object-tree level at and below which rays leave their packet
-                                  and descend one by one (0: packets down to the clusters; default 6) */
+                                  and descend one by one (0: packets down to the clusters; at or above the tree depth:
+                                  from the root, no packet phase, no ray hierarchy; default 15) */
     uint32_t plain_ray_level;  /* plain per-frame path: object-tree level at and below which the traversal
                                   emits per-ray candidates (0: packet candidates only; default 4) */
 } rsh_config;
@@ -479,7 +480,8 @@ rsh_status rsh_autotune(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_
                         rsh_stream_t stream, rsh_config* best);
 
 /* Per-scene tuning of the batched form (rsh_batch_trace, its graphs and the server): origin-grid bits,
- * direction bins (dir_log2) and the object-tree level at which rays leave their packets. A field equal
+ * direction bins (dir_log2) and the object-tree level at which rays leave their packets (at or above the
+ * tree's depth for every segment of a batch: the rays-only kernel, no ray hierarchy built). A field equal
  * to RSH_TUNE_DEFAULT takes the context's value. The plain per-frame path ignores it. No counterpart in
  * the reference (its hash has no parameters, RayTracer.cu:147-198). */
 #define RSH_TUNE_DEFAULT 0xFFFFFFFFu
@@ -502,7 +504,9 @@ typedef struct rsh_tune_space {
 /* Per-scene autotuner: coordinate descent over the space. The packet size (shared by every segment of a
  * batch) is chosen on the whole batch; then, for each distinct scene, grid bits, direction bins and the
  * switch level are chosen on that scene's segments alone, one parameter at a time, and stored in the
- * scene (rsh_scene_set_tuning); last, the packet size is chosen again with the scenes tuned. Points whose
+ * scene (rsh_scene_set_tuning); then every scene at switch level 15 at once is tried against that (the
+ * rays-only kernel, which skips the ray hierarchy, runs only when no segment uses packets below the root);
+ * last, the packet size is chosen again with the scenes tuned. Points whose
  * hash is wider than 31 bits are skipped. *best_ms (optional) is the whole batch's time with the final
  * choice, *untuned_ms (optional) its time with the context's configuration and no scene tuning. */
 rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count,

@@ -114,6 +114,7 @@ namespace {
 
 struct BatchPlan {
     uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0, hash_drop = 0;
+    uint32_t rays_only = 1;  // cleared by any segment whose rays use packets below the root
     void *rays_all, *keys, *trimmed, *ckeys, *cbases, *counts, *skeys, *svals, *sorted_keys, *sorted_ids, *scr;
     void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work, *sched, *seg_delta;
     std::vector<PrepSeg> h_prep;
@@ -228,6 +229,7 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         }
         f.any_hit = p.any_hit;
         f.ray_level = tc.ray_level;
+        if (tc.ray_level < sc->h.levels) pl.rays_only = 0;
         f.flags = g.flags;
         f.hits = reinterpret_cast<unsigned long long*>(g.hits);
         f.slot_base = start;
@@ -344,10 +346,12 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
                                static_cast<uint32_t*>(pl.cbases), static_cast<uint32_t*>(pl.trimmed), cnt, pl.total,
                                nullptr, nullptr, pl.scr, ctx->d_err, s, &po));
     stage_end(ctx, th, s);
-    th = stage_begin(ctx, RSH_STAGE_BUILD, s);
-    RSH_CUDA(launch_build_rsh(static_cast<rsh_ray*>(pl.rays_all), static_cast<uint32_t*>(pl.padded), pl.max_padded,
-                              totals, pl.P, static_cast<rsh_node*>(pl.nodes), s));
-    stage_end(ctx, th, s);
+    if (!pl.rays_only) {  // rays that leave their packets at the root never read the ray hierarchy
+        th = stage_begin(ctx, RSH_STAGE_BUILD, s);
+        RSH_CUDA(launch_build_rsh(static_cast<rsh_ray*>(pl.rays_all), static_cast<uint32_t*>(pl.padded),
+                                  pl.max_padded, totals, pl.P, static_cast<rsh_node*>(pl.nodes), s));
+        stage_end(ctx, th, s);
+    }
     RSH_CUDA(cudaMemsetAsync(pl.work, 0, 16, s));
     FusedArgs fa{};
     fa.nodes = static_cast<rsh_node*>(pl.nodes);
@@ -361,6 +365,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     fa.units_max = pl.max_padded / pl.unit_rays;
     fa.d_units = totals + 1;
     fa.work = static_cast<uint32_t*>(pl.work);
+    fa.rays_only = pl.rays_only;
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;
@@ -675,6 +680,19 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
         }
     }
     RSH_TRY(time_batch(ctx, segs, count, reps, stream, &ms));
+    // the rays-only kernel runs only when every segment's rays leave their packets at the root, which the
+    // per-scene choices above cannot see: try all scenes there at once too
+    {
+        std::vector<rsh_scene_tuning> keep;
+        for (rsh_scene* sc : scenes) keep.push_back(sc->tune);
+        for (rsh_scene* sc : scenes) sc->tune.ray_level = 15u;
+        float m2;
+        if (time_batch(ctx, segs, count, reps, stream, &m2) == RSH_OK && m2 < ms) {
+            ms = m2;
+        } else {
+            for (size_t k = 0; k < scenes.size(); ++k) scenes[k]->tune = keep[k];
+        }
+    }
     ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
     if (best_ms) *best_ms = ms;
     return RSH_OK;

@@ -284,7 +284,7 @@ void rsh_config_default(rsh_config* c) {
     c->flags = 0;
     c->reflect_jitter = 0.0f;
     c->seed = 0x5EED0000u;
-    c->ray_level = 6;
+    c->ray_level = 15;
     c->plain_ray_level = 4;
 }
 

@@ -88,8 +88,8 @@ RSH_DEV bool box_hit(float4 b0, float4 b1, float ox, float oy, float oz, float i
     return tn <= tf;
 }
 
-template <int P>
-RSH_DEV void run_jobs(FusedSmem<P>& S, const FusedSeg& sg, bool any, uint32_t lane, unsigned long long& ntests,
+template <int P, class SM>
+RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsigned long long& ntests,
                       unsigned long long& ttests, uint32_t* err) {
     const uint32_t qn = S.qn;
     uint32_t qh = 0;
@@ -532,8 +532,107 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
     }
 }
 
+// Rays-only form: every segment's switch level is at or above its tree's depth, so a ray leaves its packet
+// at the root. No packet phase: a warp stages its unit's rays and queues one root job per active ray.
+// The shared footprint is the per-ray state and a queue of one unit (so more warps fit per SM).
+template <int P>
+struct RaySmem {
+    float4 ro[8 * P];
+    float4 rs[8 * P];
+    float4 rd[8 * P];
+    uint32_t meta[8 * P];
+    uint32_t slot[8 * P];
+    unsigned long long best[8 * P];
+    uint32_t jobs[8 * P];
+    uint32_t qn;
+};
+
+#ifndef RSH_RAYS_MIN_BLOCKS
+#define RSH_RAYS_MIN_BLOCKS 8
+#endif
+
+template <int P>
+__global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(FusedArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    RaySmem<P>& S = reinterpret_cast<RaySmem<P>*>(smem_raw)[threadIdx.x >> 5];
+    const uint32_t lane = lane_id();
+    const uint32_t units = dev_count(a.d_units, a.units_max);
+    unsigned long long ntests = 0, ttests = 0;
+    constexpr uint32_t R = 8 * P;
+    if (lane == 0) S.qn = 0;
+    __syncwarp();
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(&a.work[0], 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= units) break;
+        const uint32_t sidx = find_segment(a.segs, a.nseg, u);
+        const FusedSeg& sg = a.segs[sidx];
+        const bool any = sg.any_hit != 0;
+        uint32_t qn = 0;
+        for (uint32_t base = 0; base < R; base += 32) {
+            const uint32_t i = base + lane;
+            const uint32_t id = __ldg(a.sorted_ids + u * R + i);
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, -1.f);
+            if (id != INVALID_ID) load_ray(a.rays, id, o, d);
+            const bool active = (id != INVALID_ID) && (d.w > o.w);
+            const RayWT w = wt_setup(o, d);
+            S.ro[i] = o;
+            S.rs[i] = make_float4(w.sx, w.sy, w.sz, d.w);
+            S.rd[i] = d;
+            S.meta[i] = (uint32_t)w.kx | ((uint32_t)w.ky << 2) | ((uint32_t)w.kz << 4) | (active ? 64u : 0u);
+            S.slot[i] = id;
+            S.best[i] = RSH_HIT_NONE;
+            const uint32_t bl = __ballot_sync(0xffffffffu, active);
+            if (active) S.jobs[qn + __popc(bl & lanemask_lt())] = job_word(i, sg.levels, 0u);
+            qn += __popc(bl);
+        }
+        __syncwarp();
+        if (lane == 0) S.qn = qn;
+        __syncwarp();
+        if (qn) run_jobs<P>(S, sg, any, lane, ntests, ttests, a.err);
+        __syncwarp();
+        for (uint32_t i = lane; i < R; i += 32) {
+            const uint32_t meta = S.meta[i];
+            if (!(meta & 64u)) continue;
+            const uint32_t slot = S.slot[i] - sg.slot_base;
+            if (any) sg.flags[slot] = (meta & 128u) ? RSH_OCCLUDED : 0u;
+            else sg.hits[slot] = S.best[i];
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        ntests += __shfl_xor_sync(0xffffffffu, ntests, d);
+        ttests += __shfl_xor_sync(0xffffffffu, ttests, d);
+    }
+    if (lane == 0) {
+        if (a.node_tests) atomicAdd(a.node_tests, ntests);
+        if (a.tri_tests) atomicAdd(a.tri_tests, ttests);
+    }
+}
+
+template <int P>
+static cudaError_t launch_fused_rays_p(const FusedArgs& a, cudaStream_t s) {
+    const size_t smem = sizeof(RaySmem<P>) * FW;
+    cudaError_t e = cudaFuncSetAttribute(k_fused_rays<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays<P>, FW * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    uint32_t grid = (uint32_t)(sms * per_sm);
+    const uint32_t need = (a.units_max + FW - 1) / FW;
+    if (need < grid) grid = need > 0 ? need : 1;
+    k_fused_rays<P><<<grid, FW * 32, smem, s>>>(a);
+    note_launch();
+    return cudaGetLastError();
+}
+
 template <int P>
 static cudaError_t launch_fused_p(const FusedArgs& a, cudaStream_t s) {
+    if (a.rays_only) return launch_fused_rays_p<P>(a, s);
     const size_t smem = sizeof(FusedSmem<P>) * FW;
     cudaError_t e = cudaFuncSetAttribute(k_fused<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -201,6 +201,7 @@ struct FusedArgs {
     uint32_t units_max;
     const uint32_t* d_units;       // device count of units
     uint32_t* work;
+    uint32_t rays_only;            // every segment's switch level >= its tree depth: no packet phase
     unsigned long long* node_tests;
     unsigned long long* tri_tests;
     uint32_t* err;

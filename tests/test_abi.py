@@ -53,7 +53,7 @@ def test_struct_layouts_match_header():
 def test_config_defaults_and_validation():
     c = rsh.default_config()
     assert (c.grid_bits, c.dir_log2, c.packet_size, c.cluster_size, c.ray_level, c.plain_ray_level) == \
-        (4, 6, 8, 6, 6, 4)
+        (4, 6, 8, 6, 15, 4)
     assert abs(c.epsilon - 0.01) < 1e-9
     lib = rsh.load()
     out = C.c_void_p()

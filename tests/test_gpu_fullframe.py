@@ -38,9 +38,10 @@ def _settle(ctx, s, b, key, idx, plain, fused):
     return int((plain[key][idx] == bf).sum()), int((fused[key][idx] == bf).sum())
 
 
-def test_fused_and_plain_paths_agree_on_the_full_frame():
+@pytest.mark.parametrize("ray_level", [6, 15])  # packets above the top level / rays alone from the root
+def test_fused_and_plain_paths_agree_on_the_full_frame(ray_level):
     s = scenes.by_name("P")
-    ctx = rsh.Context(rsh.default_config(reflect_jitter=float(s.jitter), seed=s.seed))
+    ctx = rsh.Context(rsh.default_config(reflect_jitter=float(s.jitter), seed=s.seed, ray_level=ray_level))
     sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
     ctx.set_camera(rsh.camera_look_at(s.eye, s.target, s.up, s.fov, s.width, s.height))
     ctx.set_lights(s.lights)
