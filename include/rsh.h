@@ -506,8 +506,9 @@ typedef struct rsh_tune_space {
  * switch level are chosen on that scene's segments alone, one parameter at a time, and stored in the
  * scene (rsh_scene_set_tuning); then every scene at switch level 15 at once is tried against that (the
  * rays-only kernel, which skips the ray hierarchy, runs only when no segment uses packets below the root);
- * last, the packet size is chosen again with the scenes tuned. Points whose
- * hash is wider than 31 bits are skipped. *best_ms (optional) is the whole batch's time with the final
+ * last, the packet size is chosen again with the scenes tuned. The search keeps the untuned configuration
+ * when its result is not faster on the whole batch. Points whose hash does not fit beside the batch's
+ * segment tag in 31 bits are skipped. *best_ms (optional) is the whole batch's time with the final
  * choice, *untuned_ms (optional) its time with the context's configuration and no scene tuning. */
 rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count,
                                const rsh_tune_space* space, rsh_stream_t stream, float* best_ms,

@@ -637,6 +637,11 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
         (space->n_ray_level && !space->ray_levels) || (space->n_packet && !space->packet_sizes))
         return RSH_ERR_INVALID;
     const uint32_t reps = space->reps ? space->reps : 2u;
+    // hash widths that fit beside this batch's segment tag without dropping bits: wider points would be
+    // tuned on a scene's own segments (a narrower tag) but lose their low bits in the whole batch
+    uint32_t tag_bits = 0;
+    while ((1u << tag_bits) < count) ++tag_bits;
+    const uint32_t max_hash_bits = 31u - std::min(tag_bits, 31u);
     std::vector<rsh_scene*> scenes;
     for (uint32_t i = 0; i < count; ++i) {
         if (!segs[i].scene) return RSH_ERR_INVALID;
@@ -645,8 +650,10 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
     }
     const rsh_scene_tuning none{RSH_TUNE_DEFAULT, RSH_TUNE_DEFAULT, RSH_TUNE_DEFAULT};
     for (rsh_scene* sc : scenes) sc->tune = none;
+    const rsh_config start = ctx->cfg;
     float ms;
     RSH_TRY(time_batch(ctx, segs, count, reps, stream, &ms));
+    const float untuned = ms;
     if (untuned_ms) *untuned_ms = ms;
     ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
     // each scene on its own segments, one parameter at a time
@@ -669,6 +676,7 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
                 uint32_t& field = param == 0 ? trial.grid_bits : param == 1 ? trial.dir_log2 : trial.ray_level;
                 if (field == vals[k]) continue;
                 field = vals[k];
+                if (3u * trial.grid_bits + 2u * trial.dir_log2 > max_hash_bits) continue;
                 if (rsh_scene_set_tuning(sc, &trial) != RSH_OK) continue;
                 float m2;
                 if (time_batch(ctx, sub.data(), (uint32_t)sub.size(), reps, stream, &m2) == RSH_OK && m2 < cur) {
@@ -694,6 +702,13 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
         }
     }
     ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
+    // keep the untuned configuration when the search found nothing faster on the whole batch (the
+    // per-scene steps time sub-batches, which need not add up)
+    if (!(ms < untuned)) {
+        for (rsh_scene* sc : scenes) sc->tune = none;
+        rsh_set_config(ctx, &start);
+        ms = untuned;
+    }
     if (best_ms) *best_ms = ms;
     return RSH_OK;
 }

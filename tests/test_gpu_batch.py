@@ -218,9 +218,11 @@ def test_autotune_scenes_per_scene_choice():
     assert ctx.config.packet_size in (8, 16)
     for sc in scs:
         t = sc.tuning()
-        # a tuned value is one of the swept points or the context's own (where the descent started)
-        assert t["grid_bits"] in (4, 5, 6) and t["dir_log2"] in (3, 4, 5)
-        assert t["ray_level"] in (2, 4, 15, rsh.default_config().ray_level)  # 15: every scene rays-only
+        # a tuned value is one of the swept points or the context's own (where the descent started), or the
+        # scene keeps no tuning at all (the search found nothing faster on the whole batch)
+        D = rsh.TUNE_DEFAULT
+        assert t["grid_bits"] in (4, 5, 6, D) and t["dir_log2"] in (3, 4, 5, D)
+        assert t["ray_level"] in (2, 4, 15, rsh.default_config().ray_level, D)  # 15: every scene rays-only
     for _, _, out in keep:
         out.fill_bytes(0x5A)
     rsh.check(rsh.lib().rsh_batch_trace(ctx.handle, segs, len(which), None), "batch")
