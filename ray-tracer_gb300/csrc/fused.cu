@@ -88,7 +88,9 @@ RSH_DEV bool box_hit(float4 b0, float4 b1, float ox, float oy, float oz, float i
     return tn <= tf;
 }
 
-template <int P, class SM>
+// SOLO: every ray has exactly one job (rays-only form), so no other lane shares its best hit: the shared
+// state is not re-read each step and the best hit is stored once, when the job ends.
+template <int P, bool SOLO = false, class SM>
 RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsigned long long& ntests,
                       unsigned long long& ttests, uint32_t* err) {
     const uint32_t qn = S.qn;
@@ -147,7 +149,8 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
         }
         if (!has) continue;
         // what other jobs of this ray found so far
-        if (any) {
+        if (SOLO) {
+        } else if (any) {
             if (*(volatile uint32_t*)&S.meta[i] & 128u) sp = 0;
         } else {
             const unsigned long long b = *(volatile unsigned long long*)&S.best[i];
@@ -182,7 +185,7 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                         if (key < best) {
                             best = key;
                             tcur = fminf(tcur, th);
-                            atomicMin(&S.best[i], key);
+                            if (!SOLO) atomicMin(&S.best[i], key);
                         }
                     }
                 }
@@ -231,7 +234,10 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                 }
             }
         }
-        if (sp == 0) has = false;
+        if (sp == 0) {
+            if (SOLO && !any) S.best[i] = best;
+            has = false;
+        }
     }
     __syncwarp();
     if (lane == 0) S.qn = 0;
@@ -590,7 +596,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
         __syncwarp();
         if (lane == 0) S.qn = qn;
         __syncwarp();
-        if (qn) run_jobs<P>(S, sg, any, lane, ntests, ttests, a.err);
+        if (qn) run_jobs<P, true>(S, sg, any, lane, ntests, ttests, a.err);
         __syncwarp();
         for (uint32_t i = lane; i < R; i += 32) {
             const uint32_t meta = S.meta[i];
