@@ -167,8 +167,9 @@ typedef struct rsh_frame_stats {
     uint64_t reflection_rays;    /* traced after trimming, all bounces */
     uint64_t chunks;             /* compressed runs, all secondary batches */
     uint64_t candidates;         /* (packet, cluster) pairs emitted by traversal */
-    uint64_t node_tests;         /* packet-node x sphere tests executed */
-    uint64_t tri_tests;          /* ray x triangle tests executed */
+    uint64_t node_tests;         /* node tests executed (packet-node x sphere; a single ray x node box);
+                                    rsh_render_frame: secondary rays only */
+    uint64_t tri_tests;          /* ray x triangle tests executed (rsh_render_frame: secondary rays only) */
     float secondary_ms;          /* first secondary raygen .. last secondary intersection */
     float frame_ms;
     float stage_ms[12];          /* see RSH_STAGE_* */

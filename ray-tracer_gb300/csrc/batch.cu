@@ -298,7 +298,9 @@ rsh_status stage_tables(rsh_ctx* ctx, const BatchPlan& pl, char** out, cudaEvent
 
 // pre_staged != nullptr: tables already in pinned memory owned by the caller (a captured graph, which must
 // not allocate while capturing); otherwise a fenced ring slot of the context.
-rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_staged = nullptr) {
+// reset_stats: zero the node / triangle test counters first (a frame keeps counting over its batches).
+rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_staged = nullptr,
+                         bool reset_stats = true) {
     if (pl.nseg == 0) return RSH_OK;
     char* tables = pre_staged;
     cudaEvent_t fence = nullptr;
@@ -309,7 +311,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     RSH_CUDA(cudaMemcpyAsync(pl.sched, tables + (sizeof(PrepSeg) + sizeof(FusedSeg)) * pl.nseg, 4ull * pl.nseg,
                              cudaMemcpyHostToDevice, s));
     if (fence) RSH_CUDA(cudaEventRecord(fence, s));
-    RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
+    if (reset_stats) RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));
     if (pl.total == 0) return RSH_OK;
     uint32_t* cnt = static_cast<uint32_t*>(pl.counts);
     uint32_t* totals = static_cast<uint32_t*>(pl.totals);
@@ -385,12 +387,53 @@ struct GraphExec {
 }  // namespace
 
 namespace rsh {
+// One segment whose rays are already in a coherent order (the frame's primary rays, generated tile by
+// tile), traced by the rays-only kernel in that order: no hash, compression, sort or ray hierarchy.
+// Scenes whose rays use packets below the root go through batch_trace.
+rsh_status batch_trace_ordered(rsh_ctx* ctx, const rsh_batch_segment& seg, cudaStream_t s) {
+    if (!ctx || !seg.scene) return RSH_ERR_INVALID;
+    const rsh_config tc = tuned_config(ctx->cfg, seg.scene);
+    if (seg.n == 0 || tc.ray_level < seg.scene->h.levels) return batch_trace(ctx, &seg, 1, s, false);
+    BatchPlan pl;
+    RSH_TRY(batch_prepare(ctx, &seg, 1, pl));
+    pl.h_fsegs[0].unit_begin = 0;
+    char* tables = nullptr;
+    cudaEvent_t fence = nullptr;
+    RSH_TRY(stage_tables(ctx, pl, &tables, &fence));
+    RSH_CUDA(cudaMemcpyAsync(pl.fsegs, tables + sizeof(PrepSeg) * pl.nseg, sizeof(FusedSeg), cudaMemcpyHostToDevice,
+                             s));
+    RSH_CUDA(cudaEventRecord(fence, s));
+    if (seg.any_hit) RSH_CUDA(cudaMemsetAsync(seg.flags, 0, 4ull * seg.n, s));
+    else RSH_CUDA(launch_fill_u64(reinterpret_cast<unsigned long long*>(seg.hits), RSH_HIT_NONE, seg.n, s));
+    RSH_CUDA(cudaMemsetAsync(pl.work, 0, 16, s));
+    FusedArgs fa{};
+    fa.packet = pl.P;
+    fa.rays = seg.rays;
+    fa.sorted_ids = nullptr;
+    fa.ordered_n = seg.n;
+    fa.segs = static_cast<FusedSeg*>(pl.fsegs);
+    fa.nseg = 1;
+    fa.unit_seg = nullptr;
+    fa.units_max = (seg.n + pl.unit_rays - 1) / pl.unit_rays;
+    fa.d_units = nullptr;
+    fa.work = static_cast<uint32_t*>(pl.work);
+    fa.rays_only = 1;
+    fa.node_tests = ctx->d_stats;
+    fa.tri_tests = ctx->d_stats + 1;
+    fa.err = ctx->d_err;
+    ctx->last_stream = s;
+    RSH_CUDA(launch_fused(fa, s));
+    ctx->batch_counts_host.assign(1, seg.n);
+    return RSH_OK;
+}
+
 // rsh_batch_trace without resetting the stage timers (a fused frame keeps its own).
-rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream) {
+rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream,
+                       bool reset_stats) {
     BatchPlan pl;
     RSH_TRY(batch_prepare(ctx, segments, count, pl));
     ctx->last_stream = stream;
-    RSH_TRY(batch_enqueue(ctx, pl, stream));
+    RSH_TRY(batch_enqueue(ctx, pl, stream, nullptr, reset_stats));
     ctx->batch_counts_host.assign(1, pl.total);
     return RSH_OK;
 }
@@ -414,7 +457,7 @@ rsh_status rsh_batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint
     if (!ctx) return RSH_ERR_INVALID;
     ctx->tev_used = 0;  // stage timers (RSH_FLAG_STAGE_TIMERS) cover this call only
     ctx->tmarks.clear();
-    return batch_trace(ctx, segments, count, stream);
+    return batch_trace(ctx, segments, count, stream, true);
 }
 
 rsh_status rsh_batch_graph_create(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count,

@@ -1116,7 +1116,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     if (fused) {
         rsh_batch_segment seg{sc, prays, np, 0, reinterpret_cast<uint64_t*>(phits), nullptr};
         ctx->timers_paused = true;  // the primary window times the whole primary pass
-        const rsh_status pst = batch_trace(ctx, &seg, 1, s);
+        const rsh_status pst = batch_trace_ordered(ctx, seg, s);  // tile order is already coherent
         ctx->timers_paused = false;
         RSH_TRY(pst);
     } else {
@@ -1129,6 +1129,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     RSH_CUDA(launch_resolve(sc->pos, sc->nrm, sc->mat, prays, phits, ppix, np,
                             static_cast<float4*>(ctx->surf0_pos.ptr), static_cast<float4*>(ctx->surf0_nrm.ptr), s));
     stage_end(ctx, th, s);
+    RSH_CUDA(cudaMemsetAsync(ctx->d_stats, 0, 64, s));  // the frame's test counters cover secondary rays
     RSH_CUDA(cudaEventRecord(ctx->ev[1], s));  // secondary window starts
 
     const float4* spos = static_cast<const float4*>(ctx->surf0_pos.ptr);
@@ -1167,7 +1168,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
             rsh_batch_segment segs[2] = {
                 {sc, srays, npix * LS, 1, nullptr, sflags},
                 {sc, rrays, npix, 0, reinterpret_cast<uint64_t*>(rhits), nullptr}};
-            RSH_TRY(batch_trace(ctx, segs, 2, s));
+            RSH_TRY(batch_trace(ctx, segs, 2, s, false));
             const uint32_t* seg_cnt = static_cast<const uint32_t*>(ctx->bufs["b_seg_cnt"].ptr);
             const uint32_t* bcnt = static_cast<const uint32_t*>(ctx->bufs["b_counts"].ptr);
             RSH_CUDA(cudaMemcpyAsync(fc + 4 * b, seg_cnt, 4, cudaMemcpyDeviceToDevice, s));

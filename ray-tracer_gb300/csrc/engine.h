@@ -97,8 +97,13 @@ rsh_status ensure_buf(rsh_ctx* ctx, DevBuf& b, size_t bytes);
 void release_buf(rsh_ctx* ctx, DevBuf& b);
 rsh_status make_hash_params(const rsh_scene* sc, const rsh_config& cfg, uint32_t tag_bits, HashP& out);
 void batch_release_ctx(const rsh_ctx* ctx);
-// rsh_batch_trace without resetting the stage timers (used inside a fused frame).
-rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream);
+// rsh_batch_trace without resetting the stage timers (used inside a fused frame, which also keeps its
+// node / triangle test counters running: reset_stats false).
+rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream,
+                       bool reset_stats);
+// One segment of rays already in a coherent order, traced in that order (rays-only kernel); adds to the
+// test counters.
+rsh_status batch_trace_ordered(rsh_ctx* ctx, const rsh_batch_segment& seg, cudaStream_t stream);
 
 // One secondary batch through compress -> sort -> decompress -> build -> traverse -> intersect.
 // keys: per slot (RSH_KEY_NONE = no ray); rays indexed by slot. Output flags/hits indexed by slot

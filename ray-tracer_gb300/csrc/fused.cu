@@ -578,7 +578,8 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
         uint32_t qn = 0;
         for (uint32_t base = 0; base < R; base += 32) {
             const uint32_t i = base + lane;
-            const uint32_t id = __ldg(a.sorted_ids + u * R + i);
+            const uint32_t k = u * R + i;  // no sorted order: the rays' own order, padded past ordered_n
+            const uint32_t id = a.sorted_ids ? __ldg(a.sorted_ids + k) : (k < a.ordered_n ? k : INVALID_ID);
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, -1.f);
             if (id != INVALID_ID) load_ray(a.rays, id, o, d);
             const bool active = (id != INVALID_ID) && (d.w > o.w);

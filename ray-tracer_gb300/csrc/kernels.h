@@ -194,7 +194,8 @@ struct FusedArgs {
     uint32_t node_off[4];
     uint32_t packet;
     const rsh_ray* rays;
-    const uint32_t* sorted_ids;
+    const uint32_t* sorted_ids;    // null (rays-only kernel): rays in their own order, ordered_n of them
+    uint32_t ordered_n;
     const FusedSeg* segs;          // device
     uint32_t nseg;
     const uint32_t* unit_seg;      // device: work unit -> segment (size = units)
