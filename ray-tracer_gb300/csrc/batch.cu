@@ -43,7 +43,7 @@ struct PrepSeg {  // per-segment table of k_batch_prep
 
 __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, uint32_t total, uint32_t tag_shift,
                              uint32_t hash_drop,
-                             rsh_ray* __restrict__ rays_all, uint32_t* __restrict__ keys,
+                             rsh_ray* __restrict__ rays_all, bool gather, uint32_t* __restrict__ keys,
                              uint32_t* __restrict__ seg_cnt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = false;
@@ -58,7 +58,7 @@ __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, ui
         const uint32_t j = i - sg.start;
         float4 o, d;
         load_ray(sg.rays, j, o, d);
-        store_ray(rays_all, i, o, d);
+        if (gather) store_ray(rays_all, i, o, d);  // else the segments already lie back to back there
         uint32_t key = RSH_KEY_NONE;
         valid = d.w > o.w;
         if (valid) key = (lo << tag_shift) | (ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, sg.hp, 0u) >> hash_drop);
@@ -115,6 +115,7 @@ namespace {
 struct BatchPlan {
     uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0, hash_drop = 0;
     uint32_t rays_only = 1;  // cleared by any segment whose rays use packets below the root
+    bool contiguous = false; // the segments' rays lie back to back in one array: no gather
     void *rays_all, *keys, *trimmed, *ckeys, *cbases, *counts, *skeys, *svals, *sorted_keys, *sorted_ids, *scr;
     void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work, *sched, *seg_delta;
     std::vector<PrepSeg> h_prep;
@@ -168,7 +169,11 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     pl.unit_rays = 8 * pl.P;
     pl.max_padded = pl.total + count * pl.unit_rays;
     const uint32_t n = pl.total ? pl.total : 1;
-    RSH_TRY(ensure(ctx, "b_rays", sizeof(rsh_ray) * (size_t)n, &pl.rays_all));
+    pl.contiguous = count > 0;
+    for (uint32_t s = 0, at = 0; s < count; at += segs[s].n, ++s)
+        if (segs[s].n && segs[s].rays != segs[0].rays + at) pl.contiguous = false;
+    if (pl.contiguous) pl.rays_all = const_cast<rsh_ray*>(segs[0].rays);
+    else RSH_TRY(ensure(ctx, "b_rays", sizeof(rsh_ray) * (size_t)n, &pl.rays_all));
     RSH_TRY(ensure(ctx, "b_keys", 4ull * n, &pl.keys));
     RSH_TRY(ensure(ctx, "trimmed", 4ull * n, &pl.trimmed));
     RSH_TRY(ensure(ctx, "ckeys", 4ull * n + 4, &pl.ckeys));
@@ -319,6 +324,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     RSH_CUDA(cudaMemsetAsync(pl.seg_cnt, 0, 4ull * pl.nseg, s));
     k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
                                                        pl.tag_shift, pl.hash_drop, static_cast<rsh_ray*>(pl.rays_all),
+                                                       !pl.contiguous,
                                                        static_cast<uint32_t*>(pl.keys), static_cast<uint32_t*>(pl.seg_cnt));
     note_launch();
     RSH_CUDA(cudaGetLastError());

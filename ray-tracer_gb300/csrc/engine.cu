@@ -339,7 +339,6 @@ rsh_status rsh_destroy(rsh_ctx* ctx) {
     for (auto& b : ctx->bounce) {
         release_buf(ctx, b.shadow_rays);
         release_buf(ctx, b.shadow_flags);
-        release_buf(ctx, b.refl_rays);
         release_buf(ctx, b.refl_hits);
         release_buf(ctx, b.surf_pos);
         release_buf(ctx, b.surf_nrm);
@@ -1096,9 +1095,10 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     RSH_TRY(ensure(ctx, "keys2", 4ull * npix, &keys2));
     for (uint32_t b = 0; b < depth; ++b) {
         BounceBufs& bb = ctx->bounce[b];
-        RSH_TRY(ensure_buf(ctx, bb.shadow_rays, sizeof(rsh_ray) * (size_t)npix * LS));
+        // shadow slots, then the reflection slots right behind them: the batched form traces both
+        // segments from this one array without gathering them
+        RSH_TRY(ensure_buf(ctx, bb.shadow_rays, sizeof(rsh_ray) * (size_t)npix * (LS + 1)));
         RSH_TRY(ensure_buf(ctx, bb.shadow_flags, 4ull * npix * LS));
-        RSH_TRY(ensure_buf(ctx, bb.refl_rays, sizeof(rsh_ray) * (size_t)npix));
         RSH_TRY(ensure_buf(ctx, bb.refl_hits, 8ull * npix));
         RSH_TRY(ensure_buf(ctx, bb.surf_pos, 16ull * npix));
         RSH_TRY(ensure_buf(ctx, bb.surf_nrm, 16ull * npix));
@@ -1154,7 +1154,7 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
         BounceBufs& bb = ctx->bounce[b];
         rsh_ray* srays = static_cast<rsh_ray*>(bb.shadow_rays.ptr);
         uint32_t* sflags = static_cast<uint32_t*>(bb.shadow_flags.ptr);
-        rsh_ray* rrays = static_cast<rsh_ray*>(bb.refl_rays.ptr);
+        rsh_ray* rrays = srays + (size_t)npix * LS;
         unsigned long long* rhits = static_cast<unsigned long long*>(bb.refl_hits.ptr);
         if (fused) {
             // both batches of the bounce in one batched call: 2 segments, one persistent launch
@@ -1302,7 +1302,8 @@ rsh_status rsh_frame_rays(rsh_ctx* ctx, int32_t bounce, int32_t shadow, rsh_ray*
         RSH_CUDA(cudaMemcpy(host_out, bb.shadow_rays.ptr, sizeof(rsh_ray) * npix * ctx->flights,
                             cudaMemcpyDeviceToHost));
     else
-        RSH_CUDA(cudaMemcpy(host_out, bb.refl_rays.ptr, sizeof(rsh_ray) * npix, cudaMemcpyDeviceToHost));
+        RSH_CUDA(cudaMemcpy(host_out, static_cast<rsh_ray*>(bb.shadow_rays.ptr) + npix * ctx->flights,
+                            sizeof(rsh_ray) * npix, cudaMemcpyDeviceToHost));
     return RSH_OK;
 }
 

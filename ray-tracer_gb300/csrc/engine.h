@@ -53,7 +53,7 @@ struct rsh_scene {
 };
 
 struct BounceBufs {
-    rsh::DevBuf shadow_rays, shadow_flags, refl_rays, refl_hits, surf_pos, surf_nrm;
+    rsh::DevBuf shadow_rays, shadow_flags, refl_hits, surf_pos, surf_nrm;  // shadow_rays: then the reflection rays
 };
 
 struct rsh_ctx {
