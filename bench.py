@@ -360,13 +360,15 @@ def gpu_arm(args, s, rank, world, td):
             ms = stage_ms[nm]
             tf = flops_stage[nm] / (ms * 1e9) if ms > 0 else 0.0
             per_stage[nm] = {"ms": round(ms, 4), "TFLOP/s": round(tf, 3), "frac_fp32": round(tf / fp32_peak, 4)}
+        # the batched form's kernel: rays alone from the root when the switch level reaches the tree's depth
+        fused_kernel = "k_fused_rays" if cfg.ray_level >= lib.rsh_scene_levels(sc.handle) else "k_fused"
         if fused_head:
-            per_stage["traverse"]["kernel"] = "k_fused (traversal + intersection)"
+            per_stage["traverse"]["kernel"] = f"{fused_kernel} (traversal + intersection)"
         dom = max(("raygen", "compress", "sort", "decompress", "build", "traverse", "intersect"),
                   key=lambda k: stage_ms[k])
         if dom in flops_stage:
             ach = per_stage[dom]["TFLOP/s"]
-            roof = {"bound": "fp32", "kernel": "k_fused" if (fused_head and dom == "traverse") else f"k_{dom}",
+            roof = {"bound": "fp32", "kernel": fused_kernel if (fused_head and dom == "traverse") else f"k_{dom}",
                     "achieved": ach, "peak": round(fp32_peak, 2), "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4),
                     "traffic": None,
                     "peak_note": f"FP32 issue: {n_sm} SMs x 128 lanes x 2 flops x {sm_clock:.0f} MHz (no measured FP32 peak)"}

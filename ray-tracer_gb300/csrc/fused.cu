@@ -556,6 +556,12 @@ struct RaySmem {
 #ifndef RSH_RAYS_MIN_BLOCKS
 #define RSH_RAYS_MIN_BLOCKS 8
 #endif
+#ifndef RSH_TAIL_PER_WARP
+#define RSH_TAIL_PER_WARP 16
+#endif
+#ifndef RSH_TAIL_SPLIT
+#define RSH_TAIL_SPLIT 2
+#endif
 
 template <int P>
 __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(FusedArgs a) {
@@ -565,13 +571,24 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     const uint32_t units = dev_count(a.d_units, a.units_max);
     unsigned long long ntests = 0, ttests = 0;
     constexpr uint32_t R = 8 * P;
+    // the launch's tail: the last units (RSH_TAIL_PER_WARP per warp of the grid) go out in pieces of
+    // R / RSH_TAIL_SPLIT rays, so that no warp is left with a whole expensive unit after the others ran out
+    const uint32_t tail = min(units, (uint32_t)RSH_TAIL_PER_WARP * gridDim.x * FW);
+    const uint32_t head = units - tail, tickets = head + RSH_TAIL_SPLIT * tail;
     if (lane == 0) S.qn = 0;
     __syncwarp();
     for (;;) {
-        uint32_t u = 0;
-        if (lane == 0) u = atomicAdd(&a.work[0], 1u);
-        u = __shfl_sync(0xffffffffu, u, 0);
-        if (u >= units) break;
+        uint32_t t = 0;
+        if (lane == 0) t = atomicAdd(&a.work[0], 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= tickets) break;
+        uint32_t u = t, lo = 0, hi = R;
+        if (t >= head) {
+            const uint32_t h = t - head;
+            u = head + h / RSH_TAIL_SPLIT;
+            lo = (h % RSH_TAIL_SPLIT) * (R / RSH_TAIL_SPLIT);
+            hi = lo + R / RSH_TAIL_SPLIT;
+        }
         const uint32_t sidx = find_segment(a.segs, a.nseg, u);
         const FusedSeg& sg = a.segs[sidx];
         const bool any = sg.any_hit != 0;
@@ -579,7 +596,9 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
         for (uint32_t base = 0; base < R; base += 32) {
             const uint32_t i = base + lane;
             const uint32_t k = u * R + i;  // no sorted order: the rays' own order, padded past ordered_n
-            const uint32_t id = a.sorted_ids ? __ldg(a.sorted_ids + k) : (k < a.ordered_n ? k : INVALID_ID);
+            const bool mine = i >= lo && i < hi;
+            const uint32_t id = !mine ? INVALID_ID
+                                      : a.sorted_ids ? __ldg(a.sorted_ids + k) : (k < a.ordered_n ? k : INVALID_ID);
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, -1.f);
             if (id != INVALID_ID) load_ray(a.rays, id, o, d);
             const bool active = (id != INVALID_ID) && (d.w > o.w);
