@@ -45,6 +45,9 @@ __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, ui
                              uint32_t hash_drop,
                              rsh_ray* __restrict__ rays_all, bool gather, uint32_t* __restrict__ keys,
                              uint32_t* __restrict__ seg_cnt) {
+    __shared__ uint32_t s_cnt[1024];  // the block's rays per segment (nseg <= 1024)
+    for (uint32_t j = threadIdx.x; j < nseg; j += blockDim.x) s_cnt[j] = 0u;
+    __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = false;
     uint32_t lo = 0;
@@ -66,9 +69,13 @@ __global__ void k_batch_prep(const PrepSeg* __restrict__ segs, uint32_t nseg, ui
         if (sg.any_hit) sg.flags[j] = 0u;
         else sg.hits[j] = RSH_HIT_NONE;
     }
-    // rays per segment: one atomic per segment present in the warp
+    // rays per segment: one shared atomic per segment present in the warp, then one global atomic per
+    // segment present in the block (a frame's two segments would otherwise see one per warp)
     const uint32_t peers = __match_any_sync(0xffffffffu, valid ? lo : 0xFFFFFFFFu);
-    if (valid && (peers & lanemask_lt()) == 0u) atomicAdd(seg_cnt + lo, (uint32_t)__popc(peers));
+    if (valid && (peers & lanemask_lt()) == 0u) atomicAdd(s_cnt + lo, (uint32_t)__popc(peers));
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < nseg; j += blockDim.x)
+        if (s_cnt[j]) atomicAdd(seg_cnt + j, s_cnt[j]);
 }
 
 // Per-segment ranges in the sorted (segment-major) order and the padded layout, from the per-segment ray

@@ -1089,10 +1089,9 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     RSH_TRY(ensure_buf(ctx, ctx->prim_pix, 4ull * np));
     RSH_TRY(ensure_buf(ctx, ctx->surf0_pos, 16ull * npix));
     RSH_TRY(ensure_buf(ctx, ctx->surf0_nrm, 16ull * npix));
-    void *accum, *keys, *keys2;
+    void *accum, *keys;
     RSH_TRY(ensure(ctx, "accum", 16ull * npix, &accum));
     RSH_TRY(ensure(ctx, "keys", 4ull * npix * (LS ? LS : 1), &keys));
-    RSH_TRY(ensure(ctx, "keys2", 4ull * npix, &keys2));
     for (uint32_t b = 0; b < depth; ++b) {
         BounceBufs& bb = ctx->bounce[b];
         // shadow slots, then the reflection slots right behind them: the batched form traces both
@@ -1159,11 +1158,10 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
         if (fused) {
             // both batches of the bounce in one batched call: 2 segments, one persistent launch
             th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);
-            RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays,
-                                          static_cast<uint32_t*>(keys), s));
+            // no keys: the batch hashes both segments itself
+            RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays, nullptr, s));
             RSH_CUDA(launch_raygen_reflect(spos, snrm, incident, ctx->cam.eye, W, H, ctx->cfg.epsilon,
-                                           ctx->cfg.reflect_jitter, ctx->cfg.seed, b, hp_r, rrays,
-                                           static_cast<uint32_t*>(keys2), s));
+                                           ctx->cfg.reflect_jitter, ctx->cfg.seed, b, hp_r, rrays, nullptr, s));
             stage_end(ctx, th, s);
             rsh_batch_segment segs[2] = {
                 {sc, srays, npix * LS, 1, nullptr, sflags},

@@ -103,13 +103,13 @@ __global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* _
             if (ok) {
                 const v3 o = src + dir * eps;
                 store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps), make_float4(dir.x, dir.y, dir.z, tm));
-                key = ray_hash(o.x, o.y, o.z, dir.x, dir.y, dir.z, hp, v);
+                key = keys ? ray_hash(o.x, o.y, o.z, dir.x, dir.y, dir.z, hp, v) : 0u;
             }
         }
     }
     if (key == RSH_KEY_NONE)  // empty slot: an explicit no-ray (tmax < tmin) for consumers without keys
         store_ray(rays, slot, make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, -1.f));
-    keys[slot] = key;
+    if (keys) keys[slot] = key;  // no keys: the batched form hashes the rays itself
 }
 
 cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_t w, uint32_t h,
@@ -177,12 +177,12 @@ __global__ void k_raygen_reflect(const float4* __restrict__ spos, const float4* 
             const v3 o = p + r * eps;
             store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps),
                       make_float4(r.x, r.y, r.z, __int_as_float(0x7f800000)));
-            key = ray_hash(o.x, o.y, o.z, r.x, r.y, r.z, hp, 0u);
+            key = keys ? ray_hash(o.x, o.y, o.z, r.x, r.y, r.z, hp, 0u) : 0u;
         }
     }
     if (key == RSH_KEY_NONE)
         store_ray(rays, slot, make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, -1.f));
-    keys[slot] = key;
+    if (keys) keys[slot] = key;
 }
 
 cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const rsh_ray* prev,
