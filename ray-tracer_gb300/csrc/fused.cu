@@ -209,11 +209,11 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                 float tcs[8];
                 uint32_t hm = 0;
                 const float4* bb = sg.boxes + 2ull * (sg.lvl_off[cl] + first);
+                ntests += min(cnt, 8u);
 #pragma unroll
                 for (uint32_t c = 0; c < 8; ++c) {
                     tcs[c] = 0.0f;
                     if (c < cnt) {
-                        ++ntests;
                         float tc;
                         const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
                         if (box_hit(b0, b1, ox, oy, oz, ix, iy, iz, tmin, tcur, tc)) {
