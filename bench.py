@@ -632,6 +632,50 @@ def batching_bench(args):
     return out
 
 
+def sort_bench(args):
+    """The onesweep sort alone: rsh_sort_pairs on N seeded random 31-bit keys (values = index), 4 digit
+    passes; algorithmic bytes C (4 + 16 P) per the stage table. CUDA events around `steps` sorts."""
+    import ctypes as C
+
+    import rsh
+
+    lib = rsh.load()
+    ctx = rsh.Context(rsh.default_config())
+    n = int(args.sort)
+    k = np.random.default_rng(scenes_seed(1)).integers(0, 1 << 31, n, dtype=np.uint32)
+    ki, ko, vo = rsh.DeviceArray.from_numpy(k), rsh.DeviceArray(n, np.uint32), rsh.DeviceArray(n, np.uint32)
+
+    def one():
+        rsh.check(lib.rsh_sort_pairs(ctx.handle, ki.ptr, None, ko.ptr, vo.ptr, n, None, 31, None), "sort")
+
+    for _ in range(args.warmup):
+        one()
+    e0, e1 = C.c_void_p(), C.c_void_p()
+    lib.rsh_event_create(C.byref(e0))
+    lib.rsh_event_create(C.byref(e1))
+    lib.rsh_stream_synchronize(None)
+    lib.rsh_event_record(e0, None)
+    for _ in range(args.steps):
+        one()
+    lib.rsh_event_record(e1, None)
+    lib.rsh_stream_synchronize(None)
+    ms = C.c_float()
+    lib.rsh_event_elapsed(e0, e1, C.byref(ms))
+    t = ms.value / args.steps
+    alg = n * (4 + 16 * 4)
+    peaks = load_peaks()
+    ctx.destroy()
+    return {"metric": "onesweep sort GB/s (algorithmic)", "value": round(alg / t / 1e6, 1), "unit": "GB/s",
+            "ms_per_step": round(t, 4), "pairs": n, "passes": 4, "steps": args.steps, "warmup": args.warmup,
+            "frac_hbm": round(alg / t / 1e6 / peaks["hbm_gbs"], 4), "data": "synthetic (seeded random 31-bit keys)"}
+
+
+def scenes_seed(k: int) -> int:
+    from rsh import scenes
+
+    return scenes.SEED_BASE + k
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -647,6 +691,7 @@ def main():
                     help="all: plain + fused + e2e + stage timers; plain/fused: only that timed pass")
     ap.add_argument("--serving", action="store_true", help="run the serving benchmark instead")
     ap.add_argument("--batching", action="store_true", help="run the batching benchmark (256 batches, 16 scenes)")
+    ap.add_argument("--sort", type=int, default=0, help="time rsh_sort_pairs alone on this many pairs")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-max-rays", type=int, default=2_000_000)
     ap.add_argument("--serve-requests", type=int, default=48)
@@ -660,6 +705,9 @@ def main():
         return 0
     if args.batching:
         print(json.dumps(batching_bench(args)))
+        return 0
+    if args.sort:
+        print(json.dumps(sort_bench(args)))
         return 0
     rank, world, td = dist_setup(args.gpus)
     s = make_workload(args.config)
