@@ -548,11 +548,12 @@ def batching_bench(args):
     st = C.c_void_p()
     rsh.check(lib.rsh_stream_create(C.byref(st)), "stream")
     # per-scene autotuner over origin-grid bits 4..10, direction bins 16..4096 (dir_log2 2..6), switch levels
-    # 3..7 and 15 (rays alone from the root) and packet sizes 8/16/32 (coordinate descent; points whose hash
-    # exceeds 31 bits are skipped)
+    # 3..7 and 15 (rays alone from the root), packet sizes 8/16/32 and 4/6/8 CTAs per SM of the traversal
+    # launch (coordinate descent; points whose hash exceeds the key's room are skipped)
     t0 = time.perf_counter()
     tuned_ms, untuned_ms = ctx.autotune_scenes(segs, len(sizes), grid_bits=range(4, 11), dir_log2=range(2, 7),
-                                               ray_levels=(3, 4, 5, 6, 7, 15), packet_sizes=(8, 16, 32), stream=st)
+                                               ray_levels=(3, 4, 5, 6, 7, 15), packet_sizes=(8, 16, 32), stream=st,
+                                               fused_blocks=(4, 6, 8))
     tune_s = time.perf_counter() - t0
     best = ctx.config
     scene_tuning = [sc.tuning() for sc in scs]
@@ -618,7 +619,8 @@ def batching_bench(args):
            "unit": "Mrays/s", "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3),
            "rays_per_step": int(total), "batches": int(len(sizes)), "scenes": len(sd),
            "scenes_tris": [int(s.tri_count) for s in sd],
-           "autotuned": {"packet_size": best.packet_size, "per_scene": scene_tuning, "tuning_s": round(tune_s, 2),
+           "autotuned": {"packet_size": best.packet_size, "fused_blocks_per_sm": best.fused_blocks,
+                         "per_scene": scene_tuning, "tuning_s": round(tune_s, 2),
                          "batch_ms_untuned": round(untuned_ms, 3), "batch_ms_tuned": round(tuned_ms, 3),
                          "context_defaults": {"grid_bits": best.grid_bits, "dir_log2": best.dir_log2,
                                               "ray_level": best.ray_level}},

@@ -147,6 +147,8 @@ typedef struct rsh_config {
                                   from the root, no packet phase, no ray hierarchy; default 15) */
     uint32_t plain_ray_level;  /* plain per-frame path: object-tree level at and below which the traversal
                                   emits per-ray candidates (0: packet candidates only; default 4) */
+    uint32_t fused_blocks;     /* batched form: CTAs of the persistent traversal launch per SM (0: as many
+                                  as fit, the default; fewer share each SM's L1 among fewer rays) */
 } rsh_config;
 
 #define RSH_FLAG_STAGE_TIMERS 1u   /* record per-stage CUDA events (TestManager timers) */
@@ -501,13 +503,14 @@ typedef struct rsh_tune_space {
     const uint32_t* ray_levels;   uint32_t n_ray_level;
     const uint32_t* packet_sizes; uint32_t n_packet;
     uint32_t reps;                /* timed repetitions per point after one warm-up (0: 2) */
+    const uint32_t* fused_blocks; uint32_t n_fused_blocks;  /* CTAs per SM of the traversal launch */
 } rsh_tune_space;
 /* Per-scene autotuner: coordinate descent over the space. The packet size (shared by every segment of a
  * batch) is chosen on the whole batch; then, for each distinct scene, grid bits, direction bins and the
  * switch level are chosen on that scene's segments alone, one parameter at a time, and stored in the
  * scene (rsh_scene_set_tuning); then every scene at switch level 15 at once is tried against that (the
  * rays-only kernel, which skips the ray hierarchy, runs only when no segment uses packets below the root);
- * last, the packet size is chosen again with the scenes tuned. The search keeps the untuned configuration
+ * last, the packet size and the traversal launch's CTAs per SM are chosen with the scenes tuned. The search keeps the untuned configuration
  * when its result is not faster on the whole batch. Points whose hash does not fit beside the batch's
  * segment tag in 31 bits are skipped. *best_ms (optional) is the whole batch's time with the final
  * choice, *untuned_ms (optional) its time with the context's configuration and no scene tuning. */

@@ -381,6 +381,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     fa.d_units = totals + 1;
     fa.work = static_cast<uint32_t*>(pl.work);
     fa.rays_only = pl.rays_only;
+    fa.blocks_per_sm = ctx->cfg.fused_blocks;
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;
@@ -431,6 +432,7 @@ rsh_status batch_trace_ordered(rsh_ctx* ctx, const rsh_batch_segment& seg, cudaS
     fa.d_units = nullptr;
     fa.work = static_cast<uint32_t*>(pl.work);
     fa.rays_only = 1;
+    fa.blocks_per_sm = ctx->cfg.fused_blocks;
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;
@@ -683,6 +685,25 @@ float tune_packet(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count, c
     rsh_set_config(ctx, &best);
     return cur_ms;
 }
+
+// CTAs per SM of the traversal launch on the whole batch, like the packet size.
+float tune_blocks(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count, const rsh_tune_space& sp,
+                  uint32_t reps, cudaStream_t stream, float cur_ms) {
+    const rsh_config base = ctx->cfg;
+    rsh_config best = base;
+    for (uint32_t i = 0; i < sp.n_fused_blocks; ++i) {
+        rsh_config c = base;
+        c.fused_blocks = sp.fused_blocks[i];
+        if (c.fused_blocks == base.fused_blocks || rsh_set_config(ctx, &c) != RSH_OK) continue;
+        float ms;
+        if (time_batch(ctx, segs, count, reps, stream, &ms) == RSH_OK && ms < cur_ms) {
+            cur_ms = ms;
+            best = c;
+        }
+    }
+    rsh_set_config(ctx, &best);
+    return cur_ms;
+}
 }  // namespace
 
 extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t count,
@@ -690,7 +711,8 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
                                           float* untuned_ms) {
     if (!ctx || !space || !segs || !count) return RSH_ERR_INVALID;
     if ((space->n_grid && !space->grid_bits) || (space->n_dir && !space->dir_log2) ||
-        (space->n_ray_level && !space->ray_levels) || (space->n_packet && !space->packet_sizes))
+        (space->n_ray_level && !space->ray_levels) || (space->n_packet && !space->packet_sizes) ||
+        (space->n_fused_blocks && !space->fused_blocks))
         return RSH_ERR_INVALID;
     const uint32_t reps = space->reps ? space->reps : 2u;
     // hash widths that fit beside this batch's segment tag without dropping bits: wider points would be
@@ -758,6 +780,7 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
         }
     }
     ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
+    ms = tune_blocks(ctx, segs, count, *space, reps, stream, ms);
     // keep the untuned configuration when the search found nothing faster on the whole batch (the
     // per-scene steps time sub-batches, which need not add up)
     if (!(ms < untuned)) {

@@ -294,7 +294,7 @@ static rsh_status validate_config(const rsh_config* c) {
     if (c->packet_size != 8 && c->packet_size != 16 && c->packet_size != 32) return RSH_ERR_INVALID;
     if (c->cluster_size < 1 || c->cluster_size > 64) return RSH_ERR_INVALID;
     if (!(c->epsilon >= 0.0f)) return RSH_ERR_INVALID;
-    if (c->ray_level > 15 || c->plain_ray_level > 15) return RSH_ERR_INVALID;
+    if (c->ray_level > 15 || c->plain_ray_level > 15 || c->fused_blocks > 64) return RSH_ERR_INVALID;
     return RSH_OK;
 }
 

@@ -658,6 +658,7 @@ static cudaError_t launch_fused_rays_p(const FusedArgs& a, cudaStream_t s) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays<P>, FW * 32, smem);
     if (per_sm < 1) per_sm = 1;
+    if (a.blocks_per_sm && (int)a.blocks_per_sm < per_sm) per_sm = (int)a.blocks_per_sm;
     uint32_t grid = (uint32_t)(sms * per_sm);
     const uint32_t need = (a.units_max + FW - 1) / FW;
     if (need < grid) grid = need > 0 ? need : 1;
@@ -677,6 +678,7 @@ static cudaError_t launch_fused_p(const FusedArgs& a, cudaStream_t s) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused<P>, FW * 32, smem);
     if (per_sm < 1) per_sm = 1;
+    if (a.blocks_per_sm && (int)a.blocks_per_sm < per_sm) per_sm = (int)a.blocks_per_sm;
     uint32_t grid = (uint32_t)(sms * per_sm);
     const uint32_t need = (a.units_max + FW - 1) / FW;
     if (need < grid) grid = need > 0 ? need : 1;

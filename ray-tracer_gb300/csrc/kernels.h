@@ -203,6 +203,7 @@ struct FusedArgs {
     const uint32_t* d_units;       // device count of units
     uint32_t* work;
     uint32_t rays_only;            // every segment's switch level >= its tree depth: no packet phase
+    uint32_t blocks_per_sm;        // CTAs per SM of the launch (0: as many as fit)
     unsigned long long* node_tests;
     unsigned long long* tri_tests;
     uint32_t* err;

@@ -46,7 +46,8 @@ class Config(C.Structure):
     _fields_ = [("grid_bits", C.c_uint32), ("dir_log2", C.c_uint32), ("packet_size", C.c_uint32),
                 ("cluster_size", C.c_uint32), ("epsilon", C.c_float), ("hbm_budget", C.c_uint64),
                 ("candidate_capacity", C.c_uint64), ("flags", C.c_uint32), ("reflect_jitter", C.c_float),
-                ("seed", C.c_uint32), ("ray_level", C.c_uint32), ("plain_ray_level", C.c_uint32)]
+                ("seed", C.c_uint32), ("ray_level", C.c_uint32), ("plain_ray_level", C.c_uint32),
+                ("fused_blocks", C.c_uint32)]
 
 
 class HashParams(C.Structure):
@@ -108,7 +109,8 @@ class SceneTuning(C.Structure):
 class TuneSpace(C.Structure):
     _fields_ = [("grid_bits", C.c_void_p), ("n_grid", C.c_uint32), ("dir_log2", C.c_void_p), ("n_dir", C.c_uint32),
                 ("ray_levels", C.c_void_p), ("n_ray_level", C.c_uint32), ("packet_sizes", C.c_void_p),
-                ("n_packet", C.c_uint32), ("reps", C.c_uint32)]
+                ("n_packet", C.c_uint32), ("reps", C.c_uint32), ("fused_blocks", C.c_void_p),
+                ("n_fused_blocks", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -472,13 +474,16 @@ class Context:
         check(lib().rsh_set_config(self.handle, C.byref(self.config)), "rsh_set_config")
 
     def autotune_scenes(self, segments, count: int, grid_bits=(), dir_log2=(), ray_levels=(), packet_sizes=(),
-                        reps: int = 2, stream=None) -> tuple:
+                        reps: int = 2, stream=None, fused_blocks=()) -> tuple:
         """rsh_autotune_scenes over a BatchSegment array; returns (tuned ms, untuned ms) of the whole batch.
-        The chosen packet size lands in this context, the rest in each scene (Scene.tuning())."""
-        lists = [(C.c_uint32 * max(1, len(v)))(*v) for v in (grid_bits, dir_log2, ray_levels, packet_sizes)]
+        The chosen packet size and CTAs per SM land in this context, the rest in each scene (Scene.tuning())."""
+        grid_bits, dir_log2, ray_levels = list(grid_bits), list(dir_log2), list(ray_levels)
+        packet_sizes, fused_blocks = list(packet_sizes), list(fused_blocks)
+        lists = [(C.c_uint32 * max(1, len(v)))(*v)
+                 for v in (grid_bits, dir_log2, ray_levels, packet_sizes, fused_blocks)]
         sp = TuneSpace(C.cast(lists[0], C.c_void_p), len(grid_bits), C.cast(lists[1], C.c_void_p), len(dir_log2),
                        C.cast(lists[2], C.c_void_p), len(ray_levels), C.cast(lists[3], C.c_void_p),
-                       len(packet_sizes), reps)
+                       len(packet_sizes), reps, C.cast(lists[4], C.c_void_p), len(fused_blocks))
         best, untuned = C.c_float(), C.c_float()
         check(lib().rsh_autotune_scenes(self.handle, segments, count, C.byref(sp), stream, C.byref(best),
                                         C.byref(untuned)), "rsh_autotune_scenes")

@@ -23,7 +23,9 @@ def ctx():
 @pytest.mark.parametrize("P", [8, 16, 32])
 @pytest.mark.parametrize("any_hit", [False, True])
 def test_fused_vs_brute(P, any_hit, ray_level):
-    c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=P, cluster_size=8, ray_level=ray_level)
+    # fewer CTAs per SM than fit (1 and 3) for some points: the persistent launches cover every unit anyway
+    c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=P, cluster_size=8, ray_level=ray_level,
+                    fused_blocks={8: 0, 16: 1, 32: 3}[P])
     s = scenes.random_soup(40_000, np.random.default_rng(P))
     sc = c.scene(s.positions, s.normals, s.material_ids, s.materials)
     rng = np.random.default_rng(100 + P)
@@ -213,9 +215,9 @@ def test_autotune_scenes_per_scene_choice():
     segs, keep = _segments(ctx, sd, scs, [20_000, 30_000, 50_000, 20_000, 4_000, 9_000], which, anyh,
                            np.random.default_rng(51))
     best_ms, untuned_ms = ctx.autotune_scenes(segs, len(which), grid_bits=(4, 6), dir_log2=(3, 5),
-                                              ray_levels=(2, 4), packet_sizes=(8, 16))
+                                              ray_levels=(2, 4), packet_sizes=(8, 16), fused_blocks=(2, 4))
     assert best_ms > 0 and untuned_ms > 0
-    assert ctx.config.packet_size in (8, 16)
+    assert ctx.config.packet_size in (8, 16) and ctx.config.fused_blocks in (0, 2, 4)
     for sc in scs:
         t = sc.tuning()
         # a tuned value is one of the swept points or the context's own (where the descent started), or the
