@@ -123,6 +123,7 @@ struct BatchPlan {
     uint32_t nseg = 0, total = 0, tag_shift = 0, key_bits = 0, P = 8, unit_rays = 64, max_padded = 0, hash_drop = 0;
     uint32_t rays_only = 1;  // cleared by any segment whose rays use packets below the root
     bool contiguous = false; // the segments' rays lie back to back in one array: no gather
+    bool gather = false;     // copy every segment's rays into one array (packet kernel, not contiguous)
     void *rays_all, *keys, *trimmed, *ckeys, *cbases, *counts, *skeys, *svals, *sorted_keys, *sorted_ids, *scr;
     void *padded, *nodes, *prep, *fsegs, *seg_begin, *seg_cnt, *pstart, *totals, *work, *sched, *seg_delta;
     std::vector<PrepSeg> h_prep;
@@ -179,8 +180,14 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     pl.contiguous = count > 0;
     for (uint32_t s = 0, at = 0; s < count; at += segs[s].n, ++s)
         if (segs[s].n && segs[s].rays != segs[0].rays + at) pl.contiguous = false;
+    for (uint32_t s = 0; s < count; ++s)
+        if (tuned_config(ctx->cfg, segs[s].scene).ray_level < segs[s].scene->h.levels) pl.rays_only = 0;
+    // one ray array for the ray hierarchy and the packet kernel: the segments' own when they lie back to
+    // back, else a gathered copy; the rays-only kernel reads every segment's rays in place
+    pl.gather = !pl.contiguous && !pl.rays_only;
     if (pl.contiguous) pl.rays_all = const_cast<rsh_ray*>(segs[0].rays);
-    else RSH_TRY(ensure(ctx, "b_rays", sizeof(rsh_ray) * (size_t)n, &pl.rays_all));
+    else if (pl.gather) RSH_TRY(ensure(ctx, "b_rays", sizeof(rsh_ray) * (size_t)n, &pl.rays_all));
+    else pl.rays_all = nullptr;
     RSH_TRY(ensure(ctx, "b_keys", 4ull * n, &pl.keys));
     RSH_TRY(ensure(ctx, "trimmed", 4ull * n, &pl.trimmed));
     RSH_TRY(ensure(ctx, "ckeys", 4ull * n + 4, &pl.ckeys));
@@ -241,7 +248,7 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         }
         f.any_hit = p.any_hit;
         f.ray_level = tc.ray_level;
-        if (tc.ray_level < sc->h.levels) pl.rays_only = 0;
+        f.rays = g.rays;
         f.flags = g.flags;
         f.hits = reinterpret_cast<unsigned long long*>(g.hits);
         f.slot_base = start;
@@ -331,7 +338,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     RSH_CUDA(cudaMemsetAsync(pl.seg_cnt, 0, 4ull * pl.nseg, s));
     k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
                                                        pl.tag_shift, pl.hash_drop, static_cast<rsh_ray*>(pl.rays_all),
-                                                       !pl.contiguous,
+                                                       pl.gather,
                                                        static_cast<uint32_t*>(pl.keys), static_cast<uint32_t*>(pl.seg_cnt));
     note_launch();
     RSH_CUDA(cudaGetLastError());

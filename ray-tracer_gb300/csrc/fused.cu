@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
             const uint32_t id = !mine ? INVALID_ID
                                       : a.sorted_ids ? __ldg(a.sorted_ids + k) : (k < a.ordered_n ? k : INVALID_ID);
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, -1.f);
-            if (id != INVALID_ID) load_ray(a.rays, id, o, d);
+            if (id != INVALID_ID) load_ray(sg.rays, id - sg.slot_base, o, d);
             const bool active = (id != INVALID_ID) && (d.w > o.w);
             const RayWT w = wt_setup(o, d);
             S.ro[i] = o;

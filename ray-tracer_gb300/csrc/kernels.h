@@ -185,6 +185,7 @@ struct FusedSeg {
     uint32_t unit_begin;           // first work unit (level-1 node) of this segment
     uint32_t any_hit;
     uint32_t ray_level;            // object-tree level at and below which rays descend individually
+    const rsh_ray* rays;           // the segment's own rays (slot - slot_base); read in place by the rays-only kernel
     uint32_t* flags;               // indexed by slot - slot_base
     unsigned long long* hits;
     uint32_t slot_base;

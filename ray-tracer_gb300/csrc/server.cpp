@@ -49,7 +49,6 @@ struct Req {
     float4* snrm = nullptr;
     rsh_ray* srays = nullptr;
     rsh_ray* rrays[2] = {nullptr, nullptr};
-    uint32_t* keys = nullptr;
     unsigned long long* hits = nullptr;  // depth x npix
     uint32_t* flags = nullptr;           // depth x npix x L
 };
@@ -58,7 +57,7 @@ size_t request_bytes(const rsh_request& r) {
     const size_t npix = (size_t)r.width * r.height;
     const size_t np = (size_t)((r.width + 7) / 8) * ((r.height + 7) / 8) * 64;
     const size_t L = r.light_count;
-    size_t b = np * (32 + 4 + 8) + npix * (16 + 16 + 32 * L + 64 + 4 * std::max<size_t>(L, 1)) +
+    size_t b = np * (32 + 4 + 8) + npix * (16 + 16 + 32 * L + 64) +
                npix * 8 * r.depth + npix * L * 4 * r.depth;
     return (b + 4095) & ~size_t(4095);
 }
@@ -106,7 +105,6 @@ rsh_status alloc_request(Req* q) {
     q->srays = reinterpret_cast<rsh_ray*>(take(npix * L * 32));
     q->rrays[0] = reinterpret_cast<rsh_ray*>(take(npix * 32));
     q->rrays[1] = reinterpret_cast<rsh_ray*>(take(npix * 32));
-    q->keys = reinterpret_cast<uint32_t*>(take(npix * std::max<size_t>(L, 1) * 4));
     q->hits = reinterpret_cast<unsigned long long*>(take(npix * 8 * r.depth));
     q->flags = reinterpret_cast<uint32_t*>(take(npix * L * 4 * r.depth));
     return RSH_OK;
@@ -152,11 +150,11 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
             lp.samples = 1;
             for (uint32_t l = 0; l < L; ++l)
                 for (int i = 0; i < 3; ++i) lp.pos[l][i] = r.lights[l].position[i];
-            RSH_CUDA(launch_raygen_shadow(q->spos, q->snrm, W, H, lp, s->ctx->cfg.epsilon, hp_s, q->srays, q->keys, st));
+            RSH_CUDA(launch_raygen_shadow(q->spos, q->snrm, W, H, lp, s->ctx->cfg.epsilon, hp_s, q->srays, nullptr, st));
             const rsh_ray* prev = (b == 0) ? nullptr : q->rrays[(b - 1) & 1];
             rsh_ray* cur = q->rrays[b & 1];
             RSH_CUDA(launch_raygen_reflect(q->spos, q->snrm, prev, r.camera.eye, W, H, s->ctx->cfg.epsilon,
-                                           s->ctx->cfg.reflect_jitter, s->ctx->cfg.seed, b, hp_r, cur, q->keys, st));
+                                           s->ctx->cfg.reflect_jitter, s->ctx->cfg.seed, b, hp_r, cur, nullptr, st));
             segs.push_back(rsh_batch_segment{sc, q->srays, npix * L, 1, nullptr, q->flags + (size_t)b * npix * L});
             segs.push_back(rsh_batch_segment{sc, cur, npix, 0,
                                              reinterpret_cast<uint64_t*>(q->hits + (size_t)b * npix), nullptr});
