@@ -4,9 +4,11 @@
 // request queue. Here a host thread runs steps: every step (1) admits queued requests while their
 // device memory fits the server's HBM budget, (2) generates the current stage's rays of every in-flight
 // request (primary rays, or one bounce's shadow + reflection rays), (3) traces all of them in ONE
-// batched call (segmented hash/compress/sort/decompress, hierarchy build, one persistent fused
-// traversal + intersection launch), (4) resolves hits and advances each request; finished requests
-// leave and new ones join between steps. Ray state and results stay on the device until rsh_server_wait
+// batched call (segmented hash/compress/sort/decompress, one persistent fused traversal + intersection
+// launch), (4) resolves hits and advances each request; finished requests leave and new ones join
+// between steps. Steps are enqueued without waiting for the GPU (at most two outstanding): the host
+// admits and prepares the next step while the current one runs, and retires steps in order as their
+// events complete. Ray state and results stay on the device until rsh_server_wait
 // copies them out. A request's results do not depend on what else is in the batch: its rays form their
 // own key segment, sort stably within it, and pack into work units of their own.
 #include <algorithm>
@@ -38,7 +40,9 @@ struct Req {
     double submit_ms = 0, start_ms = 0, finish_ms = 0;
     uint64_t rays = 0;
     bool done = false, cancelled = false, collected = false;
-    uint32_t stage = 0;  // 0 = primary; 1 + b = bounce b
+    uint32_t stage = 0;  // next stage to enqueue: 0 = primary; 1 + b = bounce b
+    uint32_t pending = 0;     // enqueued steps not yet retired
+    uint32_t stage_done = 0;  // stages whose step has retired
     size_t bytes = 0;
     // device buffers
     void* buf = nullptr;
@@ -80,6 +84,16 @@ struct rsh_server {
     bool stop = false;
     uint64_t completed = 0, steps = 0, peak_inflight = 0, bytes_in_use = 0, peak_bytes = 0;
     rsh_status fatal = RSH_OK;
+    // steps enqueued on the stream and not yet retired (oldest first); each owns a pinned readback slot
+    struct Step {
+        cudaEvent_t done = nullptr;
+        std::vector<Req*> act;       // requests with a stage in this step
+        std::vector<size_t> seg_at;  // their first segment
+        uint32_t* pinned = nullptr;  // segment counts, then the device error word
+        size_t cap = 0;
+    };
+    std::deque<Step> steps_q;
+    std::vector<Step> free_steps;  // retired records (event and pinned slot kept for reuse)
 };
 
 namespace {
@@ -118,15 +132,23 @@ void free_request(rsh_server* s, Req* q) {
     }
 }
 
-// one step of the loop (server thread, no lock held while the GPU works)
-rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
+// One step, enqueued without waiting (server thread, no lock held): generate the current stage's rays of
+// every request in `act`, trace them all in one batched call, resolve the hits into the next surfaces,
+// copy the segment counts and the device error word to the step's pinned slot and record its event.
+// The host goes on admitting and enqueueing the next step while this one runs (at most kDepth steps are
+// outstanding); steps retire in order when their events complete.
+constexpr size_t kDepth = 2;
+
+rsh_status enqueue_step(rsh_server* s, rsh_server::Step& rec) {
     cudaStream_t st = s->stream;
     std::vector<rsh_batch_segment> segs;
-    segs.reserve(act.size() * 2);
-    for (Req* q : act) {
+    segs.reserve(rec.act.size() * 2);
+    rec.seg_at.clear();
+    for (Req* q : rec.act) {
         const rsh_request& r = q->r;
         const rsh_scene* sc = s->scenes[r.scene_index];
         const uint32_t W = r.width, H = r.height, npix = W * H, L = r.light_count;
+        rec.seg_at.push_back(segs.size());
         if (q->stage == 0) {
             CameraP cp;
             for (int i = 0; i < 3; ++i) {
@@ -141,16 +163,15 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
                                              nullptr});
         } else {
             const uint32_t b = q->stage - 1;
-            // the batched call re-keys every segment itself, so the ray generators' keys are not used
+            // the batched call keys every segment itself: the ray generators write no keys
             HashP hp_r;
             RSH_TRY(make_hash_params(sc, s->ctx->cfg, 0, hp_r));
-            const HashP& hp_s = hp_r;
             LightsP lp{};
             lp.count = L;
             lp.samples = 1;
             for (uint32_t l = 0; l < L; ++l)
                 for (int i = 0; i < 3; ++i) lp.pos[l][i] = r.lights[l].position[i];
-            RSH_CUDA(launch_raygen_shadow(q->spos, q->snrm, W, H, lp, s->ctx->cfg.epsilon, hp_s, q->srays, nullptr, st));
+            RSH_CUDA(launch_raygen_shadow(q->spos, q->snrm, W, H, lp, s->ctx->cfg.epsilon, hp_r, q->srays, nullptr, st));
             const rsh_ray* prev = (b == 0) ? nullptr : q->rrays[(b - 1) & 1];
             rsh_ray* cur = q->rrays[b & 1];
             RSH_CUDA(launch_raygen_reflect(q->spos, q->snrm, prev, r.camera.eye, W, H, s->ctx->cfg.epsilon,
@@ -161,12 +182,17 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
         }
     }
     RSH_TRY(rsh_batch_trace(s->ctx, segs.data(), (uint32_t)segs.size(), st));
-    // rays traced per segment (after trimming), read back with the step's synchronisation below
-    std::vector<uint32_t> seg_cnt(segs.size());
-    RSH_CUDA(cudaMemcpyAsync(seg_cnt.data(), s->ctx->bufs["b_seg_cnt"].ptr, 4 * segs.size(), cudaMemcpyDeviceToHost,
+    if (rec.cap < segs.size() + 1) {
+        if (rec.pinned) cudaFreeHost(rec.pinned);
+        rec.pinned = nullptr;
+        rec.cap = std::max<size_t>(segs.size() + 1, 256);
+        RSH_CUDA(cudaMallocHost(&rec.pinned, 4 * rec.cap));
+    }
+    // rays traced per segment (after trimming): read when the step retires
+    RSH_CUDA(cudaMemcpyAsync(rec.pinned, s->ctx->bufs["b_seg_cnt"].ptr, 4 * segs.size(), cudaMemcpyDeviceToHost,
                              st));
     // advance: resolve hits into the next surface
-    for (Req* q : act) {
+    for (Req* q : rec.act) {
         const rsh_request& r = q->r;
         const rsh_scene* sc = s->scenes[r.scene_index];
         const uint32_t W = r.width, H = r.height, npix = W * H;
@@ -180,99 +206,160 @@ rsh_status run_step(rsh_server* s, std::vector<Req*>& act) {
                                     npix, q->spos, q->snrm, st));
         }
     }
-    RSH_CUDA(cudaStreamSynchronize(st));
-    size_t si = 0;
-    for (Req* q : act) {
-        if (q->stage == 0) {
-            si += 1;  // primary rays are not counted as secondary rays
-        } else {
-            q->rays += (uint64_t)seg_cnt[si] + seg_cnt[si + 1];
-            si += 2;
+    // the device error word after this step (read, then cleared, in stream order)
+    RSH_CUDA(cudaMemcpyAsync(rec.pinned + segs.size(), s->ctx->d_err, 4, cudaMemcpyDeviceToHost, st));
+    RSH_CUDA(cudaMemsetAsync(s->ctx->d_err, 0, 4, st));
+    if (!rec.done) RSH_CUDA(cudaEventCreateWithFlags(&rec.done, cudaEventDisableTiming));
+    RSH_CUDA(cudaEventRecord(rec.done, st));
+    return RSH_OK;
+}
+
+// Retires the oldest outstanding step once its event completed (waiting for it when `block`): adds each
+// request's traced rays, finishes the requests whose last stage it was. Caller holds the lock; the wait
+// itself runs unlocked. Returns false when nothing was retired.
+bool retire_oldest(rsh_server* s, std::unique_lock<std::mutex>& lk, bool block) {
+    if (s->steps_q.empty()) return false;
+    rsh_server::Step& rec = s->steps_q.front();
+    if (block) {
+        lk.unlock();
+        const cudaError_t e = cudaEventSynchronize(rec.done);
+        lk.lock();
+        if (e != cudaSuccess && s->fatal == RSH_OK) s->fatal = RSH_ERR_CUDA;
+    } else if (cudaEventQuery(rec.done) == cudaErrorNotReady) {
+        return false;
+    }
+    // the step's segments: each request's primary stage has one, a bounce two (steps retire in order, so a
+    // request's stage in this step is its count of retired stages)
+    size_t total_segs = 0;
+    for (size_t k = 0; k < rec.act.size(); ++k) total_segs = rec.seg_at[k] + (rec.act[k]->stage_done == 0 ? 1 : 2);
+    const uint32_t derr = rec.act.empty() ? 0u : rec.pinned[total_segs];
+    for (size_t k = 0; k < rec.act.size(); ++k) {
+        Req* q = rec.act[k];
+        if (q->stage_done > 0) q->rays += (uint64_t)rec.pinned[rec.seg_at[k]] + rec.pinned[rec.seg_at[k] + 1];
+        if (derr && q->status == RSH_OK) q->status = (derr & RSH_DEVERR_TIMEOUT) ? RSH_ERR_TIMEOUT : RSH_ERR_OVERFLOW;
+        q->stage_done += 1;
+        q->pending -= 1;
+        if (q->pending == 0 && (q->stage_done > q->r.depth || q->cancelled || q->status != RSH_OK)) {
+            q->done = true;
+            q->finish_ms = now_ms();
+            if (q->status == RSH_OK && q->cancelled) q->status = RSH_ERR_INVALID;
+            if (q->status == RSH_OK) ++s->completed;
+            s->inflight.erase(std::find(s->inflight.begin(), s->inflight.end(), q));
         }
     }
-    return rsh_check_device_errors(s->ctx, st);
+    if (derr && s->fatal == RSH_OK) s->fatal = (derr & RSH_DEVERR_TIMEOUT) ? RSH_ERR_TIMEOUT : RSH_ERR_OVERFLOW;
+    rec.act.clear();
+    s->free_steps.push_back(std::move(rec));
+    s->steps_q.pop_front();
+    s->cv_done.notify_all();
+    return true;
 }
 
 void server_main(rsh_server* s) {
     cudaSetDevice(s->ctx->device);
+    std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
-        std::vector<Req*> act;
-        {
-            std::unique_lock<std::mutex> lk(s->mu);
-            // admission by HBM budget
-            while (!s->queue.empty() && s->inflight.size() < s->max_inflight) {
-                Req* q = s->queue.front();
-                if (q->cancelled) {
-                    s->queue.pop_front();
-                    q->done = true;
-                    q->status = RSH_ERR_INVALID;
-                    q->finish_ms = now_ms();
-                    s->cv_done.notify_all();
-                    continue;
-                }
-                if (s->bytes_in_use + q->bytes > s->budget && !s->inflight.empty()) break;
-                if (q->bytes > s->budget) {  // can never fit
-                    s->queue.pop_front();
-                    q->done = true;
-                    q->status = RSH_ERR_OOM;
-                    q->finish_ms = now_ms();
-                    s->cv_done.notify_all();
-                    continue;
-                }
+        // retire what has finished, without waiting
+        while (retire_oldest(s, lk, false)) {
+        }
+        // admission by HBM budget
+        while (!s->queue.empty() && s->inflight.size() < s->max_inflight) {
+            Req* q = s->queue.front();
+            if (q->cancelled) {
                 s->queue.pop_front();
-                s->bytes_in_use += q->bytes;
-                if (alloc_request(q) != RSH_OK) {
-                    s->bytes_in_use -= q->bytes;
-                    q->done = true;
-                    q->status = RSH_ERR_OOM;
-                    q->finish_ms = now_ms();
-                    s->cv_done.notify_all();
-                    continue;
-                }
-                q->start_ms = now_ms();
-                s->inflight.push_back(q);
-            }
-            s->peak_inflight = std::max<uint64_t>(s->peak_inflight, s->inflight.size());
-            s->peak_bytes = std::max(s->peak_bytes, s->bytes_in_use);
-            // drop cancelled in-flight requests between steps
-            for (auto it = s->inflight.begin(); it != s->inflight.end();) {
-                if ((*it)->cancelled) {
-                    free_request(s, *it);
-                    (*it)->done = true;
-                    (*it)->status = RSH_ERR_INVALID;
-                    (*it)->finish_ms = now_ms();
-                    it = s->inflight.erase(it);
-                    s->cv_done.notify_all();
-                } else {
-                    ++it;
-                }
-            }
-            if (s->inflight.empty()) {
-                if (s->stop) return;
-                s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+                q->done = true;
+                q->status = RSH_ERR_INVALID;
+                q->finish_ms = now_ms();
+                s->cv_done.notify_all();
                 continue;
             }
-            act = s->inflight;
-        }
-        rsh_status st = run_step(s, act);
-        std::lock_guard<std::mutex> lk(s->mu);
-        ++s->steps;
-        for (Req* q : act) {
-            if (st != RSH_OK) {
-                q->status = st;
-                q->stage = q->r.depth + 1;
-            } else {
-                q->stage += 1;
-            }
-            if (q->stage > q->r.depth) {
+            if (s->bytes_in_use + q->bytes > s->budget && !s->inflight.empty()) break;
+            if (q->bytes > s->budget) {  // can never fit
+                s->queue.pop_front();
                 q->done = true;
+                q->status = RSH_ERR_OOM;
                 q->finish_ms = now_ms();
-                ++s->completed;
-                s->inflight.erase(std::find(s->inflight.begin(), s->inflight.end(), q));
+                s->cv_done.notify_all();
+                continue;
+            }
+            s->queue.pop_front();
+            s->bytes_in_use += q->bytes;
+            if (alloc_request(q) != RSH_OK) {
+                s->bytes_in_use -= q->bytes;
+                q->done = true;
+                q->status = RSH_ERR_OOM;
+                q->finish_ms = now_ms();
+                s->cv_done.notify_all();
+                continue;
+            }
+            q->start_ms = now_ms();
+            s->inflight.push_back(q);
+        }
+        s->peak_inflight = std::max<uint64_t>(s->peak_inflight, s->inflight.size());
+        s->peak_bytes = std::max(s->peak_bytes, s->bytes_in_use);
+        // cancelled in-flight requests with no step outstanding leave now; the others take no new stage
+        for (auto it = s->inflight.begin(); it != s->inflight.end();) {
+            Req* q = *it;
+            if (q->cancelled && q->pending == 0) {
+                free_request(s, q);
+                q->done = true;
+                q->status = RSH_ERR_INVALID;
+                q->finish_ms = now_ms();
+                it = s->inflight.erase(it);
+                s->cv_done.notify_all();
+            } else {
+                ++it;
             }
         }
-        if (st != RSH_OK) s->fatal = st;
-        s->cv_done.notify_all();
+        // the requests with a stage left to enqueue
+        std::vector<Req*> act;
+        for (Req* q : s->inflight)
+            if (!q->cancelled && q->status == RSH_OK && q->stage <= q->r.depth) act.push_back(q);
+        if (act.empty() || s->steps_q.size() >= kDepth) {
+            if (!s->steps_q.empty()) {  // the GPU is busy: wait for its oldest step
+                retire_oldest(s, lk, true);
+                continue;
+            }
+            if (s->stop && s->queue.empty()) return;
+            s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+            if (s->stop && s->queue.empty() && s->inflight.empty()) return;
+            continue;
+        }
+        rsh_server::Step rec;
+        if (!s->free_steps.empty()) {
+            rec = std::move(s->free_steps.back());
+            s->free_steps.pop_back();
+        }
+        rec.act = act;
+        for (Req* q : act) q->pending += 1;
+        lk.unlock();
+        const rsh_status st = enqueue_step(s, rec);
+        lk.lock();
+        ++s->steps;
+        if (st != RSH_OK) {
+            // nothing of this step reached the GPU in a usable state: fail its requests once idle
+            for (Req* q : act) {
+                q->status = st;
+                q->pending -= 1;
+            }
+            if (s->fatal == RSH_OK) s->fatal = st;
+            lk.unlock();
+            cudaStreamSynchronize(s->stream);
+            lk.lock();
+            for (Req* q : act) {
+                if (q->pending == 0 && !q->done) {
+                    q->done = true;
+                    q->finish_ms = now_ms();
+                    s->inflight.erase(std::find(s->inflight.begin(), s->inflight.end(), q));
+                }
+            }
+            rec.act.clear();
+            s->free_steps.push_back(std::move(rec));
+            s->cv_done.notify_all();
+            continue;
+        }
+        for (Req* q : act) q->stage += 1;
+        s->steps_q.push_back(std::move(rec));
     }
 }
 
@@ -385,6 +472,17 @@ rsh_status rsh_server_destroy(rsh_server* s) {
     for (auto& kv : s->all) {
         free_request(s, kv.second);
         delete kv.second;
+    }
+    cudaStreamSynchronize(s->stream);
+    for (auto* list : {&s->free_steps}) {
+        for (auto& rec : *list) {
+            if (rec.done) cudaEventDestroy(rec.done);
+            if (rec.pinned) cudaFreeHost(rec.pinned);
+        }
+    }
+    for (auto& rec : s->steps_q) {
+        if (rec.done) cudaEventDestroy(rec.done);
+        if (rec.pinned) cudaFreeHost(rec.pinned);
     }
     cudaStreamDestroy(s->stream);
     delete s;
