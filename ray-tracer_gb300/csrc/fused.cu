@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
         for (uint32_t g = 0; g < 4; ++g)
             fullmask |= (((f0 >> (8u * g)) & 1u) << (2u * g)) | (((f1 >> (8u * g)) & 1u) << (2u * g + 1u));
         __syncwarp();
-        if (mask != 0) {
+        if (mask != 0 && sg.levels > 0u) {  // a scene without triangles has no tree: every ray misses
             int sp = 1;
             if (lane == 0) S.stack[0] = (sg.levels << 28) | mask;
             __syncwarp();
@@ -619,8 +619,10 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
             S.meta[i] = (uint32_t)w.kx | ((uint32_t)w.ky << 2) | ((uint32_t)w.kz << 4) | (active ? 64u : 0u);
             S.slot[i] = id;
             S.best[i] = RSH_HIT_NONE;
-            const uint32_t bl = __ballot_sync(0xffffffffu, active);
-            if (active) S.jobs[qn + __popc(bl & lanemask_lt())] = job_word(i, sg.levels, 0u);
+            // a scene without triangles has no tree: its rays keep the prefilled miss
+            const bool job = active && sg.levels > 0u;
+            const uint32_t bl = __ballot_sync(0xffffffffu, job);
+            if (job) S.jobs[qn + __popc(bl & lanemask_lt())] = job_word(i, sg.levels, 0u);
             qn += __popc(bl);
         }
         __syncwarp();

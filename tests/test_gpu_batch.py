@@ -233,3 +233,38 @@ def test_autotune_scenes_per_scene_choice():
     for sc in scs:
         sc.destroy()
     ctx.destroy()
+
+
+@pytest.mark.parametrize("ray_level", [2, 15])  # the packet kernel and the rays-only kernel
+def test_empty_scene_segments_miss(ray_level):
+    """A scene without triangles in a batch: its segments report no hit and no occlusion; the other
+    segments of the same batch still equal brute force."""
+    ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=6, ray_level=ray_level)
+    s = scenes.random_soup(20_000, np.random.default_rng(61))
+    full = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+    empty = ctx.scene(np.zeros((0, 3, 4), np.float32))
+    rng = np.random.default_rng(62)
+    rays = [scenes.surface_rays(s, n, rng) for n in (9_000, 5_000, 7_000, 3_000)]
+    which = [full, empty, full, empty]
+    anyh = [False, False, True, True]
+    segs = (rsh.BatchSegment * 4)()
+    keep = []
+    for i, (r, sc, a) in enumerate(zip(rays, which, anyh)):
+        dr = rsh.DeviceArray.from_numpy(r)
+        out = rsh.DeviceArray(len(r), np.uint32 if a else np.uint64)
+        out.fill_bytes(0x5A)  # the batch must overwrite every output
+        keep.append((dr, out))
+        segs[i].scene, segs[i].rays, segs[i].n, segs[i].any_hit = sc.handle, dr.ptr, len(r), int(a)
+        segs[i].hits = None if a else out.ptr
+        segs[i].flags = out.ptr if a else None
+    rsh.check(rsh.lib().rsh_batch_trace(ctx.handle, segs, 4, None), "batch")
+    ctx.check_device_errors()
+    for i, (r, sc, a) in enumerate(zip(rays, which, anyh)):
+        got = keep[i][1].numpy(len(r))
+        if sc is empty:
+            assert np.all(got == (0 if a else rsh.HIT_NONE)), i
+        else:
+            assert np.array_equal(got, oracle.brute(s.positions, r, a)), i
+    full.destroy()
+    empty.destroy()
+    ctx.destroy()
