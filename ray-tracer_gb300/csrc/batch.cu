@@ -2,8 +2,10 @@
 //
 // The reference has no batched path: every batch is a host loop of wrappers with a blocking count
 // readback after each stage (main.cpp:951-1054, RayTracer.cu:2316-2832). Here, for S segments:
-//   k_batch_prep     one pass over all rays: gather into one array, key = segment << shift | hash
-//                    (per-segment scene box), pre-fill each segment's output, count each segment's rays;
+//   k_batch_prep     one pass over all rays: key = segment << shift | hash (per-segment scene box),
+//                    pre-fill each segment's output, count each segment's rays (shared-memory counters,
+//                    one global atomic per segment per block); it gathers the rays into one array only for
+//                    the packet kernel when the segments do not already lie back to back;
 //   k_batch_bounds   from those counts (one block): each segment's range of the sorted order (the
 //                    segment tag is the top key digit, so the sorted order is segment-major: a segmented
 //                    sort for free) and of the padded layout, padded so that no level-1 ray node straddles
@@ -12,8 +14,9 @@
 //                    are the cheap ones; the padding slots are marked empty;
 //   compress / sort / decompress over all keys at once; decompress writes each ray straight to its
 //                    padded position;
-//   build            ray-space hierarchy over the padded order;
-//   fused            ONE persistent traversal + intersection launch over every segment's work units.
+//   build            ray-space hierarchy over the padded order (packet kernel only);
+//   fused            ONE persistent traversal + intersection launch over every segment's work units
+//                    (the rays-only kernel reads each segment's rays in place).
 // Nothing reads a count back to the host, so the whole sequence is captured in a CUDA graph.
 #include <algorithm>
 #include <chrono>

@@ -1,4 +1,9 @@
-// Fused persistent traversal + intersection (the batched form's single launch).
+// Fused persistent traversal + intersection (the batched form's single launch). Two kernels:
+//   k_fused_rays (switch level at or above every segment's tree depth, the default): each warp takes
+//     64 sorted rays at a time and runs one job per ray from the root (the per-ray job queue below);
+//     no packet phase and no ray hierarchy; the launch's last units go out as half units;
+//   k_fused (a lower switch level): packets of the ray hierarchy walk the upper object tree, rays leave
+//     them at the switch level, as described next.
 //
 // Reference: the per-frame loop of HierarchyTraversalWarmUpWrapper -> HierarchyTraversalWrapper ->
 // Shadow/ReflectionRayIntersectionWrapper (main.cpp:685-755, RayTracer.cu:2537-3031), which materialises
