@@ -7,7 +7,8 @@
 //  1. one histogram kernel reads the keys once and builds all passes' 256-bin digit histograms; its last
 //     CTA turns them into per-pass exclusive digit offsets;
 //  2. one kernel per 8-bit digit pass: each CTA takes a 3840-key tile by atomic ticket, ranks its keys
-//     stably (warp peer masks from 8 ballots + per-warp digit counters), publishes its per-digit counts,
+//     stably (warp peer masks: every third item by match_any, the others from 8 ballots, 9 in a partial
+//     tile; per-warp digit counters), publishes its per-digit counts,
 //     resolves the per-digit exclusive prefix over earlier tiles by decoupled look-back (bounded spin),
 //     then scatters through shared memory so that global writes are runs of one digit. A status word
 //     holds flag and count together and nothing else is read through it, so it is published and read
@@ -27,6 +28,13 @@ constexpr int SR_TILE = SR_THREADS * SR_ITEMS;  // 3840
 constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_PRE = 2u << 30;
 constexpr uint32_t VAL_MASK = (1u << 30) - 1u;
+
+#ifndef RSH_SORT_MATCH_EVERY
+#define RSH_SORT_MATCH_EVERY 3
+#endif
+#ifndef RSH_SORT_FULL8
+#define RSH_SORT_FULL8 1
+#endif
 
 inline uint32_t num_passes(uint32_t key_bits) { return key_bits == 0 ? 1u : (key_bits + 7u) / 8u; }
 }  // namespace
@@ -115,18 +123,35 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
             val[j] = 0u;
         }
     }
+    const bool full = base + SR_TILE <= n;  // the whole tile holds valid items
     // stable in-warp ranking: items in (j, lane) order = index order
 #pragma unroll
     for (int j = 0; j < SR_ITEMS; ++j) {
         const uint32_t idx = wbase + j * 32u + lane;
         const bool valid = idx < n;
         const uint32_t d = valid ? ((key[j] >> shift) & 255u) : 256u;
-        uint32_t peers = 0xffffffffu;  // lanes holding the same digit (or also invalid)
+        uint32_t peers;  // lanes holding the same digit (or also invalid)
+        if (RSH_SORT_MATCH_EVERY && (j % RSH_SORT_MATCH_EVERY) == RSH_SORT_MATCH_EVERY - 1) {
+            // some items by match_any (the MIO pipe), the others by ballots (the ALU pipe): the two
+            // pipes share the ranking instead of one of them bounding it
+            peers = __match_any_sync(0xffffffffu, d);
+        } else {
+            peers = 0xffffffffu;
+            if (RSH_SORT_FULL8 && full) {  // a full tile has no invalid items: 8 digit bits decide
 #pragma unroll
-        for (int b = 0; b < 9; ++b) {
-            const bool bit = (d >> b) & 1u;
-            const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-            peers &= bit ? bal : ~bal;
+                for (int b = 0; b < 8; ++b) {
+                    const bool bit = (d >> b) & 1u;
+                    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+                    peers &= bit ? bal : ~bal;
+                }
+            } else {
+#pragma unroll
+                for (int b = 0; b < 9; ++b) {
+                    const bool bit = (d >> b) & 1u;
+                    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+                    peers &= bit ? bal : ~bal;
+                }
+            }
         }
         const uint32_t before = __popc(peers & lanemask_lt());
         uint32_t cnt = 0u;
