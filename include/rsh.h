@@ -158,6 +158,9 @@ typedef struct rsh_config {
  * 1680-1696); shadow slots per pixel = lights x 16. Each sample is traced exactly (the reference tests the
  * samples only against the centre ray's candidate triangles). */
 #define RSH_FLAG_SOFT_SHADOWS 8u
+/* Batched form: sort the hashed slots directly instead of their runs of equal keys (no compression or
+ * decompression), for incoherent batches whose keys hardly repeat; rsh_autotune_scenes tries both. */
+#define RSH_FLAG_NO_COMPRESS 16u
 #define RSH_FLAG_RAH 4u            /* plain path: ray-hierarchy ablation without hashing/sorting: packets
                                       of consecutive trimmed rays (the reference's algorithm 1 "RAH",
                                       main.cpp:1016-1037) */
@@ -510,7 +513,8 @@ typedef struct rsh_tune_space {
  * switch level are chosen on that scene's segments alone, one parameter at a time, and stored in the
  * scene (rsh_scene_set_tuning); then every scene at switch level 15 at once is tried against that (the
  * rays-only kernel, which skips the ray hierarchy, runs only when no segment uses packets below the root);
- * last, the packet size and the traversal launch's CTAs per SM are chosen with the scenes tuned. The search keeps the untuned configuration
+ * last, the packet size, the traversal launch's CTAs per SM and run compression on or off
+ * (RSH_FLAG_NO_COMPRESS) are chosen with the scenes tuned. The search keeps the untuned configuration
  * when its result is not faster on the whole batch. Points whose hash does not fit beside the batch's
  * segment tag in 31 bits are skipped. *best_ms (optional) is the whole batch's time with the final
  * choice, *untuned_ms (optional) its time with the context's configuration and no scene tuning. */

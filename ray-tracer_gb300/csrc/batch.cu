@@ -116,6 +116,29 @@ __global__ void k_batch_bounds(const uint32_t* __restrict__ seg_cnt, uint32_t ns
             padded[q] = INVALID_ID;
 }
 
+// Without run compression: the sorted slots go straight to the padded layout (valid keys sort before
+// every empty slot, whose key has the bit above the key's width set); also the stats words (rays,
+// "chunks" = rays) from the per-segment counts.
+__global__ void k_batch_scatter(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ svals,
+                                uint32_t total, uint32_t tag_shift, const uint32_t* __restrict__ seg_delta,
+                                uint32_t* __restrict__ padded, uint32_t max_padded,
+                                const uint32_t* __restrict__ seg_cnt, uint32_t nseg, uint32_t* __restrict__ counts) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < total) {
+        const uint32_t key = skeys[k];
+        if (key != RSH_KEY_NONE) {
+            const uint32_t q = k + __ldg(seg_delta + (key >> tag_shift));
+            if (q < max_padded) padded[q] = svals[k];
+        }
+    }
+    if (k == 0) {
+        uint32_t n = 0;
+        for (uint32_t s = 0; s < nseg; ++s) n += seg_cnt[s];
+        counts[0] = n;
+        counts[1] = n;
+    }
+}
+
 }  // namespace rsh
 
 using namespace rsh;
@@ -200,7 +223,7 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     RSH_TRY(ensure(ctx, "svals", 4ull * n, &pl.svals));
     RSH_TRY(ensure(ctx, "sorted_keys", 4ull * n, &pl.sorted_keys));
     RSH_TRY(ensure(ctx, "sorted_ids", 4ull * n, &pl.sorted_ids));
-    size_t scr = std::max(compress_scratch_bytes(n), sort_scratch_bytes(n, pl.key_bits));
+    size_t scr = std::max(compress_scratch_bytes(n), sort_scratch_bytes(n, pl.key_bits + 1u));
     scr = std::max(scr, decompress_scratch_bytes(n));
     RSH_TRY(ensure(ctx, "scratch", scr, &pl.scr));
     RSH_TRY(ensure(ctx, "b_padded", 4ull * pl.max_padded, &pl.padded));
@@ -353,6 +376,23 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     note_launch();
     RSH_CUDA(cudaGetLastError());
     stage_end(ctx, th, s);
+    if (ctx->cfg.flags & RSH_FLAG_NO_COMPRESS) {
+        // incoherent batches: sort the slots' own keys (one more bit, so that empty slots go last) and
+        // scatter the sorted slots to the padded layout
+        th = stage_begin(ctx, RSH_STAGE_SORT, s);
+        RSH_CUDA(launch_sort_pairs(static_cast<uint32_t*>(pl.keys), nullptr, static_cast<uint32_t*>(pl.skeys),
+                                   static_cast<uint32_t*>(pl.svals), pl.total, nullptr, pl.key_bits + 1u, pl.scr,
+                                   ctx->d_err, s));
+        stage_end(ctx, th, s);
+        th = stage_begin(ctx, RSH_STAGE_DECOMPRESS, s);
+        k_batch_scatter<<<(pl.total + 255) / 256, 256, 0, s>>>(
+            static_cast<uint32_t*>(pl.skeys), static_cast<uint32_t*>(pl.svals), pl.total, pl.tag_shift,
+            static_cast<const uint32_t*>(pl.seg_delta), static_cast<uint32_t*>(pl.padded), pl.max_padded,
+            static_cast<uint32_t*>(pl.seg_cnt), pl.nseg, cnt);
+        note_launch();
+        RSH_CUDA(cudaGetLastError());
+        stage_end(ctx, th, s);
+    } else {
     th = stage_begin(ctx, RSH_STAGE_COMPRESS, s);
     RSH_CUDA(launch_compress(static_cast<uint32_t*>(pl.keys), pl.total, static_cast<uint32_t*>(pl.trimmed),
                              static_cast<uint32_t*>(pl.ckeys), static_cast<uint32_t*>(pl.cbases), cnt, pl.scr,
@@ -371,6 +411,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
                                static_cast<uint32_t*>(pl.cbases), static_cast<uint32_t*>(pl.trimmed), cnt, pl.total,
                                nullptr, nullptr, pl.scr, ctx->d_err, s, &po));
     stage_end(ctx, th, s);
+    }
     if (!pl.rays_only) {  // rays that leave their packets at the root never read the ray hierarchy
         th = stage_begin(ctx, RSH_STAGE_BUILD, s);
         RSH_CUDA(launch_build_rsh(static_cast<rsh_ray*>(pl.rays_all), static_cast<uint32_t*>(pl.padded),
@@ -791,6 +832,17 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
     }
     ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
     ms = tune_blocks(ctx, segs, count, *space, reps, stream, ms);
+    {  // run compression on or off, on the whole batch
+        rsh_config c = ctx->cfg;
+        const rsh_config keep = c;
+        c.flags ^= RSH_FLAG_NO_COMPRESS;
+        float m2;
+        if (rsh_set_config(ctx, &c) == RSH_OK && time_batch(ctx, segs, count, reps, stream, &m2) == RSH_OK &&
+            m2 < ms)
+            ms = m2;
+        else
+            rsh_set_config(ctx, &keep);
+    }
     // keep the untuned configuration when the search found nothing faster on the whole batch (the
     // per-scene steps time sub-batches, which need not add up)
     if (!(ms < untuned)) {

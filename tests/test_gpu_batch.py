@@ -50,7 +50,9 @@ def test_fused_cornell_closest_and_ties(ctx, cornell):
     sc.destroy()
 
 
-def test_batch_segments_many_scenes(ctx):
+@pytest.mark.parametrize("flags", [0, rsh.FLAG_NO_COMPRESS])  # runs of equal keys, or the slots sorted as they are
+def test_batch_segments_many_scenes(ctx, flags):
+    ctx.set_config(flags=flags)
     rng = np.random.default_rng(77)
     sd = [scenes.random_soup(int(t), np.random.default_rng(200 + i)) for i, t in enumerate([12_000, 35_000, 80_000])]
     scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]
@@ -99,6 +101,7 @@ def test_batch_segments_many_scenes(ctx):
     rsh.lib().rsh_stream_destroy(st)
     for sc in scs:
         sc.destroy()
+    ctx.set_config(flags=0)
 
 
 def test_autotune_picks_a_valid_config(ctx):
@@ -121,10 +124,11 @@ def test_autotune_picks_a_valid_config(ctx):
     sc.destroy()
 
 
-def test_many_segments_drop_low_hash_bits():
+@pytest.mark.parametrize("flags", [0, rsh.FLAG_NO_COMPRESS])
+def test_many_segments_drop_low_hash_bits(flags):
     """300 segments need 9 tag bits: with a 27-bit hash (grid 5, dir 6) the key would need 36 bits, so the
     batch drops the hash's 5 lowest bits (ordering only); every segment's results still equal brute force."""
-    ctx = rsh.Context(grid_bits=5, dir_log2=6, packet_size=8, cluster_size=6)
+    ctx = rsh.Context(grid_bits=5, dir_log2=6, packet_size=8, cluster_size=6, flags=flags)
     rng = np.random.default_rng(31)
     sd = [scenes.random_soup(int(t), np.random.default_rng(300 + i)) for i, t in enumerate([4_000, 9_000, 15_000])]
     scs = [ctx.scene(s.positions, s.normals, s.material_ids, s.materials) for s in sd]

@@ -104,7 +104,7 @@ def test_fused_frame_equals_plain_frame():
     """RSH_FLAG_FUSED (batched form inside the frame) must give the same hits, flags and image."""
     s = scenes.soup(n_spheres=400, width=128, height=96, extent=25.0)
     outs = []
-    for flags in (0, rsh.FLAG_FUSED):
+    for flags in (0, rsh.FLAG_FUSED, rsh.FLAG_FUSED | rsh.FLAG_NO_COMPRESS):
         ctx = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8, reflect_jitter=1.0, flags=flags)
         sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
         ctx.set_camera(rsh.camera_look_at(s.eye, s.target, s.up, s.fov, 128, 96))
@@ -120,10 +120,11 @@ def test_fused_frame_equals_plain_frame():
         outs.append((res, st))
         sc.destroy()
         ctx.destroy()
-    for a, b in zip(outs[0][0], outs[1][0]):
-        assert np.array_equal(a, b)
-    assert outs[0][1]["shadow_rays"] == outs[1][1]["shadow_rays"]
-    assert outs[0][1]["reflection_rays"] == outs[1][1]["reflection_rays"]
+    for other in outs[1:]:
+        for a, b in zip(outs[0][0], other[0]):
+            assert np.array_equal(a, b)
+        assert outs[0][1]["shadow_rays"] == other[1]["shadow_rays"]
+        assert outs[0][1]["reflection_rays"] == other[1]["reflection_rays"]
 
 
 @pytest.mark.parametrize("ray_level", [0, 3])
