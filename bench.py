@@ -431,6 +431,16 @@ def gpu_arm(args, s, rank, world, td):
 
 
 # ---------------------------------------------------------------- serving (continuous batching)
+def fcfs_latency_ms(gaps, service) -> list:
+    """Latencies (ms) of requests arriving after the given gaps (s) at one server that takes them first
+    come, first served, each for its own service time (s)."""
+    free_at, out = 0.0, []
+    for a, sv in zip(np.cumsum(gaps), service):
+        free_at = max(free_at, a) + sv
+        out.append((free_at - a) * 1e3)
+    return out
+
+
 def serving_bench(args):
     """Poisson request arrivals over resident scenes through rsh_server_*: p50/p99 latency and Mrays/s,
     next to the same requests rendered one by one through rsh_render_frame (a serial per-frame loop)."""
@@ -481,11 +491,7 @@ def serving_bench(args):
         serial_rays += fs.shadow_rays + fs.reflection_rays
         service.append(time.perf_counter() - t1)
     serial_s = time.perf_counter() - t0
-    arrive = np.cumsum(gaps)
-    free_at, serial_lat = 0.0, []
-    for a, sv in zip(arrive, service):
-        free_at = max(free_at, a) + sv
-        serial_lat.append((free_at - a) * 1e3)
+    serial_lat = fcfs_latency_ms(gaps, service)
     # the server: submit with Poisson gaps, then wait for all
     arrs = (C.c_void_p * n_scenes)(*[s.handle for s in scs])
     srv = C.c_void_p()
