@@ -200,14 +200,15 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
     pl.tag_shift = hash_bits - pl.hash_drop;
     pl.key_bits = pl.tag_shift + tag_bits;
     pl.P = ctx->cfg.packet_size;
-    pl.unit_rays = 8 * pl.P;
+    for (uint32_t s = 0; s < count; ++s)
+        if (tuned_config(ctx->cfg, segs[s].scene).ray_level < segs[s].scene->h.levels) pl.rays_only = 0;
+    // work units: 8 packets for the packet kernel, RSH_RAYS_UNIT sorted rays for the rays-only kernel
+    pl.unit_rays = pl.rays_only ? (uint32_t)RSH_RAYS_UNIT : 8 * pl.P;
     pl.max_padded = pl.total + count * pl.unit_rays;
     const uint32_t n = pl.total ? pl.total : 1;
     pl.contiguous = count > 0;
     for (uint32_t s = 0, at = 0; s < count; at += segs[s].n, ++s)
         if (segs[s].n && segs[s].rays != segs[0].rays + at) pl.contiguous = false;
-    for (uint32_t s = 0; s < count; ++s)
-        if (tuned_config(ctx->cfg, segs[s].scene).ray_level < segs[s].scene->h.levels) pl.rays_only = 0;
     // one ray array for the ray hierarchy and the packet kernel: the segments' own when they lie back to
     // back, else a gathered copy; the rays-only kernel reads every segment's rays in place
     pl.gather = !pl.contiguous && !pl.rays_only;

@@ -676,7 +676,7 @@ static cudaError_t launch_fused_rays_p(const FusedArgs& a, cudaStream_t s) {
 
 template <int P>
 static cudaError_t launch_fused_p(const FusedArgs& a, cudaStream_t s) {
-    if (a.rays_only) return launch_fused_rays_p<P>(a, s);
+    if (a.rays_only) return launch_fused_rays_p<RSH_RAYS_UNIT / 8>(a, s);  // units of RSH_RAYS_UNIT rays
     const size_t smem = sizeof(FusedSmem<P>) * FW;
     cudaError_t e = cudaFuncSetAttribute(k_fused<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -210,6 +210,10 @@ struct FusedArgs {
     uint32_t* err;
 };
 cudaError_t launch_fused(const FusedArgs& a, cudaStream_t s);
+// rays per work unit of the rays-only kernel (a multiple of 64, at most 256: job words hold 8 bits)
+#ifndef RSH_RAYS_UNIT
+#define RSH_RAYS_UNIT 64
+#endif
 
 // ---- resolve + shade (shade.cu)
 cudaError_t launch_resolve(const float4* tris_orig_pos, const float4* tris_orig_nrm,
