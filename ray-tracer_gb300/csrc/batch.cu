@@ -13,7 +13,8 @@
 //                    ones, larger before smaller, so the work units handed out last (the launch's tail)
 //                    are the cheap ones; the padding slots are marked empty;
 //   compress / sort / decompress over all keys at once; decompress writes each ray straight to its
-//                    padded position;
+//                    padded position (RSH_FLAG_NO_COMPRESS: the slots are sorted as they are and
+//                    k_batch_scatter writes them to the padded layout);
 //   build            ray-space hierarchy over the padded order (packet kernel only);
 //   fused            ONE persistent traversal + intersection launch over every segment's work units
 //                    (the rays-only kernel reads each segment's rays in place).
