@@ -80,6 +80,29 @@ RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
 
 RSH_DEV uint32_t job_word(uint32_t i, uint32_t L, uint32_t idx) { return i | (L << 8) | (idx << 12); }
 
+// A job's stack entry. Triangle cluster c: c itself (level bits 0). Node of level L >= 1: L << 27 |
+// (children - 1) << 24 | absolute node index of its first child -- the child link its box carries
+// (lo.w, hi.w), so a popped node's children are loaded straight away. Fits 32 bits: L <= 16, at most
+// 8 children, fewer than 2^24 nodes (the batched form takes at most 2^20 nodes at level 1).
+constexpr uint32_t E_LSHIFT = 27;
+RSH_DEV uint32_t child_entry(uint32_t L, float first_bits, float count_bits) {
+    return (L << 27) | (min(__float_as_uint(count_bits) - 1u, 7u) << 24) | (__float_as_uint(first_bits) & 0xFFFFFFu);
+}
+// The entry of a job's start node (L, idx); L == levels is the virtual root over the top level.
+RSH_DEV uint32_t job_entry(const FusedSeg& sg, const float4* boxes, uint32_t L, uint32_t idx, uint32_t* err) {
+    if (L == 0u) return idx;
+    if (L == sg.levels) {
+        uint32_t cnt = sg.lvl_size[L - 1u];
+        if (cnt == 0u || cnt > 8u) {
+            raise_device_error(err, RSH_DEVERR_OVERFLOW);
+            cnt = cnt == 0u ? 1u : 8u;
+        }
+        return (L << 27) | ((cnt - 1u) << 24) | sg.lvl_off[L - 1u];
+    }
+    const size_t b = 2ull * (sg.lvl_off[L] + idx);
+    return child_entry(L, __ldg(&boxes[b].w), __ldg(&boxes[b + 1].w));
+}
+
 // Ray vs a padded node box over [tmin, tmax]: slab test, NaN-free for zero direction components (fminf /
 // fmaxf drop a NaN operand); tn = entry distance (the nearest-first order key). The padding (1e-5 of the
 // scene's largest coordinate) is far above the rounding of these products, so the cull is conservative.
@@ -98,6 +121,8 @@ RSH_DEV bool box_hit(float4 b0, float4 b1, float ox, float oy, float oz, float i
 template <int P, bool SOLO = false, class SM>
 RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsigned long long& ntests,
                       unsigned long long& ttests, uint32_t* err) {
+    const float4* __restrict__ boxes = sg.boxes;
+    const float4* __restrict__ tris = sg.tris;
     const uint32_t qn = S.qn;
     uint32_t qh = 0;
     bool has = false;
@@ -140,7 +165,7 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                     w.kz = (mt >> 4) & 3u;
                     tcur = sh.w;
                     best = RSH_HIT_NONE;
-                    stk[0] = (((job >> 8) & 15u) << 24) | (job >> 12);
+                    stk[0] = job_entry(sg, boxes, (job >> 8) & 15u, job >> 12, err);
                     sp = 1;
                     has = true;
                 }
@@ -157,7 +182,7 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
         // architecture frame; with sphere descent it had cost 25%)
         bool do_nodes;
         {
-            const bool want = has && sp > 0, node = want && (stk[sp - 1] >> 24) != 0u;
+            const bool want = has && sp > 0, node = want && (stk[sp - 1] >> E_LSHIFT) != 0u;
             const uint32_t nn = __popc(__ballot_sync(0xffffffffu, node));
             const uint32_t nc = __popc(__ballot_sync(0xffffffffu, want && !node));
             do_nodes = nn >= nc;
@@ -174,20 +199,20 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                 tcur = fminf(tcur, __uint_as_float((uint32_t)(b >> 32)));
             }
         }
-        if (sp > 0 && ((stk[sp - 1] >> 24) != 0u) == do_nodes) {
+        if (sp > 0 && ((stk[sp - 1] >> E_LSHIFT) != 0u) == do_nodes) {
             const uint32_t e = stk[--sp];
-            const uint32_t L = e >> 24, idx = e & 0xFFFFFFu;
+            const uint32_t L = e >> E_LSHIFT, idx = e & 0xFFFFFFu;
             if (L == 0u) {
                 // the cluster's padded box against [tmin, current best]: slab test, NaN-free for zero
                 // direction components (fminf/fmaxf drop a NaN operand); a miss skips the triangles
-                const float4 b0 = __ldg(sg.boxes + 2ull * idx), b1 = __ldg(sg.boxes + 2ull * idx + 1);
-                uint32_t t0, t1;
-                cluster_tris(sg.kids, idx, t0, t1);
+                const float4 b0 = __ldg(boxes + 2ull * idx), b1 = __ldg(boxes + 2ull * idx + 1);
+                const uint32_t t0 = __float_as_uint(b0.w);  // the cluster's triangles: its box's link
+                uint32_t t1 = t0 + __float_as_uint(b1.w);
                 float tnb;
                 if (!box_hit(b0, b1, ox, oy, oz, ix, iy, iz, tmin, tcur, tnb)) t1 = t0;
                 for (uint32_t tt = t0; tt < t1; ++tt) {
-                    const float4 v0 = __ldg(sg.tris + 3ull * tt), v1 = __ldg(sg.tris + 3ull * tt + 1),
-                                 v2 = __ldg(sg.tris + 3ull * tt + 2);
+                    const float4 v0 = __ldg(tris + 3ull * tt), v1 = __ldg(tris + 3ull * tt + 1),
+                                 v2 = __ldg(tris + 3ull * tt + 2);
                     float th;
                     ++ttests;
                     if (wt_hit(w, v0, v1, v2, th)) {
@@ -206,15 +231,14 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                 }
             } else {
                 const uint32_t cl = L - 1u;
-                uint32_t first, cnt;
-                node_children(sg.kids, sg.lvl_off, sg.lvl_size, sg.levels, L, idx, first, cnt);
+                // the entry holds the children's link: up to 8 boxes from absolute node `idx` on
+                const uint32_t cnt = ((e >> 24) & 7u) + 1u;
+                const float4* bb = boxes + 2ull * idx;
+                ntests += cnt;
                 // children (at most 8, an invariant of the object tree): their boxes tested into registers,
                 // hits pushed farthest first by selection, so the nearest pops first
-                if (cnt > 8u) raise_device_error(err, RSH_DEVERR_OVERFLOW);
                 float tcs[8];
                 uint32_t hm = 0;
-                const float4* bb = sg.boxes + 2ull * (sg.lvl_off[cl] + first);
-                ntests += min(cnt, 8u);
 #pragma unroll
                 for (uint32_t c = 0; c < 8; ++c) {
                     tcs[c] = 0.0f;
@@ -245,7 +269,8 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                         bc = __ffs(hm) - 1u;
                     }
                     hm &= ~(1u << bc);
-                    stk[sp++] = (cl << 24) | (first + bc);
+                    // a child node's own link, from the box just tested (an L1 hit)
+                    stk[sp++] = cl == 0u ? idx + bc : child_entry(cl, __ldg(&bb[2 * bc].w), __ldg(&bb[2 * bc + 1].w));
                 }
             }
         }

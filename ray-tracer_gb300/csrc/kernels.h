@@ -115,7 +115,7 @@ struct ObjHierarchy {
     uint32_t* kids = nullptr;      // per level l (at level_off[l] + l): level_size[l] + 1 child-range starts
     float4* tris = nullptr;        // cluster order, 3 per triangle, v0.w = original id bits
     uint32_t* order = nullptr;     // cluster slot -> original triangle id
-    float4* boxes = nullptr;       // per node, all levels like spheres: padded box lo, hi (w unused)
+    float4* boxes = nullptr;       // per node, all levels like spheres: padded box lo, hi; lo.w / hi.w: child link
 };
 cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t tri_count, uint32_t cluster,
                                    const float lo[3], const float hi[3], ObjHierarchy& h,

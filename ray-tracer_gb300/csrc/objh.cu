@@ -121,8 +121,12 @@ __global__ void k_level_nodes(const uint32_t* __restrict__ firsts, uint32_t nn, 
 
 // One warp per node: the sphere over every vertex of the node's triangle range. Min/max and max
 // reductions are exact in any order.
-// Also the node's box, widened by `pad` on every side.
+// Also the node's box, widened by `pad` on every side, whose spare w words hold the node's child link:
+// lo.w = first child as an absolute node index (`child_off` + the level's child-range start; at level 0
+// the first triangle), hi.w = the number of children (triangles), both as raw u32 bits. A single ray
+// that pops a node then loads its children's boxes directly, with no child-range lookup in between.
 __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t* __restrict__ tstart, uint32_t nnodes,
+                                const uint32_t* __restrict__ kids, uint32_t child_off,
                                 float4* __restrict__ sph, float4* __restrict__ box, float pad) {
     const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
@@ -149,8 +153,9 @@ __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t*
         mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
     }
     if (lane == 0) {
-        box[2 * j] = make_float4(mnx - pad, mny - pad, mnz - pad, 0.f);
-        box[2 * j + 1] = make_float4(mxx + pad, mxy + pad, mxz + pad, 0.f);
+        const uint32_t k0 = __ldg(kids + j), k1 = __ldg(kids + j + 1);
+        box[2 * j] = make_float4(mnx - pad, mny - pad, mnz - pad, __uint_as_float(child_off + k0));
+        box[2 * j + 1] = make_float4(mxx + pad, mxy + pad, mxz + pad, __uint_as_float(k1 - k0));
     }
     const v3 c = v3{(mnx + mxx) * 0.5f, (mny + mxy) * 0.5f, (mnz + mxz) * 0.5f};
     float r2 = 0.f;
@@ -266,7 +271,8 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
         k_level_nodes<<<(nn + 256) / 256, 256, 0, s>>>(firsts, nn, items, start, n, l == 0,
                                                        h.kids + total + l, nstart);
         note_launch();
-        k_level_spheres<<<(nn * 32 + 127) / 128, 128, 0, s>>>(h.tris, nstart, nn, h.spheres + total,
+        k_level_spheres<<<(nn * 32 + 127) / 128, 128, 0, s>>>(h.tris, nstart, nn, h.kids + total + l,
+                                                              l == 0 ? 0u : h.level_off[l - 1], h.spheres + total,
                                                               h.boxes + 2ull * total, box_pad);
         note_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) break;
