@@ -1,6 +1,9 @@
 """CPU checks of the oracle itself: against the committed golden vectors, against independent numpy
-restatements of the hash / compression / sort / decompression semantics, and the hierarchy path against
-its own brute force (conservativeness of the sphere/cone culling)."""
+restatements of the hash / compression / sort / decompression semantics, the hierarchy path against
+its own brute force (conservativeness of the sphere/cone culling), and the object tree's shape: the
+properties the GPU's single-ray descent encodes in 32-bit stack entries (at most 8 children a node, fewer
+than 2^24 nodes) and relies on (child ranges partition each level, spheres enclose their vertices). The GPU
+builds the same tree bit for bit (test_gpu_stages.py::test_object_hierarchy_bitexact)."""
 import numpy as np
 import pytest
 
@@ -146,3 +149,58 @@ def test_hierarchy_path_equals_brute_force_soup(P):
     rays["tmax"] = 2.0
     res, R, _, _ = oh.trace_keyed(rays, keys, 23, P, True)
     assert np.array_equal(res, oracle.brute(s.positions, rays, True))
+
+
+# ---------------------------------------------------------------- object-tree shape
+def _tree_checks(positions, cluster):
+    pos = np.asarray(positions, np.float32).reshape(-1, 12)
+    pts = pos.reshape(-1, 4)[:, :3]
+    lo, hi = pts.min(0), pts.max(0)
+    oh = oracle.ObjH(pos, cluster, lo, hi)
+    sizes, kids = oh.levels(), oh.kids()
+    order, tris, sph = oh.arrays()
+    levels, T = len(sizes), oh.T
+    off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    # the virtual root's children fit one node step; fewer than 2^24 nodes in all
+    assert sizes[-1] <= 8 and sum(sizes) < (1 << 24)
+    # child ranges partition the level below: clusters of 1..cluster triangles, nodes of 1..8 children
+    for l in range(levels):
+        k = kids[l].astype(np.int64)
+        below = T if l == 0 else sizes[l - 1]
+        cnt = np.diff(k)
+        assert k[0] == 0 and k[-1] == below and cnt.min() >= 1
+        assert cnt.max() <= (cluster if l == 0 else 8), (l, int(cnt.max()))
+    # every sphere encloses every vertex of its triangle range (the cull never drops a real hit)
+    tstart = kids[0].astype(np.int64)
+    v = tris.reshape(-1, 3, 4)[:, :, :3].astype(np.float64)
+    for l in range(levels):
+        if l > 0:
+            tstart = tstart[kids[l].astype(np.int64)]
+        s = sph[off[l]:off[l] + sizes[l]].astype(np.float64)
+        owner = np.repeat(np.arange(sizes[l]), np.diff(tstart))
+        d = np.sqrt(((v - s[owner, None, :3]) ** 2).sum(-1)).max(-1)
+        assert (d <= s[owner, 3]).all(), l
+    # a depth-first walk by (level, first child, count) entries -- the single-ray descent's stack --
+    # reaches every cluster and every triangle exactly once
+    seen = np.zeros(T, np.int32)
+    stack = [(levels, int(off[-1]), sizes[-1])]
+    while stack:
+        L, first, cnt = stack.pop()
+        for c in range(first, first + cnt):
+            if L == 1:
+                seen[kids[0][c]:kids[0][c + 1]] += 1
+            else:
+                j = c - off[L - 1]
+                stack.append((L - 1, int(off[L - 2] + kids[L - 1][j]), int(kids[L - 1][j + 1] - kids[L - 1][j])))
+    assert (seen == 1).all()
+    assert np.array_equal(np.sort(order), np.arange(T))
+
+
+@pytest.mark.parametrize("cluster", [6, 32])
+def test_object_tree_shape_cornell(cluster):
+    _tree_checks(scenes.cornell().positions, cluster)
+
+
+@pytest.mark.parametrize("cluster", [1, 6])
+def test_object_tree_shape_soup(cluster):
+    _tree_checks(scenes.random_soup(20000, np.random.default_rng(9)).positions, cluster)
