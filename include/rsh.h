@@ -554,6 +554,11 @@ typedef struct rsh_request_result {
 rsh_status rsh_server_create(rsh_ctx* ctx, const rsh_scene* const* scenes, uint32_t scene_count,
                              uint64_t hbm_budget, uint32_t max_inflight, rsh_server** out);
 rsh_status rsh_server_submit(rsh_server* srv, const rsh_request* req, uint64_t* id_out);
+/* Device bytes the server reserves for a request while it is in flight (what admission counts against
+ * the HBM budget); host arithmetic only. RSH_ERR_INVALID for a request that rsh_server_submit rejects
+ * on its own fields (scene index aside): zero size, depth outside 1..4, lights outside 1..8, or
+ * width x height x lights of 2^31 or more. */
+rsh_status rsh_server_request_bytes(const rsh_request* req, uint64_t* bytes);
 /* Waits up to timeout_ms for request `id`; copies its closest-hit records per bounce
  * (depth x width*height) and shadow flags (depth x width*height*lights) if the pointers are
  * non-NULL. RSH_ERR_TIMEOUT if not finished. */

@@ -57,14 +57,45 @@ struct Req {
     uint32_t* flags = nullptr;           // depth x npix x L
 };
 
-size_t request_bytes(const rsh_request& r) {
+// A request's device buffers: one allocation, regions back to back, each starting on a 256-byte boundary.
+// Returns the bytes the layout needs; with `q` and `base` set it also points q's buffers into `base`. The
+// admission budget and the allocation both come from here, so the regions always fit.
+size_t request_layout(const rsh_request& r, Req* q = nullptr, char* base = nullptr) {
     const size_t npix = (size_t)r.width * r.height;
     const size_t np = (size_t)((r.width + 7) / 8) * ((r.height + 7) / 8) * 64;
     const size_t L = r.light_count;
-    size_t b = np * (32 + 4 + 8) + npix * (16 + 16 + 32 * L + 64) +
-               npix * 8 * r.depth + npix * L * 4 * r.depth;
-    return (b + 4095) & ~size_t(4095);
+    size_t off = 0;
+    auto take = [&](size_t n) {
+        char* x = base ? base + off : nullptr;
+        off += (n + 255) & ~size_t(255);
+        return x;
+    };
+    char* prim_rays = take(np * 32);
+    char* prim_pix = take(np * 4);
+    char* prim_hits = take(np * 8);
+    char* spos = take(npix * 16);
+    char* snrm = take(npix * 16);
+    char* srays = take(npix * L * 32);
+    char* rrays0 = take(npix * 32);
+    char* rrays1 = take(npix * 32);
+    char* hits = take(npix * 8 * r.depth);
+    char* flags = take(npix * L * 4 * r.depth);
+    if (q && base) {
+        q->prim_rays = reinterpret_cast<rsh_ray*>(prim_rays);
+        q->prim_pix = reinterpret_cast<uint32_t*>(prim_pix);
+        q->prim_hits = reinterpret_cast<unsigned long long*>(prim_hits);
+        q->spos = reinterpret_cast<float4*>(spos);
+        q->snrm = reinterpret_cast<float4*>(snrm);
+        q->srays = reinterpret_cast<rsh_ray*>(srays);
+        q->rrays[0] = reinterpret_cast<rsh_ray*>(rrays0);
+        q->rrays[1] = reinterpret_cast<rsh_ray*>(rrays1);
+        q->hits = reinterpret_cast<unsigned long long*>(hits);
+        q->flags = reinterpret_cast<uint32_t*>(flags);
+    }
+    return off;
 }
+
+size_t request_bytes(const rsh_request& r) { return (request_layout(r) + 4095) & ~size_t(4095); }
 
 }  // namespace
 
@@ -99,28 +130,10 @@ struct rsh_server {
 namespace {
 
 rsh_status alloc_request(Req* q) {
-    const rsh_request& r = q->r;
-    const size_t npix = (size_t)r.width * r.height;
-    const size_t np = (size_t)((r.width + 7) / 8) * ((r.height + 7) / 8) * 64;
-    const size_t L = r.light_count;
     char* p = nullptr;
-    RSH_CUDA(cudaMalloc(&p, q->bytes));
+    RSH_CUDA(cudaMalloc(&p, q->bytes));  // q->bytes = request_bytes(q->r) >= request_layout(q->r)
     q->buf = p;
-    auto take = [&](size_t n) {
-        char* x = p;
-        p += (n + 255) & ~size_t(255);
-        return x;
-    };
-    q->prim_rays = reinterpret_cast<rsh_ray*>(take(np * 32));
-    q->prim_pix = reinterpret_cast<uint32_t*>(take(np * 4));
-    q->prim_hits = reinterpret_cast<unsigned long long*>(take(np * 8));
-    q->spos = reinterpret_cast<float4*>(take(npix * 16));
-    q->snrm = reinterpret_cast<float4*>(take(npix * 16));
-    q->srays = reinterpret_cast<rsh_ray*>(take(npix * L * 32));
-    q->rrays[0] = reinterpret_cast<rsh_ray*>(take(npix * 32));
-    q->rrays[1] = reinterpret_cast<rsh_ray*>(take(npix * 32));
-    q->hits = reinterpret_cast<unsigned long long*>(take(npix * 8 * r.depth));
-    q->flags = reinterpret_cast<uint32_t*>(take(npix * L * 4 * r.depth));
+    request_layout(q->r, q, p);
     return RSH_OK;
 }
 
@@ -386,10 +399,20 @@ rsh_status rsh_server_create(rsh_ctx* ctx, const rsh_scene* const* scenes, uint3
     return RSH_OK;
 }
 
+static bool request_fields_ok(const rsh_request* req) {
+    return req && req->width != 0 && req->height != 0 && req->depth >= 1 && req->depth <= 4 &&
+           req->light_count >= 1 && req->light_count <= 8 &&
+           (uint64_t)req->width * req->height * req->light_count < (1ull << 31);
+}
+
+rsh_status rsh_server_request_bytes(const rsh_request* req, uint64_t* bytes) {
+    if (!bytes || !request_fields_ok(req)) return RSH_ERR_INVALID;
+    *bytes = request_bytes(*req);
+    return RSH_OK;
+}
+
 rsh_status rsh_server_submit(rsh_server* s, const rsh_request* req, uint64_t* id_out) {
-    if (!s || !req || req->scene_index >= s->scenes.size() || req->width == 0 || req->height == 0 ||
-        req->depth < 1 || req->depth > 4 || req->light_count < 1 || req->light_count > 8)
-        return RSH_ERR_INVALID;
+    if (!s || !request_fields_ok(req) || req->scene_index >= s->scenes.size()) return RSH_ERR_INVALID;
     Req* q = new Req();
     q->r = *req;
     q->bytes = request_bytes(*req);

@@ -214,6 +214,7 @@ SIGNATURES = {
     "rsh_autotune_scenes": (C.c_int, [_P, _P, _U32, _P, _P, _P, _P]),
     "rsh_server_create": (C.c_int, [_P, _P, _U32, _U64, _U32, _P]),
     "rsh_server_submit": (C.c_int, [_P, _P, _P]),
+    "rsh_server_request_bytes": (C.c_int, [_P, _P]),
     "rsh_server_wait": (C.c_int, [_P, _U64, _U32, _P, _P, _P]),
     "rsh_server_cancel": (C.c_int, [_P, _U64]),
     "rsh_server_stats": (C.c_int, [_P, _P, _P, _P, _P]),

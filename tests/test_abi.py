@@ -1,5 +1,6 @@
 """CPU-only checks of the C ABI boundary: the library loads, exports every entry point declared in
-include/rsh.h, and its host-only entry points (configuration, hash parameters, camera, PNG) behave."""
+include/rsh.h, and its host-only entry points (configuration, hash parameters, serving request sizes,
+camera, PNG) behave."""
 import ctypes as C
 import re
 import struct
@@ -76,6 +77,32 @@ def test_hash_params_host_arithmetic():
         rsh.hash_params((0, 0, 0), (1, 1, 1), 10, 6, 0)  # 42 bits
     with pytest.raises(rsh.RshError):
         rsh.hash_params((0, 0, 0), (1, 1, 1), 0, 4, 0)
+
+
+def test_server_request_bytes_cover_every_region():
+    """The serving loop's per-request allocation holds ten buffers, each starting on a 256-byte boundary;
+    the bytes admission reserves must cover their padded sizes for any resolution (odd ones included)."""
+    lib = rsh.load()
+
+    def padded_sum(W, H, depth, L):
+        npix, np_ = W * H, ((W + 7) // 8) * ((H + 7) // 8) * 64
+        sizes = [np_ * 32, np_ * 4, np_ * 8, npix * 16, npix * 16, npix * L * 32, npix * 32, npix * 32,
+                 npix * 8 * depth, npix * L * 4 * depth]
+        return sum((n + 255) // 256 * 256 for n in sizes)
+
+    for W, H, depth, L in [(64, 64, 1, 1), (33, 33, 2, 3), (1, 1, 1, 1), (1921, 1079, 4, 8), (7, 513, 3, 5),
+                           (255, 257, 1, 2)]:
+        r = rsh.Request()
+        r.width, r.height, r.depth, r.light_count = W, H, depth, L
+        got = C.c_uint64()
+        assert lib.rsh_server_request_bytes(C.byref(r), C.byref(got)) == rsh.RSH_OK
+        assert got.value >= padded_sum(W, H, depth, L) and got.value % 4096 == 0, (W, H, depth, L)
+    for W, H, depth, L in [(0, 8, 1, 1), (8, 8, 0, 1), (8, 8, 5, 1), (8, 8, 1, 0), (8, 8, 1, 9),
+                           (65536, 4096, 1, 8)]:
+        r = rsh.Request()
+        r.width, r.height, r.depth, r.light_count = W, H, depth, L
+        got = C.c_uint64()
+        assert lib.rsh_server_request_bytes(C.byref(r), C.byref(got)) == rsh.RSH_ERR_INVALID, (W, H, depth, L)
 
 
 def test_camera_look_at_matches_engine_camera():
