@@ -175,7 +175,7 @@ struct FusedSeg {
     const float4* spheres;
     const uint32_t* kids;          // object-tree child ranges (level l at lvl_off[l] + l)
     const float4* tris;
-    const float4* boxes;           // per node (like spheres): padded box lo, hi
+    const float4* boxes;           // per node (like spheres): padded box lo, hi; lo.w / hi.w: child link
     uint32_t tri_count;
     uint32_t cluster;
     uint32_t levels;
