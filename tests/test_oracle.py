@@ -3,7 +3,9 @@ restatements of the hash / compression / sort / decompression semantics, the hie
 its own brute force (conservativeness of the sphere/cone culling), and the object tree's shape: the
 properties the GPU's single-ray descent encodes in 32-bit stack entries (at most 8 children a node, fewer
 than 2^24 nodes) and relies on (child ranges partition each level, spheres enclose their vertices). The GPU
-builds the same tree bit for bit (test_gpu_stages.py::test_object_hierarchy_bitexact)."""
+builds the same tree bit for bit (test_gpu_stages.py::test_object_hierarchy_bitexact). Last, the watertight
+triangle test (Woop, Benthin & Wald 2013) lets no ray through a shared edge or vertex, including rays with
+zero direction components."""
 import numpy as np
 import pytest
 
@@ -204,3 +206,56 @@ def test_object_tree_shape_cornell(cluster):
 @pytest.mark.parametrize("cluster", [1, 6])
 def test_object_tree_shape_soup(cluster):
     _tree_checks(scenes.random_soup(20000, np.random.default_rng(9)).positions, cluster)
+
+
+# ---------------------------------------------------------------- watertight intersection
+def _rays(o, d):
+    r = np.zeros(len(o), oracle.RAY_DTYPE)
+    r["o"], r["d"], r["tmin"], r["tmax"] = o, d, 0.0, np.inf
+    return r
+
+
+def test_watertight_grid_edges_and_vertices():
+    """A flat grid of 2 x 16 x 16 triangles in z = 0, hit straight down (zero x and y direction components)
+    and obliquely exactly on its shared edges (axis-aligned and diagonal) and vertices: a watertight test
+    lets no such ray through, and every hit lies at the plane's distance."""
+    N = 16
+    ij = np.stack(np.meshgrid(np.arange(N + 1), np.arange(N + 1), indexing="ij"), -1).reshape(-1, 2)
+    verts = np.concatenate([ij.astype(np.float32), np.zeros((len(ij), 1), np.float32)], 1)
+    vid = lambda i, j: i * (N + 1) + j
+    faces = []
+    for i in range(N):
+        for j in range(N):
+            faces += [(vid(i, j), vid(i + 1, j), vid(i + 1, j + 1)), (vid(i, j), vid(i + 1, j + 1), vid(i, j + 1))]
+    pos, _ = scenes._pack(verts, np.array(faces))
+    g = np.arange(1, N, dtype=np.float32)
+    h = np.arange(N, dtype=np.float32) + np.float32(0.5)
+    pts = np.concatenate([
+        np.stack(np.meshgrid(g, h, indexing="ij"), -1).reshape(-1, 2),   # edges along y
+        np.stack(np.meshgrid(h, g, indexing="ij"), -1).reshape(-1, 2),   # edges along x
+        np.stack([h, h], -1),                                             # diagonals (cell centres)
+        np.stack(np.meshgrid(g, g, indexing="ij"), -1).reshape(-1, 2),   # inner vertices
+    ]).astype(np.float32)
+    targets = np.concatenate([pts, np.zeros((len(pts), 1), np.float32)], 1)
+    for d in (np.array([0, 0, -1], np.float32), np.array([0.3, -0.2, -1], np.float32)):
+        d = (d / np.linalg.norm(d)).astype(np.float32)
+        o = (targets - 4.0 * d).astype(np.float32)
+        hits = oracle.brute(pos, _rays(o, np.repeat(d[None], len(o), 0)), False)
+        assert np.all(hits != oracle.HIT_NONE), "a ray through an edge or vertex slipped through the grid"
+        t = (hits >> np.uint64(32)).astype(np.uint32).view(np.float32)
+        assert np.allclose(t, 4.0, rtol=1e-5)
+        occl = oracle.brute(pos, _rays(o, np.repeat(d[None], len(o), 0)), True)
+        assert np.all(occl != 0)
+
+
+def test_watertight_closed_mesh():
+    """Rays from outside at every edge midpoint and vertex of a closed icosphere all hit it."""
+    sv, sf = scenes.icosphere(2)
+    pos, _ = scenes._pack(sv, sf, sv)
+    edges = np.concatenate([sf[:, [0, 1]], sf[:, [1, 2]], sf[:, [2, 0]]])
+    targets = np.concatenate([(sv[edges[:, 0]] + sv[edges[:, 1]]) * 0.5, sv]).astype(np.float32)
+    o = (targets * 3.0 + np.random.default_rng(2).normal(0, 0.2, targets.shape)).astype(np.float32)
+    d = targets - o
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    hits = oracle.brute(pos, _rays(o, d), False)
+    assert np.all(hits != oracle.HIT_NONE)
