@@ -109,6 +109,36 @@ def test_compress_sort_decompress_match_numpy():
     assert np.array_equal(dk, tk[o2])
 
 
+def _np_pipeline(keys):
+    valid = np.nonzero(keys != 0xFFFFFFFF)[0]
+    tk = keys[valid]
+    heads = np.concatenate([[True], tk[1:] != tk[:-1]]) if len(tk) else np.zeros(0, bool)
+    return valid, tk, heads
+
+
+@pytest.mark.parametrize("case", ["empty", "all_invalid", "one", "all_equal", "full_32_bit", "alternating"])
+def test_compress_sort_decompress_edge_cases(case):
+    rng = np.random.default_rng(7)
+    keys = {
+        "empty": np.zeros(0, np.uint32),
+        "all_invalid": np.full(77, 0xFFFFFFFF, np.uint32),
+        "one": np.array([12345], np.uint32),
+        "all_equal": np.full(5000, 3, np.uint32),
+        "full_32_bit": rng.integers(0, 0xFFFFFFFF, 20000, dtype=np.uint64).astype(np.uint32),
+        "alternating": np.tile(np.array([1, 2], np.uint32), 3000),
+    }[case]
+    valid, tk, heads = _np_pipeline(keys)
+    tr, ck, cb, cs = oracle.compress(keys)
+    assert np.array_equal(tr, valid) and np.array_equal(ck, tk[heads])
+    assert np.array_equal(cb, np.append(np.nonzero(heads)[0], len(tk))) and np.array_equal(cs, np.diff(cb))
+    sk, sv = oracle.sort_pairs(ck, None, 32)
+    order = np.argsort(ck, kind="stable")
+    assert np.array_equal(sv, order) and np.array_equal(sk, ck[order])
+    dk, di = oracle.decompress(sk, sv, cb, tr)
+    o2 = np.argsort(tk, kind="stable")
+    assert np.array_equal(di, valid[o2]) and np.array_equal(dk, tk[o2])
+
+
 def test_hierarchy_path_equals_brute_force_cornell(cornell):
     s = cornell
     W = H = 48
