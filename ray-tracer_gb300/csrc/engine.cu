@@ -13,6 +13,8 @@
 #include <mutex>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "engine.h"
 
 namespace rsh {
@@ -22,7 +24,14 @@ static std::atomic<uint64_t> g_launches{0};
 
 void note_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Every stage is also an NVTX range on the calling host thread (a no-op unless a profiler such as Nsight
+// Systems is attached), so a timeline shows the pipeline's stages around their kernels.
+static const char* const kStageNames[RSH_STAGE_COUNT] = {"rsh primary", "rsh raygen",     "rsh compress",
+                                                         "rsh sort",    "rsh decompress", "rsh build",
+                                                         "rsh traverse", "rsh intersect", "rsh shade"};
+
 int stage_begin(rsh_ctx* ctx, int stage, cudaStream_t s) {
+    nvtxRangePushA(stage >= 0 && stage < RSH_STAGE_COUNT ? kStageNames[stage] : "rsh stage");
     if (!(ctx->cfg.flags & RSH_FLAG_STAGE_TIMERS) || ctx->timers_paused) return -1;
     while (ctx->tev.size() < ctx->tev_used + 2) {
         cudaEvent_t ev;
@@ -37,6 +46,7 @@ int stage_begin(rsh_ctx* ctx, int stage, cudaStream_t s) {
 }
 
 void stage_end(rsh_ctx* ctx, int handle, cudaStream_t s) {
+    nvtxRangePop();
     if (handle < 0) return;
     cudaEventRecord(ctx->tev[handle + 1], s);
 }
