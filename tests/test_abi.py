@@ -105,6 +105,25 @@ def test_server_request_bytes_cover_every_region():
         assert lib.rsh_server_request_bytes(C.byref(r), C.byref(got)) == rsh.RSH_ERR_INVALID, (W, H, depth, L)
 
 
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_host_stub_compiles_and_links(lang, tmp_path):
+    """tests/host_stub.c, an engine-style host that renders one frame through the C ABI, compiles against
+    include/rsh.h with warnings as errors, as C99 and as C++17, and links against librsh.so."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    lib = rsh.load()  # builds nothing; the library must exist
+    root = HEADER.parent.parent
+    std = ["-std=c99"] if lang == "c" else ["-x", "c++", "-std=c++17"]
+    cmd = [cc, *std, "-Wall", "-Wextra", "-Werror", "-I", str(HEADER.parent), str(root / "tests" / "host_stub.c"),
+           "-L", str(Path(lib._name).parent), "-lrsh", "-o", str(tmp_path / "host_stub")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_camera_look_at_matches_engine_camera():
     cam = rsh.camera_look_at((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 60.0, 512, 256)
     dist = 3.4
