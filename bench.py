@@ -184,14 +184,13 @@ def cpu_baseline(s, crop=None, threads=None, steps=1, min_seconds=0.0, max_passe
     W, H = s.width, s.height
     cw, chh = crop if crop else (W, H)
     x0, y0 = (W - cw) // 2, (H - chh) // 2
-    import rsh
-
-    cam = rsh.camera_look_at(s.eye, s.target, s.up, s.fov, W, H).as_array()
+    # the camera and the GPU path's default configuration come from the oracle too, so that this leg maps
+    # no product code (grid bits, direction bits, packet, cluster, ray level)
+    cam = oracle.camera_look_at(s.eye, s.target, s.up, s.fov, W, H)
     lo = s.positions[..., :3].reshape(-1, 3).min(0)
     hi = s.positions[..., :3].reshape(-1, 3).max(0)
-    # the GPU path's default configuration (grid bits, direction bits, packet, cluster, ray level)
-    dc = rsh.default_config()
-    g, b, P, K, rl = dc.grid_bits, dc.dir_log2, dc.packet_size, dc.cluster_size, dc.plain_ray_level
+    dc = oracle.DEFAULTS
+    g, b, P, K, rl = dc["grid_bits"], dc["dir_log2"], dc["packet_size"], dc["cluster_size"], dc["plain_ray_level"]
     t0 = time.perf_counter()
     oh = oracle.ObjH(s.positions, K, lo, hi)
     build_s = time.perf_counter() - t0

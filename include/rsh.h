@@ -230,6 +230,8 @@ rsh_status rsh_event_record(void* ev, rsh_stream_t stream);
 rsh_status rsh_event_elapsed(void* start, void* stop, float* ms);
 int rsh_device_count(void);
 int rsh_sm_count(void);
+/* Free and total memory of the current device (cudaMemGetInfo), e.g. to size an HBM budget. */
+rsh_status rsh_device_memory(uint64_t* free_bytes, uint64_t* total_bytes);
 /* Number of this library's kernels launched by this process so far (all contexts). */
 uint64_t rsh_kernel_launches(void);
 
@@ -378,7 +380,8 @@ rsh_status rsh_compress(rsh_ctx* ctx, const uint32_t* keys, uint32_t n_slots, ui
  * pre-partition all device memory, and loops that allocate once at start-up and must not allocate while
  * they run. No counterpart in the reference. The scratch (per-tile summaries and prefixes) is a static device array of 196,684 bytes that every GPU loading the
  * library keeps until the process exits; n_slots above 16,777,216 is rejected with RSH_ERR_INVALID. The
- * first call on a device looks up the array's device address (call it once before any stream capture).
+ * first call on a device looks up the array's device address (call it once before any stream capture);
+ * that address is kept for the process, so a cudaDeviceReset of that device invalidates it.
  * All calls share the array: calls that overlap on the GPU race, so serialise them on one stream. */
 rsh_status rsh_compress_noalloc(const uint32_t* keys, uint32_t n_slots, uint32_t* trimmed_ids,
                                 uint32_t* chunk_keys, uint32_t* chunk_bases, uint32_t* chunk_sizes,

@@ -22,6 +22,12 @@ KEY_NONE = 0xFFFFFFFF
 HIT_NONE = 0xFFFFFFFFFFFFFFFF
 OCCLUDED = 0xFFFFFFFF
 
+# The GPU path's default configuration (rsh_config_default): origin-grid bits, direction bits (2 per
+# octahedral axis), packet size, cluster size, and the plain path's switch level from packets to rays.
+# The CPU baseline follows the same configuration; a CPU test checks these against the library's.
+DEFAULTS = {"grid_bits": 4, "dir_log2": 6, "packet_size": 8, "cluster_size": 6, "plain_ray_level": 4,
+            "ray_level": 15, "epsilon": 0.01}
+
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 NODE_DTYPE = np.dtype([("c", "<f4", 3), ("radius", "<f4"), ("axis", "<f4", 3), ("cos_spread", "<f4"),
                        ("sin_spread", "<f4"), ("reach", "<f4"), ("first", "<u4"), ("count", "<u4")])
@@ -54,6 +60,7 @@ def lib():
             "orc_hash_params": (None, [P, P, U32, P]),
             "orc_hash": (None, [P, U32, P, P, U32, U32, U32, P]),
             "orc_raygen_primary": (None, [P, U32, U32, P, P]),
+            "orc_camera_look_at": (I, [P, P, P, F, U32, U32, P]),
             "orc_raygen_shadow": (None, [P, P, U32, U32, P, U32, F, P, P, U32, U32, P, P]),
             "orc_raygen_shadow_samples": (None, [P, P, U32, U32, P, U32, U32, F, P, P, U32, U32, P, P]),
             "orc_shade": (None, [P, P, P, U32, P, P, U32, U32, P, U32, U32, P, U32, P]),
@@ -76,6 +83,7 @@ def lib():
             "orc_traverse": (U64, [P, P, U32, U32, U32, P, U64, P]),
             "orc_intersect": (None, [P, P, P, U32, U32, P, U64, I, P, P]),
             "orc_brute": (None, [P, U32, P, U32, I, P, P]),
+            "orc_brute_scalar": (None, [P, U32, P, U32, I, P, P]),
             "orc_brute_second": (None, [P, U32, P, U32, P, P]),
             "orc_resolve": (None, [P, P, P, P, P, P, U32, P, P]),
             "orc_trace_keyed": (U32, [P, P, P, U32, U32, U32, I, P, P, P, P, U32]),
@@ -88,7 +96,8 @@ def lib():
 
 
 def _p(a):
-    return None if a is None else a.ctypes.data
+    # a ctypes pointer that keeps the array alive for the call (the array may be a temporary conversion)
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
 def _f32(a):
@@ -114,6 +123,16 @@ def hash_rays(rays, lo, scale, g, b, tag=0):
     keys = np.empty(len(rays), np.uint32)
     lib().orc_hash(_p(rays), len(rays), _p(_f32(lo)), _p(_f32(scale)), g, b, tag, _p(keys))
     return keys
+
+
+def camera_look_at(eye, target, up, fov_degrees, W, H) -> np.ndarray:
+    """Camera::loadView's basis as 12 floats (eye, direction, right, up), the layout of rsh_camera."""
+    cam = np.zeros(12, np.float32)
+    e, t, u = _f32(eye), _f32(target), _f32(up)
+    ok = lib().orc_camera_look_at(_p(e), _p(t), _p(u), float(fov_degrees), W, H, _p(cam))
+    if not ok:
+        raise ValueError("degenerate camera")
+    return cam
 
 
 def raygen_primary(cam: np.ndarray, W: int, H: int):
@@ -297,13 +316,16 @@ class ObjH:
             pass
 
 
-def brute(positions, rays, any_hit):
+def brute(positions, rays, any_hit, scalar=False):
+    """Every ray against every triangle: shadow flags (any_hit) or closest-hit records. scalar=True runs the
+    plain one-triangle-at-a-time loop (same results, slower)."""
     pos = _f32(positions).reshape(-1, 12)
     rays = np.ascontiguousarray(rays, RAY_DTYPE)
     n = len(rays)
     flags = np.zeros(n, np.uint32)
     hits = np.full(n, HIT_NONE, np.uint64)
-    lib().orc_brute(_p(pos), pos.shape[0], _p(rays), n, int(any_hit), _p(flags), _p(hits))
+    fn = lib().orc_brute_scalar if scalar else lib().orc_brute
+    fn(_p(pos), pos.shape[0], _p(rays), n, int(any_hit), _p(flags), _p(hits))
     return flags if any_hit else hits
 
 

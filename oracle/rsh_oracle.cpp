@@ -487,6 +487,36 @@ void orc_hash(const float* rays, uint32_t n, const float lo[3], const float scal
         keys[i] = (r[i].tmax > r[i].tmin) ? ray_hash(r[i].o, r[i].d, hp, tag) : KEY_NONE;
 }
 
+// Camera basis of Camera::loadView (E/Camera.cpp:108-133): direction = unit(target - eye) * dist,
+// right = unit(direction x up) * halfW, up = unit(right x direction) * halfH with halfH = 2 dist tan(fov/2)
+// and halfW = halfH * W / H. Evaluated in double and rounded once to float (cam: eye, dir, right, up).
+// Returns 0 for a degenerate camera (eye == target, zero size).
+int orc_camera_look_at(const float eye[3], const float target[3], const float up[3], float fov_degrees,
+                       uint32_t W, uint32_t H, float* cam) {
+    if (W == 0 || H == 0) return 0;
+    double dir[3] = {target[0] - (double)eye[0], target[1] - (double)eye[1], target[2] - (double)eye[2]};
+    const double dist = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    if (!(dist > 0)) return 0;
+    const double half_h = 2.0 * dist * std::tan(0.5 * fov_degrees * 3.14159265358979323846 / 180.0);
+    const double half_w = half_h * (double)W / (double)H;
+    auto unit = [](double* v) {
+        const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (l > 0) for (int i = 0; i < 3; ++i) v[i] /= l;
+    };
+    double f[3] = {dir[0] / dist, dir[1] / dist, dir[2] / dist};
+    double r[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+    unit(r);
+    double u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+    unit(u);
+    for (int i = 0; i < 3; ++i) {
+        cam[i] = eye[i];
+        cam[3 + i] = (float)(f[i] * dist);
+        cam[6 + i] = (float)(r[i] * half_w);
+        cam[9 + i] = (float)(u[i] * half_h);
+    }
+    return 1;
+}
+
 // Camera ray (CUDA-Naive-Ray-Tracer RayTracer.cu:606-607; RayTracer.cu:666-667) in 8x8 tile order.
 void orc_raygen_primary(const float* cam /*eye,dir,right,up*/, uint32_t W, uint32_t H, float* rays_out,
                         uint32_t* pix_out) {
@@ -1153,10 +1183,11 @@ void orc_intersect(void* hp, const float* rays_in, const uint32_t* ids, uint32_t
     }
 }
 
-// Brute force over all triangles (CUDA-Naive-Engine RayTracer.cu:276-291 any-hit, :344-360 closest).
-// pos: original order, 12 floats per triangle. Fills flags (any) or hits (closest) for every ray.
-void orc_brute(const float* pos, uint32_t T, const float* rays_in, uint32_t n, int any, uint32_t* flags,
-               uint64_t* hits) {
+// Brute force over all triangles (CUDA-Naive-Engine RayTracer.cu:276-291 any-hit, :344-360 closest),
+// one triangle after the other with the scalar watertight test. Kept as the plain statement of the
+// semantics; orc_brute gives the same results faster.
+void orc_brute_scalar(const float* pos, uint32_t T, const float* rays_in, uint32_t n, int any, uint32_t* flags,
+                      uint64_t* hits) {
     const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < (int64_t)n; ++i) {
@@ -1179,6 +1210,93 @@ void orc_brute(const float* pos, uint32_t T, const float* rays_in, uint32_t n, i
             }
         }
         if (!any) hits[i] = best;
+    }
+}
+
+// Brute force over all triangles, same results as orc_brute_scalar (every ray against every triangle), in
+// two steps. (1) For a tile of rays and a block of triangles, the watertight test's 2-D edge functions U,
+// V, W are computed in FP32 exactly as wt_hit computes them (same operations, same order, no contraction)
+// over a structure-of-arrays copy of the triangles, in a loop the compiler vectorises; a triangle stays a
+// candidate unless wt_hit would reject it at its sign test with no edge function exactly zero (a zero sends
+// wt_hit to its double-precision fallback, so such a triangle stays a candidate too). (2) Every candidate
+// goes through wt_hit itself. A ray's line crosses few triangles, so (2) is cheap and (1) is the whole
+// cost. pos: original order, 12 floats per triangle. Fills flags (any) or hits (closest) for every ray.
+void orc_brute(const float* pos, uint32_t T, const float* rays_in, uint32_t n, int any, uint32_t* flags,
+               uint64_t* hits) {
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+    constexpr uint32_t TB = 2048;  // triangles per block: 72 KB of the SoA copy, reused by a tile of rays
+    constexpr uint32_t RT = 32;    // rays per tile
+    std::vector<float> soa(9ull * T);
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < (int64_t)T; ++t)
+        for (int v = 0; v < 3; ++v)
+            for (int c = 0; c < 3; ++c) soa[(3ull * v + c) * T + t] = pos[12ull * t + 4 * v + c];
+    const int64_t tiles = ((int64_t)n + RT - 1) / RT;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t tile = 0; tile < tiles; ++tile) {
+        const uint32_t r0 = (uint32_t)tile * RT, r1 = std::min<uint32_t>(n, r0 + RT);
+        RayWT w[RT];
+        uint64_t best[RT];
+        bool live[RT];
+        for (uint32_t i = r0; i < r1; ++i) {
+            const Ray& r = rays[i];
+            live[i - r0] = r.tmax > r.tmin;
+            if (live[i - r0]) w[i - r0] = wt_setup(r);
+            best[i - r0] = HIT_NONE;
+        }
+        alignas(64) uint8_t cand[TB];
+        for (uint32_t b0 = 0; b0 < T; b0 += TB) {
+            const uint32_t nb = std::min<uint32_t>(TB, T - b0);
+            for (uint32_t j = 0; j < r1 - r0; ++j) {
+                if (!live[j]) continue;
+                const RayWT& q = w[j];
+                const float* ax = &soa[(0ull + q.kx) * T + b0];
+                const float* ay = &soa[(0ull + q.ky) * T + b0];
+                const float* az = &soa[(0ull + q.kz) * T + b0];
+                const float* bx = &soa[(3ull + q.kx) * T + b0];
+                const float* by = &soa[(3ull + q.ky) * T + b0];
+                const float* bz = &soa[(3ull + q.kz) * T + b0];
+                const float* cx = &soa[(6ull + q.kx) * T + b0];
+                const float* cy = &soa[(6ull + q.ky) * T + b0];
+                const float* cz = &soa[(6ull + q.kz) * T + b0];
+                const float ox = q.o[q.kx], oy = q.o[q.ky], oz = q.o[q.kz];
+                const float sx = q.s[0], sy = q.s[1];
+                uint32_t any_c = 0;
+#pragma omp simd reduction(| : any_c)
+                for (uint32_t t = 0; t < nb; ++t) {
+                    const float Akz = az[t] - oz, Bkz = bz[t] - oz, Ckz = cz[t] - oz;
+                    const float Ax = (ax[t] - ox) - sx * Akz, Ay = (ay[t] - oy) - sy * Akz;
+                    const float Bx = (bx[t] - ox) - sx * Bkz, By = (by[t] - oy) - sy * Bkz;
+                    const float Cx = (cx[t] - ox) - sx * Ckz, Cy = (cy[t] - oy) - sy * Ckz;
+                    const float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+                    const uint32_t neg = (U < 0.0f) | (V < 0.0f) | (W < 0.0f);
+                    const uint32_t pos_ = (U > 0.0f) | (V > 0.0f) | (W > 0.0f);
+                    const uint32_t zero = (U == 0.0f) | (V == 0.0f) | (W == 0.0f);
+                    const uint32_t c = (1u - (neg & pos_)) | zero;
+                    cand[t] = (uint8_t)c;
+                    any_c |= c;
+                }
+                if (!any_c) continue;
+                for (uint32_t t = 0; t < nb; ++t) {
+                    if (!cand[t]) continue;
+                    const float* v = pos + 12ull * (b0 + t);
+                    float th;
+                    if (wt_hit(q, v, v + 4, v + 8, th)) {
+                        if (any) {
+                            live[j] = false;
+                            best[j] = 0;  // occluded
+                            break;
+                        }
+                        const uint64_t key = hit_key(th, b0 + t);
+                        if (key < best[j]) best[j] = key;
+                    }
+                }
+            }
+        }
+        for (uint32_t i = r0; i < r1; ++i) {
+            if (any) flags[i] = best[i - r0] == 0 ? OCCLUDED : 0u;
+            else hits[i] = best[i - r0];
+        }
     }
 }
 

@@ -499,6 +499,16 @@ int rsh_sm_count(void) {
     return n;
 }
 
+rsh_status rsh_device_memory(uint64_t* free_bytes, uint64_t* total_bytes) {
+    if (!free_bytes || !total_bytes) return RSH_ERR_INVALID;
+    size_t f = 0, t = 0;
+    const cudaError_t e = cudaMemGetInfo(&f, &t);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMemGetInfo");
+    *free_bytes = f;
+    *total_bytes = t;
+    return RSH_OK;
+}
+
 // ------------------------------------------------------------------------------------ hashing
 rsh_status rsh_hash_params_make(const float lo[3], const float hi[3], uint32_t grid_bits,
                                 uint32_t dir_log2, uint32_t tag_bits, rsh_hash_params* out) {

@@ -125,9 +125,11 @@ __global__ void k_level_nodes(const uint32_t* __restrict__ firsts, uint32_t nn, 
 // lo.w = first child as an absolute node index (`child_off` + the level's child-range start; at level 0
 // the first triangle), hi.w = the number of children (triangles), both as raw u32 bits. A single ray
 // that pops a node then loads its children's boxes directly, with no child-range lookup in between.
+// Traversals rely on every node above level 0 having 1 to 8 children; a node outside that range raises
+// RSH_DEVERR_OVERFLOW (its link then covers no child at all or only the first 8).
 __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t* __restrict__ tstart, uint32_t nnodes,
-                                const uint32_t* __restrict__ kids, uint32_t child_off,
-                                float4* __restrict__ sph, float4* __restrict__ box, float pad) {
+                                const uint32_t* __restrict__ kids, uint32_t child_off, bool upper,
+                                float4* __restrict__ sph, float4* __restrict__ box, float pad, uint32_t* err) {
     const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (j >= nnodes) return;
@@ -154,6 +156,7 @@ __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t*
     }
     if (lane == 0) {
         const uint32_t k0 = __ldg(kids + j), k1 = __ldg(kids + j + 1);
+        if (upper && (k1 <= k0 || k1 - k0 > 8u)) raise_device_error(err, RSH_DEVERR_OVERFLOW);
         box[2 * j] = make_float4(mnx - pad, mny - pad, mnz - pad, __uint_as_float(child_off + k0));
         box[2 * j + 1] = make_float4(mxx + pad, mxy + pad, mxz + pad, __uint_as_float(k1 - k0));
     }
@@ -272,8 +275,9 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
                                                        h.kids + total + l, nstart);
         note_launch();
         k_level_spheres<<<(nn * 32 + 127) / 128, 128, 0, s>>>(h.tris, nstart, nn, h.kids + total + l,
-                                                              l == 0 ? 0u : h.level_off[l - 1], h.spheres + total,
-                                                              h.boxes + 2ull * total, box_pad);
+                                                              l == 0 ? 0u : h.level_off[l - 1], l > 0,
+                                                              h.spheres + total, h.boxes + 2ull * total, box_pad,
+                                                              err);
         note_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) break;
         total += nn;

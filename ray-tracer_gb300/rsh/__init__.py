@@ -160,6 +160,7 @@ SIGNATURES = {
     "rsh_event_elapsed": (C.c_int, [_P, _P, _P]),
     "rsh_device_count": (C.c_int, []),
     "rsh_sm_count": (C.c_int, []),
+    "rsh_device_memory": (C.c_int, [_P, _P]),
     "rsh_kernel_launches": (_U64, []),
     "rsh_scene_upload": (C.c_int, [_P, _P, _P]),
     "rsh_scene_set_transforms": (C.c_int, [_P, _P, _P, _P, _U32, _P]),

@@ -158,3 +158,19 @@ def test_png_writer(tmp_path):
     px = rows[:, 1:].reshape(h, w, 4)[::-1].reshape(-1, 4)
     want = img.view(np.uint8).reshape(-1, 4)
     assert np.array_equal(px, want)
+
+
+def test_oracle_camera_and_defaults_match_the_library():
+    """The CPU baseline builds its camera and configuration from the oracle alone (so that it maps no
+    product code); both must equal the library's."""
+    import oracle
+
+    for eye, tgt, up, fov, W, H in (((0, 0, 3.4), (0, 0, 0), (0, 1, 0), 60.0, 512, 256),
+                                     ((-6.0, 5.0, -6.0), (78.0, 3.0, 78.0), (0, 1, 0), 60.0, 1920, 1080),
+                                     ((83.9, -23.4, -78.1), (4.35, -24.35, 1.5), (0, 0.99996, 0), 60.0, 512, 512)):
+        a = rsh.camera_look_at(eye, tgt, up, fov, W, H).as_array()
+        b = oracle.camera_look_at(eye, tgt, up, fov, W, H)
+        assert a.tobytes() == b.tobytes()
+    c = rsh.default_config()
+    for k, v in oracle.DEFAULTS.items():
+        assert getattr(c, k) == pytest.approx(v), k

@@ -289,3 +289,27 @@ def test_watertight_closed_mesh():
     d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
     hits = oracle.brute(pos, _rays(o, d), False)
     assert np.all(hits != oracle.HIT_NONE)
+
+
+def test_blocked_brute_force_equals_scalar_loop():
+    """oracle.brute (sign prefilter over a structure-of-arrays copy, then the exact test on the survivors)
+    gives exactly the scalar loop's results: closest-hit records and shadow flags, for rays from inside and
+    outside the scene, rays with zero direction components (the double-precision fallback) and short
+    intervals."""
+    s = scenes.soup(n_spheres=60, width=8, height=8, extent=6.0)
+    rng = np.random.default_rng(11)
+    n = 3000
+    r = np.zeros(n, oracle.RAY_DTYPE)
+    r["o"] = rng.uniform(-8, 8, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d[: n // 4, rng.integers(0, 3)] = 0.0          # zero components
+    d[n // 4: n // 3] = np.eye(3)[rng.integers(0, 3, n // 3 - n // 4)]  # axis-aligned
+    r["d"] = d / np.linalg.norm(d, axis=1)[:, None]
+    r["tmin"] = 0.0
+    r["tmax"] = np.where(rng.random(n) < 0.5, np.inf, rng.uniform(0.1, 10.0, n))
+    r["tmax"][:7] = -1.0                           # empty slots
+    for any_hit in (False, True):
+        a = oracle.brute(s.positions, r, any_hit)
+        b = oracle.brute(s.positions, r, any_hit, scalar=True)
+        assert np.array_equal(a, b)
+        assert (a != (0 if any_hit else oracle.HIT_NONE)).sum() > n // 10
