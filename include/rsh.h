@@ -304,6 +304,11 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* scene, uint32_t width
                             uint32_t depth, uint32_t* rgba_out, rsh_stream_t stream);
 /* Statistics of the last rsh_render_frame (synchronises the stream it ran on). */
 rsh_status rsh_frame_stats_get(rsh_ctx* ctx, rsh_frame_stats* out);
+/* The context's test counters, accumulated by every traversal and intersection since the last reset
+ * (rsh_render_frame resets them): node tests and ray x triangle tests, the work the reference's
+ * TestManager totals count (TestManager.cpp:276-281). Waits for `stream`; reset != 0 then zeroes them. */
+rsh_status rsh_test_counters(rsh_ctx* ctx, uint64_t* node_tests, uint64_t* tri_tests, int32_t reset,
+                             rsh_stream_t stream);
 /* Device buffers of the last frame, for parity checks: per-bounce closest-hit records and shadow
  * flags. Sizes: width*height and width*height*lights. bounce < depth; bounce -1 = primary hits. */
 rsh_status rsh_frame_hits(rsh_ctx* ctx, int32_t bounce, uint64_t* host_out);

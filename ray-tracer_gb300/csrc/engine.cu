@@ -1248,6 +1248,18 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
     return RSH_OK;
 }
 
+rsh_status rsh_test_counters(rsh_ctx* ctx, uint64_t* node_tests, uint64_t* tri_tests, int32_t reset,
+                             rsh_stream_t stream) {
+    if (!ctx) return RSH_ERR_INVALID;
+    RSH_CUDA(cudaStreamSynchronize(stream));
+    unsigned long long d[2] = {0, 0};
+    RSH_CUDA(cudaMemcpy(d, ctx->d_stats, 16, cudaMemcpyDeviceToHost));
+    if (node_tests) *node_tests = d[0];
+    if (tri_tests) *tri_tests = d[1];
+    if (reset) RSH_CUDA(cudaMemset(ctx->d_stats, 0, 16));
+    return RSH_OK;
+}
+
 rsh_status rsh_frame_stats_get(rsh_ctx* ctx, rsh_frame_stats* out) {
     if (!ctx || !out) return RSH_ERR_INVALID;
     RSH_CUDA(cudaStreamSynchronize(ctx->last_stream));

@@ -160,6 +160,7 @@ SIGNATURES = {
     "rsh_event_elapsed": (C.c_int, [_P, _P, _P]),
     "rsh_device_count": (C.c_int, []),
     "rsh_sm_count": (C.c_int, []),
+    "rsh_test_counters": (C.c_int, [_P, _P, _P, _I32, _P]),
     "rsh_device_memory": (C.c_int, [_P, _P]),
     "rsh_kernel_launches": (_U64, []),
     "rsh_scene_upload": (C.c_int, [_P, _P, _P]),
@@ -532,6 +533,12 @@ class Context:
         n = np.empty((npix, 4), np.float32)
         check(lib().rsh_frame_surface(self.handle, bounce, p.ctypes.data, n.ctypes.data), "rsh_frame_surface")
         return p, n
+
+    def test_counters(self, reset: bool = True, stream=None):
+        """(node tests, ray x triangle tests) accumulated since the last reset."""
+        a, b = C.c_uint64(), C.c_uint64()
+        check(lib().rsh_test_counters(self.handle, C.byref(a), C.byref(b), int(reset), stream), "rsh_test_counters")
+        return a.value, b.value
 
     def check_device_errors(self, stream=None):
         check(lib().rsh_check_device_errors(self.handle, stream), "device error word")

@@ -5,7 +5,7 @@ shading of the same buffers within 2/255 per channel (host and device powf / log
 import numpy as np
 import pytest
 
-import oracle
+import frame_check
 import rsh
 from rsh import scenes
 
@@ -13,68 +13,8 @@ pytestmark = pytest.mark.gpu
 
 
 def _check_frame(ctx, s, sc, W, H, depth, jitter, samples=1):
-    lights = s.lights
-    L = len(lights)
-    LS = L * samples
-    cam = rsh.camera_look_at(s.eye, s.target, s.up, s.fov, W, H)
-    ctx.set_camera(cam)
-    ctx.set_lights(lights)
-    rgba = rsh.DeviceArray(W * H, np.uint32)
-    ctx.render(sc, W, H, depth, rgba)
-    ctx.check_device_errors()
-    st = ctx.stats()
-    npix = W * H
-    lo, hi = sc.bounds()
-    g, b = ctx.config.grid_bits, ctx.config.dir_log2
-    scale = oracle.hash_scale(lo, hi, g)
-    # primary
-    prays, pix = oracle.raygen_primary(cam.as_array(), W, H)
-    assert ctx.frame_rays(-1, False, len(prays)).tobytes() == prays.tobytes()
-    bf = oracle.brute(s.positions, prays, False)
-    ph = ctx.frame_hits(-1, npix)
-    want = np.zeros(npix, np.uint64)
-    want[pix[pix != 0xFFFFFFFF]] = bf[pix != 0xFFFFFFFF]
-    assert np.array_equal(ph, want)
-    spos, snrm = ctx.frame_surface(-1, npix)
-    ospos, osnrm = oracle.resolve(s.positions, s.normals, s.material_ids, prays, bf, pix, npix)
-    assert spos.tobytes() == ospos.tobytes() and snrm.tobytes() == osnrm.tobytes()
-    prev = None
-    lp = np.array([l["position"] for l in lights], np.float32)
-    nshadow = nrefl = 0
-    accum = np.zeros((npix, 4), np.float32)
-    eye = cam.as_array()[:3]
-    for bnc in range(depth):
-        srays = ctx.frame_rays(bnc, True, npix * LS)
-        orays, okeys = oracle.raygen_shadow(spos, snrm, W, H, lp, ctx.config.epsilon, lo, scale, g, b, samples)
-        v = okeys != oracle.KEY_NONE
-        nshadow += int(v.sum())
-        assert srays[v].tobytes() == orays[v].tobytes()
-        sflags = ctx.frame_shadow(bnc, npix * LS)
-        assert np.array_equal(sflags[v], oracle.brute(s.positions, orays[v], True))
-        assert np.all(sflags[~v] == 0)
-        oracle.shade(spos, snrm, s.materials, sflags, accum, W, H, lights, eye, bnc, prev, samples)
-        rrays = ctx.frame_rays(bnc, False, npix)
-        o_r, o_k = oracle.raygen_reflect(spos, snrm, prev, cam.as_array()[:3] if prev is None else None, W, H,
-                                         ctx.config.epsilon, jitter, ctx.config.seed, bnc, lo, scale, g, b)
-        v = o_k != oracle.KEY_NONE
-        nrefl += int(v.sum())
-        assert rrays[v].tobytes() == o_r[v].tobytes()
-        rh = ctx.frame_hits(bnc, npix)
-        bfr = oracle.brute(s.positions, o_r[v], False)
-        assert np.array_equal(rh[v], bfr)
-        assert np.all(rh[~v] == oracle.HIT_NONE)
-        spos2, snrm2 = ctx.frame_surface(bnc, npix)
-        o2p, o2n = oracle.resolve(s.positions, s.normals, s.material_ids, rrays, rh, None, npix)
-        assert spos2.tobytes() == o2p.tobytes() and snrm2.tobytes() == o2n.tobytes()
-        spos, snrm, prev = spos2, snrm2, rrays
-    assert st["shadow_rays"] == nshadow and st["reflection_rays"] == nrefl
-    img = rgba.numpy()
-    assert np.any(img & 0xFFFFFF)  # something was lit
-    # the last reflection surface is shaded once more, unshadowed, then packed
-    oracle.shade(spos, snrm, s.materials, None, accum, W, H, lights, eye, depth, prev, samples)
-    want = oracle.pack(accum)
-    diff = np.abs(img.view(np.uint8).reshape(-1, 4).astype(np.int32) - want.view(np.uint8).reshape(-1, 4))
-    assert diff.max() <= 2, diff.max()
+    """Every ray of the frame against the oracle (frame_check.check_frame with no sampling)."""
+    st, _ = frame_check.check_frame(ctx, s, sc, W, H, depth, jitter, samples=samples)
     return st
 
 
@@ -149,6 +89,18 @@ def test_rah_ablation_same_results_more_work(cornell, ray_level):
         assert np.array_equal(a, b)
     if ray_level == 0:
         assert res[rsh.FLAG_RAH][1]["node_tests"] > res[0][1]["node_tests"]
+
+
+@pytest.mark.parametrize("ray_level", [0, 3])
+def test_frame_rah_against_the_oracle(cornell, ray_level):
+    """RAH frames (unsorted packets) pass the whole stage-by-stage check: every hit and flag equals brute
+    force, not only the CRSH frame's."""
+    ctx = rsh.Context(grid_bits=5, dir_log2=5, packet_size=8, cluster_size=8, flags=rsh.FLAG_RAH,
+                      reflect_jitter=1.0, ray_level=ray_level, plain_ray_level=ray_level)
+    sc = ctx.scene(cornell.positions, cornell.normals, cornell.material_ids, cornell.materials)
+    _check_frame(ctx, cornell, sc, 128, 96, 2, 1.0)
+    sc.destroy()
+    ctx.destroy()
 
 
 @pytest.mark.parametrize("flags", [0, rsh.FLAG_FUSED])
