@@ -83,6 +83,8 @@ def lib():
             "orc_traverse": (U64, [P, P, U32, U32, U32, P, U64, P]),
             "orc_intersect": (None, [P, P, P, U32, U32, P, U64, I, P, P]),
             "orc_brute": (None, [P, U32, P, U32, I, P, P]),
+            "orc_trace_rays_box": (I, [P, P, U32, I, P, P, P, P]),
+            "orc_objh_boxes": (None, [P, P]),
             "orc_brute_scalar": (None, [P, U32, P, U32, I, P, P]),
             "orc_brute_second": (None, [P, U32, P, U32, P, P]),
             "orc_resolve": (None, [P, P, P, P, P, P, U32, P, P]),
@@ -308,6 +310,27 @@ class ObjH:
         R = lib().orc_trace_keyed(self.h, _p(rays), _p(keys), n, key_bits, P, int(any_hit), _p(flags), _p(hits),
                                   _p(ms), _p(ctr), ray_level)
         return (flags if any_hit else hits), int(R), ms, ctr
+
+    def boxes(self) -> np.ndarray:
+        """Per node (levels concatenated): padded box lo xyz, link, hi xyz, count; link and count as u32 bits."""
+        out = np.empty((max(sum(self.levels()), 1), 8), np.float32)
+        lib().orc_objh_boxes(self.h, _p(out))
+        return out[: sum(self.levels())]
+
+    def trace_box(self, rays, any_hit, per_ray=False):
+        """Per-ray box descent from the root (the batched form's rays-only traversal): flags or hits, the
+        (node tests, triangle tests) totals and, with per_ray, the counts of every ray ([n, 2] u32)."""
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        n = len(rays)
+        flags = np.zeros(n, np.uint32)
+        hits = np.full(n, HIT_NONE, np.uint64)
+        pr = np.zeros((n, 2), np.uint32) if per_ray else None
+        ctr = np.zeros(2, np.uint64)
+        ok = lib().orc_trace_rays_box(self.h, _p(rays), n, int(any_hit), _p(flags), _p(hits), _p(pr), _p(ctr))
+        if not ok:
+            raise OverflowError("job stack overflow")
+        out = flags if any_hit else hits
+        return (out, (int(ctr[0]), int(ctr[1])), pr) if per_ray else (out, (int(ctr[0]), int(ctr[1])))
 
     def __del__(self):
         try:

@@ -363,6 +363,10 @@ struct ObjH {
                                  // (level 0: the cluster's triangles)
     std::vector<float> tris;     // 12 per triangle, cluster order, w of vertex 0 = original id bits
     std::vector<uint32_t> order;
+    // per node (absolute index off[l] + j): padded box lo xyz, link, hi xyz, count (8 floats). The link
+    // is the first child's absolute node index (level 0: the cluster's first triangle) and the count its
+    // children (triangles), both as raw u32 bits in the w words
+    std::vector<float> box;
 };
 
 // children of node (L, idx) at level L-1 (L == levels: the virtual root over the top level)
@@ -458,6 +462,103 @@ bool ray_descend(const ObjH& h, const Ray& r, const RayWT& w, uint32_t L0, uint3
         }
     }
     return false;
+}
+
+// Ray vs a padded node box over [tmin, tmax] (fused.cu box_hit_fma): per plane t = fma(b, inv, -(o * inv))
+// with inv the IEEE reciprocal of the direction component, components below 1e-20 in magnitude replaced by
+// +-1e-20; entry distance tn = max(tmin, per-axis minima), exit = min(tmax, per-axis maxima). tn is the
+// nearest-first order key.
+inline float safe_rcp(float d) {
+    const float m = 1e-20f;
+    return 1.0f / (std::fabs(d) < m ? std::copysign(m, d) : d);
+}
+inline bool box_hit(const float* b, const float inv[3], const float oi[3], float tmin, float tmax, float& tn) {
+    const float ax = std::fma(b[0], inv[0], -oi[0]), bx = std::fma(b[4], inv[0], -oi[0]);
+    const float ay = std::fma(b[1], inv[1], -oi[1]), by = std::fma(b[5], inv[1], -oi[1]);
+    const float az = std::fma(b[2], inv[2], -oi[2]), bz = std::fma(b[6], inv[2], -oi[2]);
+    tn = std::fmax(std::fmax(std::fmax(tmin, std::fmin(ax, bx)), std::fmin(ay, by)), std::fmin(az, bz));
+    const float tf = std::fmin(std::fmin(std::fmin(tmax, std::fmax(ax, bx)), std::fmax(ay, by)), std::fmax(az, bz));
+    return tn <= tf;
+}
+
+// One ray from the root of the object tree by node boxes: the batched form's rays-only traversal (fused.cu
+// k_fused_rays, run_jobs with one job per ray). A stack entry is a triangle cluster (its index) or a node
+// (level << 27 | (children - 1) << 24 | absolute index of its first child, from the link in the node's box).
+// A node step tests every child's box against [tmin, current best] and pushes the hits: any hit in child
+// order (the last child pops first), closest hit farthest first (the nearest pops first; among equal entry
+// distances the lower child). A cluster step tests the cluster's box, then its triangles. Counts node
+// tests (every child of a popped node) and triangle tests. Returns false on a stack overflow.
+bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint64_t& best, uint64_t& ntests,
+                     uint64_t& ttests) {
+    occluded = false;
+    best = HIT_NONE;
+    if (!(r.tmax > r.tmin) || h.levels == 0) return true;
+    const RayWT w = wt_setup(r);
+    const float inv[3] = {safe_rcp(r.d[0]), safe_rcp(r.d[1]), safe_rcp(r.d[2])};
+    const float oi[3] = {r.o[0] * inv[0], r.o[1] * inv[1], r.o[2] * inv[2]};
+    float tcur = r.tmax;
+    uint32_t stk[96];
+    int sp = 0;
+    const uint32_t top = h.levels, tcnt = h.size[top - 1];
+    if (tcnt == 0 || tcnt > 8) return false;
+    stk[sp++] = (top << 27) | ((tcnt - 1) << 24) | h.off[top - 1];
+    while (sp > 0) {
+        const uint32_t e = stk[--sp];
+        const uint32_t L = e >> 27, idx = e & 0xFFFFFFu;
+        if (L == 0) {
+            const float* b = &h.box[8ull * idx];
+            float tn;
+            if (!box_hit(b, inv, oi, r.tmin, tcur, tn)) continue;
+            const uint32_t t0 = f2u(b[3]), t1 = t0 + f2u(b[7]);
+            for (uint32_t t = t0; t < t1; ++t) {
+                const float* v = &h.tris[12ull * t];
+                float th;
+                ++ttests;
+                if (wt_hit(w, v, v + 4, v + 8, th)) {
+                    if (any) {
+                        occluded = true;
+                        return true;
+                    }
+                    const uint64_t key = hit_key(th, f2u(v[3]));
+                    if (key < best) {
+                        best = key;
+                        tcur = std::fmin(tcur, th);
+                    }
+                }
+            }
+            continue;
+        }
+        const uint32_t cl = L - 1, cnt = ((e >> 24) & 7u) + 1u;
+        ntests += cnt;
+        float tcs[8];
+        uint32_t hm = 0;
+        for (uint32_t c = 0; c < cnt; ++c) {
+            float tc;
+            tcs[c] = 0.0f;
+            if (box_hit(&h.box[8ull * (idx + c)], inv, oi, r.tmin, tcur, tc)) {
+                hm |= 1u << c;
+                tcs[c] = tc;
+            }
+        }
+        if (sp + __builtin_popcount(hm) > 96) return false;
+        while (hm) {
+            uint32_t bc = 0;
+            if (!any) {
+                float bt = -INF;
+                for (uint32_t c = 0; c < 8; ++c)
+                    if (((hm >> c) & 1u) && tcs[c] >= bt) {
+                        bt = tcs[c];
+                        bc = c;
+                    }
+            } else {
+                bc = (uint32_t)__builtin_ctz(hm);
+            }
+            hm &= ~(1u << bc);
+            const float* cb = &h.box[8ull * (idx + bc)];
+            stk[sp++] = cl == 0 ? idx + bc : (cl << 27) | ((f2u(cb[7]) - 1u) << 24) | (f2u(cb[3]) & 0xFFFFFFu);
+        }
+    }
+    return true;
 }
 
 }  // namespace
@@ -1029,6 +1130,11 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
         if (n <= 8 || h.levels >= 16) break;
     }
     h.sph.assign(4ull * total_nodes, 0.0f);
+    h.box.assign(8ull * total_nodes, 0.0f);
+    // boxes are widened by 1e-5 of the scene's largest coordinate magnitude (objh.cu)
+    float smax = 0.0f;
+    for (int a = 0; a < 3; ++a) smax = std::fmax(smax, std::fmax(std::fabs(lo[a]), std::fabs(hi[a])));
+    const float pad = 1e-5f * smax + 1e-30f;
     h.kid.assign(total_kids, 0u);
     for (uint32_t l = 0; l < h.levels; ++l) {
         // level 0 stores the clusters' triangle ranges, higher levels their child ranges
@@ -1056,6 +1162,16 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
             s[1] = c.y;
             s[2] = c.z;
             s[3] = std::sqrt(r2) * kRadSlack;
+            // the padded box and child link (objh.cu k_level_spheres)
+            const uint32_t* k = &h.kid[h.koff[l] + j];
+            const uint32_t child_off = (l == 0) ? 0u : h.off[l - 1];
+            float* bx = &h.box[8ull * (h.off[l] + j)];
+            for (int i = 0; i < 3; ++i) {
+                bx[i] = mn[i] - pad;
+                bx[4 + i] = mx[i] + pad;
+            }
+            bx[3] = u2f(child_off + k[0]);
+            bx[7] = u2f(k[1] - k[0]);
         }
     }
 }
@@ -1101,6 +1217,10 @@ void* orc_objh_build(const float* pos, uint32_t T, uint32_t cluster, const float
     return h;
 }
 void orc_objh_free(void* hp) { delete static_cast<ObjH*>(hp); }
+void orc_objh_boxes(void* hp, float* out) {
+    const ObjH& h = *static_cast<ObjH*>(hp);
+    std::memcpy(out, h.box.data(), 4ull * h.box.size());
+}
 uint32_t orc_objh_levels(void* hp) { return static_cast<ObjH*>(hp)->levels; }
 uint32_t orc_objh_level_size(void* hp, uint32_t l) { return static_cast<ObjH*>(hp)->size[l]; }
 // child ranges of every level, level after level (size[l] + 1 entries each; level 0: triangle ranges)
@@ -1181,6 +1301,37 @@ void orc_intersect(void* hp, const float* rays_in, const uint32_t* ids, uint32_t
             }
         }
     }
+}
+
+// Traces rays by per-ray box descent from the root (the batched form's rays-only traversal, fused.cu
+// k_fused_rays) on all host threads. Outputs per ray: flags (any) or hits (closest); per_ray (nullable)
+// gets node tests and triangle tests per ray (2 x u32). counters = total node tests, triangle tests.
+// Returns 0 on a job-stack overflow (the GPU raises RSH_DEVERR_OVERFLOW there), else 1.
+int orc_trace_rays_box(void* hp, const float* rays_in, uint32_t n, int any, uint32_t* flags, uint64_t* hits,
+                       uint32_t* per_ray, uint64_t* counters) {
+    const ObjH& h = *static_cast<ObjH*>(hp);
+    const Ray* rays = reinterpret_cast<const Ray*>(rays_in);
+    uint64_t nt = 0, tt = 0;
+    int ok = 1;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : nt, tt) reduction(& : ok)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        bool occ = false;
+        uint64_t best = HIT_NONE, a = 0, b = 0;
+        if (!ray_descend_box(h, rays[i], any != 0, occ, best, a, b)) ok = 0;
+        if (any) flags[i] = occ ? OCCLUDED : 0u;
+        else hits[i] = best;
+        if (per_ray) {
+            per_ray[2 * i] = (uint32_t)a;
+            per_ray[2 * i + 1] = (uint32_t)b;
+        }
+        nt += a;
+        tt += b;
+    }
+    if (counters) {
+        counters[0] = nt;
+        counters[1] = tt;
+    }
+    return ok;
 }
 
 // Brute force over all triangles (CUDA-Naive-Engine RayTracer.cu:276-291 any-hit, :344-360 closest),

@@ -116,9 +116,7 @@ RSH_DEV bool box_hit(float4 b0, float4 b1, float ox, float oy, float oz, float i
     return tn <= tf;
 }
 
-// SOLO: every ray has exactly one job (rays-only form), so no other lane shares its best hit: the shared
-// state is not re-read each step and the best hit is stored once, when the job ends.
-template <int P, bool SOLO = false, class SM>
+template <int P, class SM>
 RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsigned long long& ntests,
                       unsigned long long& ttests, uint32_t* err) {
     const float4* __restrict__ boxes = sg.boxes;
@@ -189,8 +187,7 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
         }
         if (!has) continue;
         // what other jobs of this ray found so far
-        if (SOLO) {
-        } else if (any) {
+        if (any) {
             if (*(volatile uint32_t*)&S.meta[i] & 128u) sp = 0;
         } else {
             const unsigned long long b = *(volatile unsigned long long*)&S.best[i];
@@ -225,7 +222,7 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                         if (key < best) {
                             best = key;
                             tcur = fminf(tcur, th);
-                            if (!SOLO) atomicMin(&S.best[i], key);
+                            atomicMin(&S.best[i], key);
                         }
                     }
                 }
@@ -274,10 +271,7 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                 }
             }
         }
-        if (sp == 0) {
-            if (SOLO && !any) S.best[i] = best;
-            has = false;
-        }
+        if (sp == 0) has = false;
     }
     __syncwarp();
     if (lane == 0) S.qn = 0;
@@ -578,20 +572,43 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
     }
 }
 
-// Rays-only form: every segment's switch level is at or above its tree's depth, so a ray leaves its packet
-// at the root. No packet phase: a warp stages its unit's rays and queues one root job per active ray.
-// The shared footprint is the per-ray state and a queue of one unit (so more warps fit per SM).
-template <int P>
-struct RaySmem {
-    float4 ro[8 * P];
-    float4 rs[8 * P];
-    float4 rd[8 * P];
-    uint32_t meta[8 * P];
-    uint32_t slot[8 * P];
-    unsigned long long best[8 * P];
-    uint32_t jobs[8 * P];
-    uint32_t qn;
-};
+// Rays-only form: every segment's switch level is at or above its tree's depth, so every ray is one job
+// from the root and no lane ever shares a ray. The warp keeps no per-unit state: it takes work units
+// (RSH_RAYS_UNIT sorted rays, never straddling a segment) by atomic ticket, and every lane whose ray has
+// finished takes the next ray of the warp's current unit straight from global memory (its id from the
+// sorted order, the ray itself from the segment's array), fetching the next unit when the current one runs
+// out. So lanes are refilled continuously and no lane waits for the slowest ray of a unit; a lane writes its
+// ray's result (shadow flag or hit record) itself when the ray ends. The launch's last units go out as
+// pieces of RSH_RAYS_UNIT / RSH_TAIL_SPLIT rays.
+//
+// Box test (box_hit_fma): t = b * (1 / d) - o * (1 / d) as one fused multiply-add per plane, with direction
+// components below 1e-20 in magnitude replaced by +-1e-20 (finite reciprocals, no inf - inf), and the
+// entry / exit distances reduced with three-input min / max. The change of rounding against (b - o) / d is
+// about one ulp of the coordinates, far below the boxes' padding (1e-5 of the scene's largest coordinate),
+// so the cull stays conservative; the triangle tests alone decide every hit.
+RSH_DEV float fmax3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+RSH_DEV float fmin3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+RSH_DEV float safe_rcp(float d) {
+    const float m = 1e-20f;
+    return __frcp_rn(fabsf(d) < m ? copysignf(m, d) : d);
+}
+RSH_DEV bool box_hit_fma(float4 b0, float4 b1, float ix, float iy, float iz, float oix, float oiy, float oiz,
+                         float tmin, float tmax, float& tn) {
+    const float ax = __fmaf_rn(b0.x, ix, -oix), bx = __fmaf_rn(b1.x, ix, -oix);
+    const float ay = __fmaf_rn(b0.y, iy, -oiy), by = __fmaf_rn(b1.y, iy, -oiy);
+    const float az = __fmaf_rn(b0.z, iz, -oiz), bz = __fmaf_rn(b1.z, iz, -oiz);
+    tn = fmaxf(fmax3f(tmin, fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
+    const float tf = fminf(fmin3f(tmax, fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
+    return tn <= tf;
+}
 
 #ifndef RSH_RAYS_MIN_BLOCKS
 #define RSH_RAYS_MIN_BLOCKS 8
@@ -603,71 +620,181 @@ struct RaySmem {
 #define RSH_TAIL_SPLIT 2
 #endif
 
-template <int P>
+template <int U>
 __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(FusedArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    RaySmem<P>& S = reinterpret_cast<RaySmem<P>*>(smem_raw)[threadIdx.x >> 5];
     const uint32_t lane = lane_id();
     const uint32_t units = dev_count(a.d_units, a.units_max);
-    unsigned long long ntests = 0, ttests = 0;
-    constexpr uint32_t R = 8 * P;
-    // the launch's tail: the last units (RSH_TAIL_PER_WARP per warp of the grid) go out in pieces of
-    // R / RSH_TAIL_SPLIT rays, so that no warp is left with a whole expensive unit after the others ran out
     const uint32_t tail = min(units, (uint32_t)RSH_TAIL_PER_WARP * gridDim.x * FW);
     const uint32_t head = units - tail, tickets = head + RSH_TAIL_SPLIT * tail;
-    if (lane == 0) S.qn = 0;
-    __syncwarp();
+    unsigned long long ntests = 0, ttests = 0;
+    // the warp's current unit: sorted rays [nk, nend) of segment cs
+    uint32_t nk = 0, nend = 0, cs = 0;
+    bool drained = false;
+    // the lane's ray
+    bool has = false, any = false;
+    uint32_t seg = 0, slot = 0;
+    const float4* __restrict__ boxes = nullptr;
+    const float4* __restrict__ tris = nullptr;
+    int sp = 0;
+    uint32_t stk[J_STACK];
+    float ox = 0.f, oy = 0.f, oz = 0.f, tmin = 0.f, tcur = 0.f;
+    float ix = 0.f, iy = 0.f, iz = 0.f, oix = 0.f, oiy = 0.f, oiz = 0.f;
+    RayWT w;
+    unsigned long long best = RSH_HIT_NONE;
     for (;;) {
-        uint32_t t = 0;
-        if (lane == 0) t = atomicAdd(&a.work[0], 1u);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= tickets) break;
-        uint32_t u = t, lo = 0, hi = R;
-        if (t >= head) {
-            const uint32_t h = t - head;
-            u = head + h / RSH_TAIL_SPLIT;
-            lo = (h % RSH_TAIL_SPLIT) * (R / RSH_TAIL_SPLIT);
-            hi = lo + R / RSH_TAIL_SPLIT;
+        // idle lanes take the next rays of the warp's unit, units are fetched as they run out
+        for (;;) {
+            const uint32_t need = __ballot_sync(0xffffffffu, !has);
+            if (!need) break;
+            if (nk >= nend) {
+                if (drained) break;
+                uint32_t t = 0;
+                if (lane == 0) t = atomicAdd(&a.work[0], 1u);
+                t = __shfl_sync(0xffffffffu, t, 0);
+                if (t >= tickets) {
+                    drained = true;
+                    break;
+                }
+                uint32_t u = t, lo = 0, hi = U;
+                if (t >= head) {
+                    const uint32_t h = t - head;
+                    u = head + h / RSH_TAIL_SPLIT;
+                    lo = (h % RSH_TAIL_SPLIT) * (U / RSH_TAIL_SPLIT);
+                    hi = lo + U / RSH_TAIL_SPLIT;
+                }
+                nk = u * U + lo;
+                nend = u * U + hi;
+                cs = find_segment(a.segs, a.nseg, u);
+            }
+            const uint32_t k = nk + __popc(need & lanemask_lt());
+            if (!has && k < nend) {
+                // no sorted order: the rays' own order, padded past ordered_n
+                const uint32_t id = a.sorted_ids ? __ldg(a.sorted_ids + k) : (k < a.ordered_n ? k : INVALID_ID);
+                if (id != INVALID_ID) {
+                    const FusedSeg& sg = a.segs[cs];
+                    float4 o, d;
+                    load_ray(sg.rays, id - sg.slot_base, o, d);
+                    if (d.w > o.w) {
+                        if (sg.levels == 0u) {
+                            // a scene without triangles has no tree: the ray misses
+                            if (sg.any_hit) sg.flags[id - sg.slot_base] = 0u;
+                            else sg.hits[id - sg.slot_base] = RSH_HIT_NONE;
+                        } else {
+                            seg = cs;
+                            slot = id - sg.slot_base;
+                            any = sg.any_hit != 0u;
+                            boxes = sg.boxes;
+                            tris = sg.tris;
+                            ox = o.x;
+                            oy = o.y;
+                            oz = o.z;
+                            tmin = o.w;
+                            tcur = d.w;
+                            ix = safe_rcp(d.x);
+                            iy = safe_rcp(d.y);
+                            iz = safe_rcp(d.z);
+                            oix = ox * ix;
+                            oiy = oy * iy;
+                            oiz = oz * iz;
+                            w = wt_setup(o, d);
+                            best = RSH_HIT_NONE;
+                            stk[0] = job_entry(sg, boxes, sg.levels, 0u, a.err);
+                            sp = 1;
+                            has = true;
+                        }
+                    }
+                }
+            }
+            nk = min(nend, nk + __popc(need));
         }
-        const uint32_t sidx = find_segment(a.segs, a.nseg, u);
-        const FusedSeg& sg = a.segs[sidx];
-        const bool any = sg.any_hit != 0;
-        uint32_t qn = 0;
-        for (uint32_t base = 0; base < R; base += 32) {
-            const uint32_t i = base + lane;
-            const uint32_t k = u * R + i;  // no sorted order: the rays' own order, padded past ordered_n
-            const bool mine = i >= lo && i < hi;
-            const uint32_t id = !mine ? INVALID_ID
-                                      : a.sorted_ids ? __ldg(a.sorted_ids + k) : (k < a.ordered_n ? k : INVALID_ID);
-            float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, -1.f);
-            if (id != INVALID_ID) load_ray(sg.rays, id - sg.slot_base, o, d);
-            const bool active = (id != INVALID_ID) && (d.w > o.w);
-            const RayWT w = wt_setup(o, d);
-            S.ro[i] = o;
-            S.rs[i] = make_float4(w.sx, w.sy, w.sz, d.w);
-            S.rd[i] = d;
-            S.meta[i] = (uint32_t)w.kx | ((uint32_t)w.ky << 2) | ((uint32_t)w.kz << 4) | (active ? 64u : 0u);
-            S.slot[i] = id;
-            S.best[i] = RSH_HIT_NONE;
-            // a scene without triangles has no tree: its rays keep the prefilled miss
-            const bool job = active && sg.levels > 0u;
-            const uint32_t bl = __ballot_sync(0xffffffffu, job);
-            if (job) S.jobs[qn + __popc(bl & lanemask_lt())] = job_word(i, sg.levels, 0u);
-            qn += __popc(bl);
+        if (!__any_sync(0xffffffffu, has)) break;  // nothing in flight and nothing left to fetch
+        // one kind of step per iteration, the kind more lanes want
+        bool do_nodes;
+        {
+            const bool node = has && (stk[sp - 1] >> E_LSHIFT) != 0u;
+            const uint32_t nn = __popc(__ballot_sync(0xffffffffu, node));
+            const uint32_t nc = __popc(__ballot_sync(0xffffffffu, has && !node));
+            do_nodes = nn >= nc;
         }
-        __syncwarp();
-        if (lane == 0) S.qn = qn;
-        __syncwarp();
-        if (qn) run_jobs<P, true>(S, sg, any, lane, ntests, ttests, a.err);
-        __syncwarp();
-        for (uint32_t i = lane; i < R; i += 32) {
-            const uint32_t meta = S.meta[i];
-            if (!(meta & 64u)) continue;
-            const uint32_t slot = S.slot[i] - sg.slot_base;
-            if (any) sg.flags[slot] = (meta & 128u) ? RSH_OCCLUDED : 0u;
-            else sg.hits[slot] = S.best[i];
+        if (has && ((stk[sp - 1] >> E_LSHIFT) != 0u) == do_nodes) {
+            const uint32_t e = stk[--sp];
+            const uint32_t L = e >> E_LSHIFT, idx = e & 0xFFFFFFu;
+            if (L == 0u) {
+                // the cluster's box against [tmin, current best]; a miss skips its triangles
+                const float4 b0 = __ldg(boxes + 2ull * idx), b1 = __ldg(boxes + 2ull * idx + 1);
+                const uint32_t t0 = __float_as_uint(b0.w);  // the cluster's triangles: its box's link
+                uint32_t t1 = t0 + __float_as_uint(b1.w);
+                float tnb;
+                if (!box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tnb)) t1 = t0;
+                for (uint32_t tt = t0; tt < t1; ++tt) {
+                    const float4 v0 = __ldg(tris + 3ull * tt), v1 = __ldg(tris + 3ull * tt + 1),
+                                 v2 = __ldg(tris + 3ull * tt + 2);
+                    float th;
+                    ++ttests;
+                    if (wt_hit(w, v0, v1, v2, th)) {
+                        if (any) {
+                            best = 0ull;  // occluded
+                            sp = 0;
+                            break;
+                        }
+                        const unsigned long long key = hit_key(th, __float_as_uint(v0.w));
+                        if (key < best) {
+                            best = key;
+                            tcur = fminf(tcur, th);
+                        }
+                    }
+                }
+            } else {
+                const uint32_t cl = L - 1u;
+                // the entry holds the children's link: up to 8 boxes from absolute node `idx` on
+                const uint32_t cnt = ((e >> 24) & 7u) + 1u;
+                const float4* bb = boxes + 2ull * idx;
+                ntests += cnt;
+                float tcs[8];
+                uint32_t hm = 0;
+#pragma unroll
+                for (uint32_t c = 0; c < 8; ++c) {
+                    tcs[c] = 0.0f;
+                    if (c < cnt) {
+                        float tc;
+                        const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
+                        if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc)) {
+                            hm |= 1u << c;
+                            tcs[c] = tc;
+                        }
+                    }
+                }
+                if (sp + __popc(hm) > J_STACK) {
+                    raise_device_error(a.err, RSH_DEVERR_OVERFLOW);
+                    hm = 0;
+                }
+                // hits pushed farthest first (closest hit: the nearest pops first), in child order (any)
+                while (hm) {
+                    uint32_t bc = 0;
+                    if (!any) {
+                        float bt = -INFINITY;
+#pragma unroll
+                        for (uint32_t c = 0; c < 8; ++c)
+                            if (((hm >> c) & 1u) && tcs[c] >= bt) {
+                                bt = tcs[c];
+                                bc = c;
+                            }
+                    } else {
+                        bc = __ffs(hm) - 1u;
+                    }
+                    hm &= ~(1u << bc);
+                    // a child node's own link, from the box just tested (an L1 hit)
+                    stk[sp++] = cl == 0u ? idx + bc : child_entry(cl, __ldg(&bb[2 * bc].w), __ldg(&bb[2 * bc + 1].w));
+                }
+            }
+            if (sp == 0) {
+                // the ray is done: its result, written by its own lane
+                const FusedSeg& sg = a.segs[seg];
+                if (any) sg.flags[slot] = best == 0ull ? RSH_OCCLUDED : 0u;
+                else sg.hits[slot] = best;
+                has = false;
+            }
         }
-        __syncwarp();
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -680,28 +807,25 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     }
 }
 
-template <int P>
-static cudaError_t launch_fused_rays_p(const FusedArgs& a, cudaStream_t s) {
-    const size_t smem = sizeof(RaySmem<P>) * FW;
-    cudaError_t e = cudaFuncSetAttribute(k_fused_rays<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+template <int U>
+static cudaError_t launch_fused_rays_u(const FusedArgs& a, cudaStream_t s) {
     int dev = 0, sms = 152, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays<P>, FW * 32, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays<U>, FW * 32, 0);
     if (per_sm < 1) per_sm = 1;
     if (a.blocks_per_sm && (int)a.blocks_per_sm < per_sm) per_sm = (int)a.blocks_per_sm;
     uint32_t grid = (uint32_t)(sms * per_sm);
     const uint32_t need = (a.units_max + FW - 1) / FW;
     if (need < grid) grid = need > 0 ? need : 1;
-    k_fused_rays<P><<<grid, FW * 32, smem, s>>>(a);
+    k_fused_rays<U><<<grid, FW * 32, 0, s>>>(a);
     note_launch();
     return cudaGetLastError();
 }
 
 template <int P>
 static cudaError_t launch_fused_p(const FusedArgs& a, cudaStream_t s) {
-    if (a.rays_only) return launch_fused_rays_p<RSH_RAYS_UNIT / 8>(a, s);  // units of RSH_RAYS_UNIT rays
+    if (a.rays_only) return launch_fused_rays_u<RSH_RAYS_UNIT>(a, s);  // units of RSH_RAYS_UNIT rays
     const size_t smem = sizeof(FusedSmem<P>) * FW;
     cudaError_t e = cudaFuncSetAttribute(k_fused<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

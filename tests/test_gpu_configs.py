@@ -17,6 +17,7 @@ import numpy as np
 import pytest
 
 import frame_check
+import oracle
 import rsh
 from rsh import scenes
 
@@ -36,6 +37,18 @@ def _both_forms(name, sample):
         st, checked = frame_check.check_frame(ctx, s, sc, s.width, s.height, s.depth, float(s.jitter),
                                               sample=sample, seed=0x5EED0000, cache=cache)
         out[form] = (st, checked)
+    # the batched form's work counters (the roofline's numerator) equal the oracle's restatement of its
+    # traversal (per-ray box descent from the root) over the frame's own secondary rays, test for test
+    lo, hi = sc.bounds()
+    oh = oracle.ObjH(s.positions, ctx.config.cluster_size, lo, hi)
+    npix, L = s.width * s.height, len(s.lights)
+    nodes = tris = 0
+    for b in range(s.depth):
+        for rays, any_hit in ((ctx.frame_rays(b, True, npix * L), True), (ctx.frame_rays(b, False, npix), False)):
+            _, (n, t) = oh.trace_box(rays[rays["tmax"] > rays["tmin"]], any_hit)
+            nodes, tris = nodes + n, tris + t
+    st = out["batched"][0]
+    assert (st["node_tests"], st["tri_tests"]) == (nodes, tris)
     sc.destroy()
     ctx.destroy()
     # both forms trace the same rays

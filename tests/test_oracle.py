@@ -313,3 +313,39 @@ def test_blocked_brute_force_equals_scalar_loop():
         b = oracle.brute(s.positions, r, any_hit, scalar=True)
         assert np.array_equal(a, b)
         assert (a != (0 if any_hit else oracle.HIT_NONE)).sum() > n // 10
+
+
+@pytest.mark.parametrize("cluster", [3, 6])
+def test_box_descent_equals_brute_force(cluster):
+    """The oracle's restatement of the batched form's traversal (per-ray box descent from the root of the
+    object tree, fused.cu k_fused_rays) gives exactly the brute-force records and flags, including rays with
+    zero direction components and short intervals; its work counts are sums of per-ray counts."""
+    s = scenes.soup(n_spheres=120, width=8, height=8, extent=10.0)
+    lo = s.positions[..., :3].reshape(-1, 3).min(0)
+    hi = s.positions[..., :3].reshape(-1, 3).max(0)
+    oh = oracle.ObjH(s.positions, cluster, lo, hi)
+    rng = np.random.default_rng(5)
+    n = 4000
+    r = np.zeros(n, oracle.RAY_DTYPE)
+    r["o"] = rng.uniform(-12, 12, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d[: n // 5, rng.integers(0, 3)] = 0.0
+    r["d"] = d / np.linalg.norm(d, axis=1)[:, None]
+    r["tmin"] = 0.01
+    r["tmax"] = np.where(rng.random(n) < 0.5, np.inf, rng.uniform(0.5, 15.0, n))
+    for any_hit in (False, True):
+        got, (nt, tt), per = oh.trace_box(r, any_hit, per_ray=True)
+        assert np.array_equal(got, oracle.brute(s.positions, r, any_hit))
+        assert per[:, 0].sum() == nt and per[:, 1].sum() == tt and tt > 0
+    # the boxes contain their triangles and carry the child links
+    bx = oh.boxes()
+    levels = oh.levels()
+    order, tris, _ = oh.arrays()
+    c0 = bx[: levels[0]]
+    first = c0[:, 3].view(np.uint32)
+    cnt = c0[:, 7].view(np.uint32)
+    assert first[0] == 0 and np.all(first[1:] == first[:-1] + cnt[:-1]) and cnt.sum() == s.tri_count
+    v = tris.reshape(-1, 3, 4)[:, :, :3]
+    for j in range(0, levels[0], 97):
+        tv = v[first[j]:first[j] + cnt[j]].reshape(-1, 3)
+        assert np.all(tv >= c0[j, :3]) and np.all(tv <= c0[j, 4:7])
