@@ -363,9 +363,9 @@ struct ObjH {
                                  // (level 0: the cluster's triangles)
     std::vector<float> tris;     // 12 per triangle, cluster order, w of vertex 0 = original id bits
     std::vector<uint32_t> order;
-    // per node (absolute index off[l] + j): padded box lo xyz, link, hi xyz, count (8 floats). The link
-    // is the first child's absolute node index (level 0: the cluster's first triangle) and the count its
-    // children (triangles), both as raw u32 bits in the w words
+    // per node (absolute index off[l] + j): padded box lo xyz, link, hi xyz, count (8 floats), link and
+    // count as raw u32 bits. A cluster's link is its first triangle; a node's (level l >= 1) is its whole
+    // single-ray stack entry, l << 27 | (children - 1) << 24 | absolute node index of its first child
     std::vector<float> box;
 };
 
@@ -530,6 +530,7 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
         }
         const uint32_t cl = L - 1, cnt = ((e >> 24) & 7u) + 1u;
         ntests += cnt;
+        if (sp + (int)cnt > 96) return false;
         float tcs[8];
         uint32_t hm = 0;
         for (uint32_t c = 0; c < cnt; ++c) {
@@ -540,7 +541,6 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
                 tcs[c] = tc;
             }
         }
-        if (sp + __builtin_popcount(hm) > 96) return false;
         while (hm) {
             uint32_t bc = 0;
             if (!any) {
@@ -554,8 +554,7 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
                 bc = (uint32_t)__builtin_ctz(hm);
             }
             hm &= ~(1u << bc);
-            const float* cb = &h.box[8ull * (idx + bc)];
-            stk[sp++] = cl == 0 ? idx + bc : (cl << 27) | ((f2u(cb[7]) - 1u) << 24) | (f2u(cb[3]) & 0xFFFFFFu);
+            stk[sp++] = cl == 0 ? idx + bc : f2u(h.box[8ull * (idx + bc) + 3]);
         }
     }
     return true;
@@ -1170,7 +1169,8 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
                 bx[i] = mn[i] - pad;
                 bx[4 + i] = mx[i] + pad;
             }
-            bx[3] = u2f(child_off + k[0]);
+            // level 0: the first triangle; above: the node's whole single-ray stack entry
+            bx[3] = u2f(l == 0 ? k[0] : (l << 27) | ((k[1] - k[0] - 1u) << 24) | ((child_off + k[0]) & 0xFFFFFFu));
             bx[7] = u2f(k[1] - k[0]);
         }
     }

@@ -81,13 +81,12 @@ RSH_DEV uint32_t find_segment(const FusedSeg* segs, uint32_t nseg, uint32_t u) {
 RSH_DEV uint32_t job_word(uint32_t i, uint32_t L, uint32_t idx) { return i | (L << 8) | (idx << 12); }
 
 // A job's stack entry. Triangle cluster c: c itself (level bits 0). Node of level L >= 1: L << 27 |
-// (children - 1) << 24 | absolute node index of its first child -- the child link its box carries
-// (lo.w, hi.w), so a popped node's children are loaded straight away. Fits 32 bits: L <= 16, at most
-// 8 children, fewer than 2^24 nodes (the batched form takes at most 2^20 nodes at level 1).
+// (children - 1) << 24 | absolute node index of its first child -- the word its box carries in lo.w
+// (written by the object-tree build), so a popped node's children are loaded straight away. Fits 32 bits:
+// L <= 16, at most 8 children, fewer than 2^24 nodes (the batched form takes at most 2^20 nodes at
+// level 1).
 constexpr uint32_t E_LSHIFT = 27;
-RSH_DEV uint32_t child_entry(uint32_t L, float first_bits, float count_bits) {
-    return (L << 27) | (min(__float_as_uint(count_bits) - 1u, 7u) << 24) | (__float_as_uint(first_bits) & 0xFFFFFFu);
-}
+RSH_DEV uint32_t child_entry(float lo_w) { return __float_as_uint(lo_w); }
 // The entry of a job's start node (L, idx); L == levels is the virtual root over the top level.
 RSH_DEV uint32_t job_entry(const FusedSeg& sg, const float4* boxes, uint32_t L, uint32_t idx, uint32_t* err) {
     if (L == 0u) return idx;
@@ -99,8 +98,7 @@ RSH_DEV uint32_t job_entry(const FusedSeg& sg, const float4* boxes, uint32_t L, 
         }
         return (L << 27) | ((cnt - 1u) << 24) | sg.lvl_off[L - 1u];
     }
-    const size_t b = 2ull * (sg.lvl_off[L] + idx);
-    return child_entry(L, __ldg(&boxes[b].w), __ldg(&boxes[b + 1].w));
+    return child_entry(__ldg(&boxes[2ull * (sg.lvl_off[L] + idx)].w));
 }
 
 // Ray vs a padded node box over [tmin, tmax]: slab test, NaN-free for zero direction components (fminf /
@@ -267,7 +265,7 @@ RSH_DEV void run_jobs(SM& S, const FusedSeg& sg, bool any, uint32_t lane, unsign
                     }
                     hm &= ~(1u << bc);
                     // a child node's own link, from the box just tested (an L1 hit)
-                    stk[sp++] = cl == 0u ? idx + bc : child_entry(cl, __ldg(&bb[2 * bc].w), __ldg(&bb[2 * bc + 1].w));
+                    stk[sp++] = cl == 0u ? idx + bc : child_entry(__ldg(&bb[2 * bc].w));
                 }
             }
         }
@@ -750,28 +748,39 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                 const uint32_t cnt = ((e >> 24) & 7u) + 1u;
                 const float4* bb = boxes + 2ull * idx;
                 ntests += cnt;
-                float tcs[8];
-                uint32_t hm = 0;
+                if (sp + cnt > J_STACK) {
+                    raise_device_error(a.err, RSH_DEVERR_OVERFLOW);
+                } else if (any) {
+                    // any hit: every child whose box the ray crosses is pushed as it is tested, in child
+                    // order (the last pops first); a child node's entry is its box's lo.w
 #pragma unroll
-                for (uint32_t c = 0; c < 8; ++c) {
-                    tcs[c] = 0.0f;
-                    if (c < cnt) {
-                        float tc;
-                        const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
-                        if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc)) {
-                            hm |= 1u << c;
-                            tcs[c] = tc;
+                    for (uint32_t c = 0; c < 8; ++c) {
+                        if (c < cnt) {
+                            float tc;
+                            const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
+                            if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc))
+                                stk[sp++] = cl == 0u ? idx + c : child_entry(b0.w);
                         }
                     }
-                }
-                if (sp + __popc(hm) > J_STACK) {
-                    raise_device_error(a.err, RSH_DEVERR_OVERFLOW);
-                    hm = 0;
-                }
-                // hits pushed farthest first (closest hit: the nearest pops first), in child order (any)
-                while (hm) {
-                    uint32_t bc = 0;
-                    if (!any) {
+                } else {
+                    // closest hit: the hits pushed farthest first, so that the nearest pops first (among
+                    // equal entry distances the lower child)
+                    float tcs[8];
+                    uint32_t hm = 0;
+#pragma unroll
+                    for (uint32_t c = 0; c < 8; ++c) {
+                        tcs[c] = 0.0f;
+                        if (c < cnt) {
+                            float tc;
+                            const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
+                            if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc)) {
+                                hm |= 1u << c;
+                                tcs[c] = tc;
+                            }
+                        }
+                    }
+                    while (hm) {
+                        uint32_t bc = 0;
                         float bt = -INFINITY;
 #pragma unroll
                         for (uint32_t c = 0; c < 8; ++c)
@@ -779,12 +788,10 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                                 bt = tcs[c];
                                 bc = c;
                             }
-                    } else {
-                        bc = __ffs(hm) - 1u;
+                        hm &= ~(1u << bc);
+                        // a child node's entry, from the box just tested (an L1 hit)
+                        stk[sp++] = cl == 0u ? idx + bc : child_entry(__ldg(&bb[2 * bc].w));
                     }
-                    hm &= ~(1u << bc);
-                    // a child node's own link, from the box just tested (an L1 hit)
-                    stk[sp++] = cl == 0u ? idx + bc : child_entry(cl, __ldg(&bb[2 * bc].w), __ldg(&bb[2 * bc + 1].w));
                 }
             }
             if (sp == 0) {

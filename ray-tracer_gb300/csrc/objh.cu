@@ -121,14 +121,15 @@ __global__ void k_level_nodes(const uint32_t* __restrict__ firsts, uint32_t nn, 
 
 // One warp per node: the sphere over every vertex of the node's triangle range. Min/max and max
 // reductions are exact in any order.
-// Also the node's box, widened by `pad` on every side, whose spare w words hold the node's child link:
-// lo.w = first child as an absolute node index (`child_off` + the level's child-range start; at level 0
-// the first triangle), hi.w = the number of children (triangles), both as raw u32 bits. A single ray
-// that pops a node then loads its children's boxes directly, with no child-range lookup in between.
-// Traversals rely on every node above level 0 having 1 to 8 children; a node outside that range raises
-// RSH_DEVERR_OVERFLOW (its link then covers no child at all or only the first 8).
+// Also the node's box, widened by `pad` on every side, whose spare w words hold the node's child link as
+// raw u32 bits. A cluster (level 0): lo.w = its first triangle, hi.w = its triangle count. A node of level
+// l >= 1: lo.w = its whole single-ray job-stack entry, l << 27 | (children - 1) << 24 | absolute node index
+// of its first child (`child_off` + the level's child-range start), hi.w = its child count. A single ray
+// that tests a node's box pushes that word as it is and, when it pops it, loads the children's boxes
+// directly, with no child-range lookup in between. Traversals rely on every node above level 0 having 1
+// to 8 children; a node outside that range raises RSH_DEVERR_OVERFLOW (its entry then lists 1 or 8).
 __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t* __restrict__ tstart, uint32_t nnodes,
-                                const uint32_t* __restrict__ kids, uint32_t child_off, bool upper,
+                                const uint32_t* __restrict__ kids, uint32_t child_off, uint32_t level,
                                 float4* __restrict__ sph, float4* __restrict__ box, float pad, uint32_t* err) {
     const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
@@ -156,8 +157,16 @@ __global__ void k_level_spheres(const float4* __restrict__ tris, const uint32_t*
     }
     if (lane == 0) {
         const uint32_t k0 = __ldg(kids + j), k1 = __ldg(kids + j + 1);
-        if (upper && (k1 <= k0 || k1 - k0 > 8u)) raise_device_error(err, RSH_DEVERR_OVERFLOW);
-        box[2 * j] = make_float4(mnx - pad, mny - pad, mnz - pad, __uint_as_float(child_off + k0));
+        uint32_t link = k0;  // level 0: the first triangle
+        if (level > 0u) {
+            uint32_t n = k1 - k0;
+            if (k1 <= k0 || n > 8u) {
+                raise_device_error(err, RSH_DEVERR_OVERFLOW);
+                n = k1 <= k0 ? 1u : 8u;
+            }
+            link = (level << 27) | ((n - 1u) << 24) | ((child_off + k0) & 0xFFFFFFu);
+        }
+        box[2 * j] = make_float4(mnx - pad, mny - pad, mnz - pad, __uint_as_float(link));
         box[2 * j + 1] = make_float4(mxx + pad, mxy + pad, mxz + pad, __uint_as_float(k1 - k0));
     }
     const v3 c = v3{(mnx + mxx) * 0.5f, (mny + mxy) * 0.5f, (mnz + mxz) * 0.5f};
@@ -275,7 +284,7 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
                                                        h.kids + total + l, nstart);
         note_launch();
         k_level_spheres<<<(nn * 32 + 127) / 128, 128, 0, s>>>(h.tris, nstart, nn, h.kids + total + l,
-                                                              l == 0 ? 0u : h.level_off[l - 1], l > 0,
+                                                              l == 0 ? 0u : h.level_off[l - 1], l,
                                                               h.spheres + total, h.boxes + 2ull * total, box_pad,
                                                               err);
         note_launch();

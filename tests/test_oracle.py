@@ -345,6 +345,14 @@ def test_box_descent_equals_brute_force(cluster):
     first = c0[:, 3].view(np.uint32)
     cnt = c0[:, 7].view(np.uint32)
     assert first[0] == 0 and np.all(first[1:] == first[:-1] + cnt[:-1]) and cnt.sum() == s.tri_count
+    # a node's link is its stack entry: level, child count and first child (absolute index)
+    off = np.concatenate([[0], np.cumsum(levels)])
+    for l in range(1, len(levels)):
+        e = bx[off[l]:off[l + 1], 3].view(np.uint32)
+        n = bx[off[l]:off[l + 1], 7].view(np.uint32)
+        assert np.all(e >> 27 == l) and np.all(((e >> 24) & 7) + 1 == n) and np.all((n >= 1) & (n <= 8))
+        f = e & 0xFFFFFF
+        assert f[0] == off[l - 1] and np.all(f[1:] == f[:-1] + n[:-1]) and f[-1] + n[-1] == off[l]
     v = tris.reshape(-1, 3, 4)[:, :, :3]
     for j in range(0, levels[0], 97):
         tv = v[first[j]:first[j] + cnt[j]].reshape(-1, 3)
