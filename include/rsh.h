@@ -281,6 +281,13 @@ uint32_t rsh_scene_level_size(const rsh_scene* scene, uint32_t level);
 rsh_status rsh_scene_get_level(const rsh_scene* scene, uint32_t level, rsh_object_node* host_out);
 /* Original triangle id of each cluster-order slot (host copy). */
 rsh_status rsh_scene_get_order(const rsh_scene* scene, uint32_t* host_out);
+/* The scene's single-ray box tree (built with the object hierarchy; the batched form's rays-only traversal
+ * descends it): returns its slot count (slot 0 unused) and writes its root's stack entry; copies its slots
+ * (2 float4 each: padded box lo + link word, hi + count word) and its triangles (3 float4 each, in the
+ * tree's depth-first order, w of the first = original id bits) to host memory when the pointers are not
+ * NULL. An 8-wide tree built by PLOC clustering: no counterpart in the reference, whose rays test
+ * per-triangle bounding spheres (CreateTriangleBoundingSphere, RayTracer.cu:301-376). */
+uint32_t rsh_scene_box_tree(const rsh_scene* scene, uint32_t* root, float* host_boxes, float* host_tris);
 /* Device pointers for stage-level calls: cluster-order vertices (3 float4 per triangle, w of the
  * first = original id bits) and the per-level sphere arrays. */
 const void* rsh_scene_device_triangles(const rsh_scene* scene);

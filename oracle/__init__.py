@@ -85,6 +85,7 @@ def lib():
             "orc_brute": (None, [P, U32, P, U32, I, P, P]),
             "orc_trace_rays_box": (I, [P, P, U32, I, P, P, P, P]),
             "orc_objh_boxes": (None, [P, P]),
+            "orc_objh_box_tree": (U32, [P, P, P, P]),
             "orc_brute_scalar": (None, [P, U32, P, U32, I, P, P]),
             "orc_brute_second": (None, [P, U32, P, U32, P, P]),
             "orc_resolve": (None, [P, P, P, P, P, P, U32, P, P]),
@@ -317,8 +318,18 @@ class ObjH:
         lib().orc_objh_boxes(self.h, _p(out))
         return out[: sum(self.levels())]
 
+    def box_tree(self):
+        """The single-ray box tree: (root entry, boxes [slots, 8] float32 with u32 words in columns 3 and 7,
+        triangles [T, 12] in its depth-first order)."""
+        root = np.zeros(1, np.uint32)
+        n = lib().orc_objh_box_tree(self.h, _p(root), None, None)
+        boxes = np.empty((max(n, 1), 8), np.float32)
+        tris = np.empty((max(self.T, 1), 12), np.float32)
+        lib().orc_objh_box_tree(self.h, None, _p(boxes), _p(tris))
+        return int(root[0]), boxes[:n], tris[: self.T]
+
     def trace_box(self, rays, any_hit, per_ray=False):
-        """Per-ray box descent from the root (the batched form's rays-only traversal): flags or hits, the
+        """Per-ray descent of the single-ray box tree (the batched form's rays-only traversal): flags or hits, the
         (node tests, triangle tests) totals and, with per_ray, the counts of every ray ([n, 2] u32)."""
         rays = np.ascontiguousarray(rays, RAY_DTYPE)
         n = len(rays)

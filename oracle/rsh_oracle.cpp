@@ -367,6 +367,11 @@ struct ObjH {
     // count as raw u32 bits. A cluster's link is its first triangle; a node's (level l >= 1) is its whole
     // single-ray stack entry, l << 27 | (children - 1) << 24 | absolute node index of its first child
     std::vector<float> box;
+    // the single-ray box tree (wide.cu): 8 floats per slot laid out as `box`, a cluster's count with the
+    // top bit set; its triangles in its own depth-first order; the root's stack entry
+    std::vector<float> wbox;
+    std::vector<float> wtris;
+    uint32_t wroot = 0;
 };
 
 // children of node (L, idx) at level L-1 (L == levels: the virtual root over the top level)
@@ -481,13 +486,13 @@ inline bool box_hit(const float* b, const float inv[3], const float oi[3], float
     return tn <= tf;
 }
 
-// One ray from the root of the object tree by node boxes: the batched form's rays-only traversal (fused.cu
-// k_fused_rays, run_jobs with one job per ray). A stack entry is a triangle cluster (its index) or a node
-// (level << 27 | (children - 1) << 24 | absolute index of its first child, from the link in the node's box).
-// A node step tests every child's box against [tmin, current best] and pushes the hits: any hit in child
-// order (the last child pops first), closest hit farthest first (the nearest pops first; among equal entry
-// distances the lower child). A cluster step tests the cluster's box, then its triangles. Counts node
-// tests (every child of a popped node) and triangle tests. Returns false on a stack overflow.
+// One ray from the root of the single-ray box tree (wide.cu): the batched form's rays-only traversal
+// (fused.cu k_fused_rays). A stack entry is a node's entry word (its box's lo.w: 1 << 27 | (children - 1)
+// << 24 | first child slot) or a cluster's slot. A node step tests every child's box against [tmin, current
+// best] and pushes the hits: any hit in child order (the last child pops first), closest hit farthest first
+// (the nearest pops first; among equal entry distances the lower child). A cluster step tests the
+// cluster's box, then its triangles. Counts node tests (every child of a popped node) and triangle tests.
+// Returns false on a stack overflow (more than 96 entries).
 bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint64_t& best, uint64_t& ntests,
                      uint64_t& ttests) {
     occluded = false;
@@ -499,19 +504,17 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
     float tcur = r.tmax;
     uint32_t stk[96];
     int sp = 0;
-    const uint32_t top = h.levels, tcnt = h.size[top - 1];
-    if (tcnt == 0 || tcnt > 8) return false;
-    stk[sp++] = (top << 27) | ((tcnt - 1) << 24) | h.off[top - 1];
+    stk[sp++] = h.wroot;
     while (sp > 0) {
         const uint32_t e = stk[--sp];
         const uint32_t L = e >> 27, idx = e & 0xFFFFFFu;
         if (L == 0) {
-            const float* b = &h.box[8ull * idx];
+            const float* b = &h.wbox[8ull * idx];
             float tn;
             if (!box_hit(b, inv, oi, r.tmin, tcur, tn)) continue;
-            const uint32_t t0 = f2u(b[3]), t1 = t0 + f2u(b[7]);
+            const uint32_t t0 = f2u(b[3]), t1 = t0 + (f2u(b[7]) & 0x7FFFFFFFu);
             for (uint32_t t = t0; t < t1; ++t) {
-                const float* v = &h.tris[12ull * t];
+                const float* v = &h.wtris[12ull * t];
                 float th;
                 ++ttests;
                 if (wt_hit(w, v, v + 4, v + 8, th)) {
@@ -528,7 +531,7 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
             }
             continue;
         }
-        const uint32_t cl = L - 1, cnt = ((e >> 24) & 7u) + 1u;
+        const uint32_t cnt = ((e >> 24) & 7u) + 1u;
         ntests += cnt;
         if (sp + (int)cnt > 96) return false;
         float tcs[8];
@@ -536,7 +539,7 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
         for (uint32_t c = 0; c < cnt; ++c) {
             float tc;
             tcs[c] = 0.0f;
-            if (box_hit(&h.box[8ull * (idx + c)], inv, oi, r.tmin, tcur, tc)) {
+            if (box_hit(&h.wbox[8ull * (idx + c)], inv, oi, r.tmin, tcur, tc)) {
                 hm |= 1u << c;
                 tcs[c] = tc;
             }
@@ -554,7 +557,8 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
                 bc = (uint32_t)__builtin_ctz(hm);
             }
             hm &= ~(1u << bc);
-            stk[sp++] = cl == 0 ? idx + bc : f2u(h.box[8ull * (idx + bc) + 3]);
+            const float* cb = &h.wbox[8ull * (idx + bc)];
+            stk[sp++] = (f2u(cb[7]) & 0x80000000u) ? idx + bc : f2u(cb[3]);
         }
     }
     return true;
@@ -1032,6 +1036,7 @@ void orc_build_rsh(const float* rays_in, const uint32_t* ids, uint32_t n, uint32
 // vertex of a node's triangle range; up to the first level of at most 8 nodes.
 static ObjH* g_last_objh = nullptr;
 
+static void build_box_tree(ObjH& h, float pad);
 static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const float lo[3], const float hi[3],
                        ObjH& h) {
     h.T = T;
@@ -1174,6 +1179,171 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
             bx[7] = u2f(k[1] - k[0]);
         }
     }
+    build_box_tree(h, pad);
+}
+
+// The single-ray box tree (wide.cu), restated: PLOC (Meister & Bittner 2018) over the Morton-ordered
+// triangles h.tris with search radius 8 -- each pass every cluster's nearest neighbour by merged-box area
+// (x y + y z) + x z (ties: the lower position), mutual pairs merge into a node at the lower position,
+// merged nodes numbered in position order -- then the triangles in depth-first order (left first), then the
+// breadth-first collapse to 8-wide nodes (open the largest-area child that is not a cluster of at most
+// `cluster` triangles, in place, while fewer than 8), children in consecutive slots from slot 1.
+namespace {
+struct PBox {
+    float lo[3], hi[3];
+    uint32_t cnt;
+};
+inline float parea(const float* a, const float* b) {
+    const float x = b[0] - a[0], y = b[1] - a[1], z = b[2] - a[2];
+    return (x * y + y * z) + x * z;
+}
+inline float pmerged(const PBox& p, const PBox& q) {
+    float a[3], b[3];
+    for (int i = 0; i < 3; ++i) {
+        a[i] = std::fmin(p.lo[i], q.lo[i]);
+        b[i] = std::fmax(p.hi[i], q.hi[i]);
+    }
+    return parea(a, b);
+}
+}  // namespace
+
+static void build_box_tree(ObjH& h, float pad) {
+    const uint32_t n = h.T;
+    h.wbox.clear();
+    h.wtris.clear();
+    h.wroot = 0;
+    if (n == 0) return;
+    std::vector<PBox> nodes(n);
+    std::vector<std::pair<int32_t, int32_t>> ch(n);
+    std::vector<int32_t> cur(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        const float* v = &h.tris[12ull * k];
+        PBox b;
+        for (int i = 0; i < 3; ++i) {
+            b.lo[i] = std::fmin(std::fmin(v[i], v[4 + i]), v[8 + i]);
+            b.hi[i] = std::fmax(std::fmax(v[i], v[4 + i]), v[8 + i]);
+        }
+        b.cnt = 1;
+        nodes[k] = b;
+        ch[k] = {-(int32_t)k - 1, 0};
+        cur[k] = (int32_t)k;
+    }
+    const int64_t R = 8;
+    while (cur.size() > 1) {
+        const int64_t m = (int64_t)cur.size();
+        std::vector<int64_t> nn(m);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < m; ++i) {
+            float best = INF;
+            int64_t bj = -1;
+            for (int64_t j = std::max<int64_t>(0, i - R); j <= std::min<int64_t>(m - 1, i + R); ++j) {
+                if (j == i) continue;
+                const float a = pmerged(nodes[cur[i]], nodes[cur[j]]);
+                if (a < best) {
+                    best = a;
+                    bj = j;
+                }
+            }
+            nn[i] = bj;
+        }
+        std::vector<int32_t> nxt;
+        nxt.reserve(m);
+        for (int64_t i = 0; i < m; ++i) {
+            const int64_t j = nn[i];
+            const bool mutual = j >= 0 && nn[j] == i;
+            if (mutual && i > j) continue;
+            if (mutual) {
+                const PBox& p = nodes[cur[i]];
+                const PBox& q = nodes[cur[j]];
+                PBox b;
+                for (int a = 0; a < 3; ++a) {
+                    b.lo[a] = std::fmin(p.lo[a], q.lo[a]);
+                    b.hi[a] = std::fmax(p.hi[a], q.hi[a]);
+                }
+                b.cnt = p.cnt + q.cnt;
+                nodes.push_back(b);
+                ch.push_back({cur[i], cur[j]});
+                nxt.push_back((int32_t)nodes.size() - 1);
+            } else {
+                nxt.push_back(cur[i]);
+            }
+        }
+        cur.swap(nxt);
+    }
+    const int32_t root = cur[0];
+    // depth-first triangle order: a node's children always have lower ids, so ids descending visit every
+    // parent before its children
+    std::vector<uint32_t> first(nodes.size(), 0);
+    for (int64_t x = (int64_t)nodes.size() - 1; x >= (int64_t)n; --x) {
+        first[ch[x].first] = first[x];
+        first[ch[x].second] = first[x] + nodes[ch[x].first].cnt;
+    }
+    h.wtris.resize(12ull * n);
+    for (uint32_t k = 0; k < n; ++k) std::memcpy(&h.wtris[12ull * first[k]], &h.tris[12ull * k], 48);
+    // breadth-first collapse
+    const uint32_t G = h.cluster;
+    auto is_cluster = [&](int32_t x) { return nodes[x].cnt <= G; };
+    auto expand = [&](int32_t x, bool at_root, std::vector<int32_t>& c) {
+        c.clear();
+        if (is_cluster(x)) {
+            if (at_root) c.push_back(x);
+            return;
+        }
+        c.push_back(x);
+        for (;;) {
+            int best = -1;
+            float ba = -1.0f;
+            for (size_t q = 0; q < c.size(); ++q) {
+                if (is_cluster(c[q])) continue;
+                const float a = parea(nodes[c[q]].lo, nodes[c[q]].hi);
+                if (a > ba) {
+                    ba = a;
+                    best = (int)q;
+                }
+            }
+            if (best < 0 || c.size() + 1 > 8) break;
+            const int32_t y = c[best];
+            c[best] = ch[y].first;
+            c.insert(c.begin() + best + 1, ch[y].second);
+        }
+    };
+    h.wbox.assign(8, 0.0f);  // slot 0: unused (the root has no slot)
+    std::vector<std::pair<int32_t, uint32_t>> level{{root, 0u}}, next;
+    std::vector<int32_t> c;
+    uint32_t slots = 1;
+    bool at_root = true;
+    while (!level.empty()) {
+        next.clear();
+        for (const auto& it : level) {
+            expand(it.first, at_root, c);
+            const uint32_t f = slots;
+            uint32_t lw, hw;
+            if (c.empty()) {
+                lw = first[it.first];
+                hw = 0x80000000u | nodes[it.first].cnt;
+            } else {
+                lw = (1u << 27) | (((uint32_t)c.size() - 1u) << 24) | (f & 0xFFFFFFu);
+                hw = (uint32_t)c.size();
+                for (size_t q = 0; q < c.size(); ++q) next.push_back({c[q], f + (uint32_t)q});
+                slots += (uint32_t)c.size();
+            }
+            if (at_root) {
+                h.wroot = lw;
+                continue;
+            }
+            const PBox& b = nodes[it.first];
+            float* bx = &h.wbox[8ull * it.second];
+            for (int i = 0; i < 3; ++i) {
+                bx[i] = b.lo[i] - pad;
+                bx[4 + i] = b.hi[i] + pad;
+            }
+            bx[3] = u2f(lw);
+            bx[7] = u2f(hw);
+        }
+        h.wbox.resize(8ull * slots, 0.0f);
+        level.swap(next);
+        at_root = false;
+    }
 }
 
 // UpdateVertex (RayTracer.cu:448-511): per vertex of triangle t, the object obj[t]'s row-major model
@@ -1220,6 +1390,15 @@ void orc_objh_free(void* hp) { delete static_cast<ObjH*>(hp); }
 void orc_objh_boxes(void* hp, float* out) {
     const ObjH& h = *static_cast<ObjH*>(hp);
     std::memcpy(out, h.box.data(), 4ull * h.box.size());
+}
+// the single-ray box tree: number of slots (slot 0 unused) and the root's entry; boxes (8 floats per slot)
+// and triangles (12 floats each, its depth-first order) when the pointers are not NULL
+uint32_t orc_objh_box_tree(void* hp, uint32_t* root, float* boxes, float* tris) {
+    const ObjH& h = *static_cast<ObjH*>(hp);
+    if (root) *root = h.wroot;
+    if (boxes) std::memcpy(boxes, h.wbox.data(), 4ull * h.wbox.size());
+    if (tris) std::memcpy(tris, h.wtris.data(), 4ull * h.wtris.size());
+    return (uint32_t)(h.wbox.size() / 8);
 }
 uint32_t orc_objh_levels(void* hp) { return static_cast<ObjH*>(hp)->levels; }
 uint32_t orc_objh_level_size(void* hp, uint32_t l) { return static_cast<ObjH*>(hp)->size[l]; }

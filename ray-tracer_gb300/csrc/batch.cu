@@ -267,6 +267,9 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         f.kids = sc->h.kids;
         f.tris = sc->h.tris;
         f.boxes = sc->h.boxes;
+        f.wboxes = sc->h.wboxes;
+        f.wtris = sc->h.wtris;
+        f.wroot = sc->h.wroot;
         f.tri_count = sc->tri_count;
         f.cluster = sc->h.cluster;
         f.levels = sc->h.levels;

@@ -627,7 +627,8 @@ rsh_status rsh_scene_upload(rsh_ctx* ctx, const rsh_scene_desc* d, rsh_scene** o
     }
     uint32_t total = 0;
     for (uint32_t l = 0; l < sc->h.levels; ++l) total += sc->h.level_size[l];
-    sc->bytes = tri_bytes * 3 + 8ull * T + 48ull * total +
+    // + the single-ray box tree: 2 float4 per slot (at most 2T + 8) and its own copy of the triangles
+    sc->bytes = tri_bytes * 3 + 8ull * T + 48ull * total + 32ull * (2ull * T + 8) + 48ull * T +
                 sizeof(rsh_material) * sc->material_count;
     ctx->allocated += sc->bytes;
     *out = sc;
@@ -649,6 +650,8 @@ rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* sc) {
     if (sc->h.tris) cudaFree(sc->h.tris);
     if (sc->h.order) cudaFree(sc->h.order);
     if (sc->h.boxes) cudaFree(sc->h.boxes);
+    if (sc->h.wboxes) cudaFree(sc->h.wboxes);
+    if (sc->h.wtris) cudaFree(sc->h.wtris);
     if (ctx && ctx->allocated >= sc->bytes) ctx->allocated -= sc->bytes;
     delete sc;
     return RSH_OK;
@@ -678,7 +681,7 @@ rsh_status rsh_build_object_hierarchy(rsh_ctx* ctx, rsh_scene* sc, rsh_stream_t 
     }
     RSH_CUDA(cudaStreamSynchronize(s));
     for (void* p : {(void*)sc->h.spheres, (void*)sc->h.kids, (void*)sc->h.tris, (void*)sc->h.order,
-                    (void*)sc->h.boxes})
+                    (void*)sc->h.boxes, (void*)sc->h.wboxes, (void*)sc->h.wtris})
         if (p) cudaFree(p);
     sc->h = ObjHierarchy();
     void* scr = nullptr;
@@ -730,6 +733,17 @@ rsh_status rsh_scene_bounds(const rsh_scene* sc, float lo[3], float hi[3]) {
 }
 uint32_t rsh_scene_triangle_count(const rsh_scene* sc) { return sc ? sc->tri_count : 0; }
 uint32_t rsh_scene_levels(const rsh_scene* sc) { return sc ? sc->h.levels : 0; }
+uint32_t rsh_scene_box_tree(const rsh_scene* sc, uint32_t* root, float* boxes, float* tris) {
+    if (!sc) return 0;
+    if (root) *root = sc->h.wroot;
+    if (boxes && sc->h.wslots &&
+        cudaMemcpy(boxes, sc->h.wboxes, 32ull * sc->h.wslots, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return 0;
+    if (tris && sc->tri_count &&
+        cudaMemcpy(tris, sc->h.wtris, 48ull * sc->tri_count, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return 0;
+    return sc->h.wslots;
+}
 uint32_t rsh_scene_level_size(const rsh_scene* sc, uint32_t level) {
     return (sc && level < sc->h.levels) ? sc->h.level_size[level] : 0;
 }

@@ -571,7 +571,10 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
 }
 
 // Rays-only form: every segment's switch level is at or above its tree's depth, so every ray is one job
-// from the root and no lane ever shares a ray. The warp keeps no per-unit state: it takes work units
+// from the root and no lane ever shares a ray. The rays descend the scene's single-ray box tree (wide.cu: an
+// 8-wide tree of mixed depth built by PLOC clustering, tighter than the object-sphere hierarchy's level
+// structure): a stack entry is a node's entry word from its box's lo.w, or a cluster's slot (a child is a
+// cluster when its hi.w has the top bit set; a cluster's hi.w holds its triangle count below that bit). The warp keeps no per-unit state: it takes work units
 // (RSH_RAYS_UNIT sorted rays, never straddling a segment) by atomic ticket, and every lane whose ray has
 // finished takes the next ray of the warp's current unit straight from global memory (its id from the
 // sorted order, the ray itself from the segment's array), fetching the next unit when the current one runs
@@ -681,8 +684,8 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             seg = cs;
                             slot = id - sg.slot_base;
                             any = sg.any_hit != 0u;
-                            boxes = sg.boxes;
-                            tris = sg.tris;
+                            boxes = sg.wboxes;
+                            tris = sg.wtris;
                             ox = o.x;
                             oy = o.y;
                             oz = o.z;
@@ -696,7 +699,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             oiz = oz * iz;
                             w = wt_setup(o, d);
                             best = RSH_HIT_NONE;
-                            stk[0] = job_entry(sg, boxes, sg.levels, 0u, a.err);
+                            stk[0] = sg.wroot;
                             sp = 1;
                             has = true;
                         }
@@ -721,7 +724,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                 // the cluster's box against [tmin, current best]; a miss skips its triangles
                 const float4 b0 = __ldg(boxes + 2ull * idx), b1 = __ldg(boxes + 2ull * idx + 1);
                 const uint32_t t0 = __float_as_uint(b0.w);  // the cluster's triangles: its box's link
-                uint32_t t1 = t0 + __float_as_uint(b1.w);
+                uint32_t t1 = t0 + (__float_as_uint(b1.w) & 0x7FFFFFFFu);
                 float tnb;
                 if (!box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tnb)) t1 = t0;
                 for (uint32_t tt = t0; tt < t1; ++tt) {
@@ -743,8 +746,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                     }
                 }
             } else {
-                const uint32_t cl = L - 1u;
-                // the entry holds the children's link: up to 8 boxes from absolute node `idx` on
+                // the entry holds the children's link: up to 8 slots from `idx` on
                 const uint32_t cnt = ((e >> 24) & 7u) + 1u;
                 const float4* bb = boxes + 2ull * idx;
                 ntests += cnt;
@@ -752,21 +754,21 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                     raise_device_error(a.err, RSH_DEVERR_OVERFLOW);
                 } else if (any) {
                     // any hit: every child whose box the ray crosses is pushed as it is tested, in child
-                    // order (the last pops first); a child node's entry is its box's lo.w
+                    // order (the last pops first): a cluster as its slot, a node as its entry word
 #pragma unroll
                     for (uint32_t c = 0; c < 8; ++c) {
                         if (c < cnt) {
                             float tc;
                             const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
                             if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc))
-                                stk[sp++] = cl == 0u ? idx + c : child_entry(b0.w);
+                                stk[sp++] = (__float_as_uint(b1.w) >> 31) ? idx + c : __float_as_uint(b0.w);
                         }
                     }
                 } else {
                     // closest hit: the hits pushed farthest first, so that the nearest pops first (among
                     // equal entry distances the lower child)
                     float tcs[8];
-                    uint32_t hm = 0;
+                    uint32_t hm = 0, cm = 0;
 #pragma unroll
                     for (uint32_t c = 0; c < 8; ++c) {
                         tcs[c] = 0.0f;
@@ -775,6 +777,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
                             if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc)) {
                                 hm |= 1u << c;
+                                cm |= (__float_as_uint(b1.w) >> 31) << c;
                                 tcs[c] = tc;
                             }
                         }
@@ -790,7 +793,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             }
                         hm &= ~(1u << bc);
                         // a child node's entry, from the box just tested (an L1 hit)
-                        stk[sp++] = cl == 0u ? idx + bc : child_entry(__ldg(&bb[2 * bc].w));
+                        stk[sp++] = ((cm >> bc) & 1u) ? idx + bc : __float_as_uint(__ldg(&bb[2 * bc].w));
                     }
                 }
             }

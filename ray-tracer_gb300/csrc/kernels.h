@@ -116,7 +116,15 @@ struct ObjHierarchy {
     float4* tris = nullptr;        // cluster order, 3 per triangle, v0.w = original id bits
     uint32_t* order = nullptr;     // cluster slot -> original triangle id
     float4* boxes = nullptr;       // per node, all levels like spheres: padded box lo, hi; lo.w / hi.w: child link
+    // the single-ray box tree (wide.cu): 8-wide, mixed depth, 2 float4 per slot; triangles in its own
+    // depth-first order (v0.w = original id bits); wroot = the root's stack entry
+    float4* wboxes = nullptr;
+    float4* wtris = nullptr;
+    uint32_t wroot = 0;
+    uint32_t wslots = 0;
 };
+// Builds the single-ray box tree from h.tris (Morton order) and h.cluster; boxes widened by `pad`.
+cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s);
 cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t tri_count, uint32_t cluster,
                                    const float lo[3], const float hi[3], ObjHierarchy& h,
                                    void* scratch, size_t scratch_bytes, uint32_t* err, cudaStream_t s);
@@ -176,6 +184,9 @@ struct FusedSeg {
     const uint32_t* kids;          // object-tree child ranges (level l at lvl_off[l] + l)
     const float4* tris;
     const float4* boxes;           // per node (like spheres): padded box lo, hi; lo.w / hi.w: child link
+    const float4* wboxes;          // the single-ray box tree (wide.cu), its triangles and its root's entry
+    const float4* wtris;
+    uint32_t wroot;
     uint32_t tri_count;
     uint32_t cluster;
     uint32_t levels;

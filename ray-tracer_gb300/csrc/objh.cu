@@ -299,7 +299,9 @@ cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t n, uint
     cudaError_t e2 = cudaStreamSynchronize(s);
     cudaFree(perm_tmp);
     if (e != cudaSuccess) return e;
-    return e2 != cudaSuccess ? e2 : cudaGetLastError();
+    if (e2 != cudaSuccess || (e2 = cudaGetLastError()) != cudaSuccess) return e2;
+    // the single-ray box tree over the same Morton-ordered triangles, with the same padding
+    return build_box_tree(h, box_pad, s);
 }
 
 }  // namespace rsh

@@ -172,6 +172,7 @@ SIGNATURES = {
     "rsh_scene_bounds": (C.c_int, [_P, _P, _P]),
     "rsh_scene_triangle_count": (_U32, [_P]),
     "rsh_scene_levels": (_U32, [_P]),
+    "rsh_scene_box_tree": (_U32, [_P, _P, _P, _P]),
     "rsh_scene_level_size": (_U32, [_P, _U32]),
     "rsh_scene_get_level": (C.c_int, [_P, _U32, _P]),
     "rsh_scene_get_order": (C.c_int, [_P, _P]),
@@ -452,6 +453,17 @@ class Scene:
         out[self.order()] = tris
         out[:, 0, 3] = self.positions[:, 0, 3]  # cluster order keeps the original id in v0.w
         return out
+
+    def box_tree(self):
+        """The single-ray box tree: (root entry, slots [n, 8] float32 with u32 words in columns 3 and 7,
+        triangles [T, 12] in its depth-first order)."""
+        root = C.c_uint32()
+        n = lib().rsh_scene_box_tree(self.handle, C.byref(root), None, None)
+        boxes = np.empty((max(n, 1), 8), np.float32)
+        T = lib().rsh_scene_triangle_count(self.handle)
+        tris = np.empty((max(T, 1), 12), np.float32)
+        lib().rsh_scene_box_tree(self.handle, None, boxes.ctypes.data, tris.ctypes.data)
+        return root.value, boxes[:n], tris[:T]
 
     def order(self) -> np.ndarray:
         a = np.empty(self.tri_count, np.uint32)

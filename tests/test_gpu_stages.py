@@ -391,6 +391,43 @@ def test_object_hierarchy_bitexact(ctx, which, cornell, soup_scene):
     sc.destroy()
 
 
+@pytest.mark.parametrize("which", ["cornell", "soup", "one", "six", "architecture"])
+def test_box_tree_bitexact(ctx, which, cornell, soup_scene):
+    """The single-ray box tree (PLOC clustering collapsed to 8-wide nodes) built on the GPU equals the
+    oracle's restatement slot for slot, with its triangles in the same depth-first order; a scene of one
+    triangle, or of no more triangles than a cluster holds, is a single cluster under the root."""
+    from rsh import scenes
+
+    if which == "cornell":
+        s = cornell
+    elif which == "soup":
+        s = soup_scene
+    elif which == "architecture":
+        s = scenes.architecture(grid=6, segments=12, rings=3)
+    else:
+        n = 1 if which == "one" else 6
+        s = scenes.SceneData(name=which, positions=cornell.positions[:n].copy(), normals=cornell.normals[:n].copy(),
+                             material_ids=cornell.material_ids[:n].copy(), materials=cornell.materials)
+    sc = ctx.scene(s.positions, s.normals, s.material_ids, s.materials)
+    lo, hi = sc.bounds()
+    oh = oracle.ObjH(s.positions, ctx.config.cluster_size, lo, hi)
+    root, boxes, tris = sc.box_tree()
+    oroot, oboxes, otris = oh.box_tree()
+    assert root == oroot and boxes.shape == oboxes.shape
+    assert boxes[1:].tobytes() == oboxes[1:].tobytes()
+    assert tris.tobytes() == otris.tobytes()
+    # every triangle in exactly one cluster, every cluster within the cluster size
+    w = boxes.view(np.uint32)
+    cl = (w[:, 7] >> 31) == 1
+    cnt = w[cl, 7] & 0x7FFFFFFF
+    assert cnt.sum() == s.tri_count and cnt.max() <= ctx.config.cluster_size
+    covered = np.sort(np.concatenate([np.arange(a, a + c) for a, c in zip(w[cl, 3], cnt)]))
+    assert np.array_equal(covered, np.arange(s.tri_count))
+    if which in ("one", "six"):
+        assert root >> 27 == 1 and ((root >> 24) & 7) == 0 and cl.sum() == 1
+    sc.destroy()
+
+
 def _stage_pipeline(ctx, sc, s, rays, any_hit, P=8, cap=1 << 25):
     """Runs hash -> compress -> sort -> decompress -> build -> traverse -> intersect stage by stage on the
     GPU and the same chain on the oracle; returns both."""

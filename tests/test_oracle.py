@@ -317,9 +317,11 @@ def test_blocked_brute_force_equals_scalar_loop():
 
 @pytest.mark.parametrize("cluster", [3, 6])
 def test_box_descent_equals_brute_force(cluster):
-    """The oracle's restatement of the batched form's traversal (per-ray box descent from the root of the
-    object tree, fused.cu k_fused_rays) gives exactly the brute-force records and flags, including rays with
-    zero direction components and short intervals; its work counts are sums of per-ray counts."""
+    """The oracle's restatement of the batched form's traversal (per-ray descent of the single-ray box tree,
+    fused.cu k_fused_rays) gives exactly the brute-force records and flags, including rays with zero
+    direction components and short intervals; its work counts are sums of per-ray counts. The box tree
+    partitions the triangles into clusters of at most `cluster`, every node has 1 to 8 children in
+    consecutive slots, and every box contains what is below it."""
     s = scenes.soup(n_spheres=120, width=8, height=8, extent=10.0)
     lo = s.positions[..., :3].reshape(-1, 3).min(0)
     hi = s.positions[..., :3].reshape(-1, 3).max(0)
@@ -337,7 +339,31 @@ def test_box_descent_equals_brute_force(cluster):
         got, (nt, tt), per = oh.trace_box(r, any_hit, per_ray=True)
         assert np.array_equal(got, oracle.brute(s.positions, r, any_hit))
         assert per[:, 0].sum() == nt and per[:, 1].sum() == tt and tt > 0
-    # the boxes contain their triangles and carry the child links
+    root, wb, wt = oh.box_tree()
+    w = wb.view(np.uint32)
+    is_cl = (w[:, 7] >> 31) == 1
+    cnt = w[is_cl, 7] & 0x7FFFFFFF
+    covered = np.sort(np.concatenate([np.arange(a, a + c) for a, c in zip(w[is_cl, 3], cnt)]))
+    assert np.array_equal(covered, np.arange(s.tri_count)) and cnt.max() <= cluster
+    assert np.array_equal(np.sort(wt[:, 3].view(np.uint32)), np.arange(s.tri_count))  # original ids
+    seen = np.zeros(len(wb), bool)
+    stack = [(root, None)]
+    while stack:
+        e, parent = stack.pop()
+        n, f = ((e >> 24) & 7) + 1, e & 0xFFFFFF
+        assert e >> 27 == 1 and 1 <= n <= 8 and f + n <= len(wb)
+        for c in range(f, f + n):
+            assert not seen[c]
+            seen[c] = True
+            if parent is not None:
+                assert np.all(wb[c, :3] >= wb[parent, :3]) and np.all(wb[c, 4:7] <= wb[parent, 4:7])
+            if not is_cl[c]:
+                stack.append((int(w[c, 3]), c))
+            else:
+                tv = wt[w[c, 3]:w[c, 3] + (w[c, 7] & 0x7FFFFFFF)].reshape(-1, 3, 4)[:, :, :3].reshape(-1, 3)
+                assert np.all(tv >= wb[c, :3]) and np.all(tv <= wb[c, 4:7])
+    assert seen[1:].all()
+    # the level tree's boxes contain their triangles and carry the child links
     bx = oh.boxes()
     levels = oh.levels()
     order, tris, _ = oh.arrays()
