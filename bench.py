@@ -14,8 +14,9 @@ bounce), FP32, seeded synthetic input. One step = one frame through rsh_render_f
   e2e         the same metric through the C ABI with host buffers: camera + lights from host structs in,
               the RGBA8 frame copied to pinned host memory, both inside the timed region
   roofline    the dominant kernel's achieved rate against its roofline (per-stage CUDA events)
-  cpu_baseline the oracle's C++/OpenMP restatement of the same algorithm on the same frame (the same
-               secondary rays), repeated for about --cpu-seconds
+  cpu_baseline the oracle's C++/OpenMP restatement of the same algorithm (per-ray descent of the single-ray
+               box tree) on the same frame (the same secondary rays), repeated for about --cpu-seconds;
+               cpu_baseline.packet: the reference's stage order (packet traversal) restated, one pass
 
 `--impl reference` times the CPU restatement alone (the reference ships no CPU path and cannot be built
 here) on the same workload and metric, and prints its own line.
@@ -50,6 +51,20 @@ ALGO = {
     "traverse": ("fp32", 24.0),    # flops / packet-node x sphere test
     "intersect": ("fp32", 46.0),   # flops / ray x triangle test
 }
+
+
+def batch_sort_passes(hash_bits: int, n_segments: int, no_compress: bool = False) -> tuple[int, int]:
+    """(key bits, 8-bit digit passes) of a batched call's sort, as the batch plans it: segment tag above
+    the hash, the hash's lowest bits dropped to fit 31 bits, and 1 or 2 leftover bits of a last pass
+    dropped too (no_compress sorts one more bit, empty slots last)."""
+    tag_bits = max(0, (n_segments - 1).bit_length())
+    drop = max(0, hash_bits + tag_bits - 31)
+    extra = 1 if no_compress else 0
+    kb = hash_bits + tag_bits - drop + extra
+    tail = kb % 8
+    if kb > 8 and tail and tail <= 2 and hash_bits - drop > tail:
+        kb -= tail
+    return kb, (kb + 7) // 8
 
 
 # ---------------------------------------------------------------- clocks
@@ -169,12 +184,17 @@ def make_workload(name: str):
     return scenes.by_name(name)
 
 
-def cpu_baseline(s, crop=None, threads=None, steps=1, min_seconds=0.0, max_passes=64):
-    """The oracle (C++/OpenMP restatement of the same algorithm) on the frame (crop=None: the whole frame,
-    the GPU metric's own rays) or a centred crop of it: primary hits, then `depth` bounces of shadow +
-    reflection batches through compress -> sort -> decompress -> build -> traverse+intersect. Times the
-    secondary part only (the GPU metric's window). One result per pass; passes repeat the same bounces
-    until there are `steps` of them and they took `min_seconds` in all (at most `max_passes`)."""
+def cpu_baseline(s, crop=None, threads=None, steps=1, min_seconds=0.0, max_passes=64, algo="box"):
+    """The oracle (C++/OpenMP on the host cores) on the frame (crop=None: the whole frame, the GPU metric's
+    own rays) or a centred crop of it: primary hits, then `depth` bounces of shadow + reflection rays.
+      algo "box":    the headline's own algorithm, the batched form's rays-only traversal restated: every
+                     ray descends the scene's single-ray box tree (PLOC, 8-wide) from the root, one ray per
+                     host thread at a time (oracle ObjH.trace_box; the GPU's counters equal its counts);
+      algo "packet": the reference's stage order, compress -> sort -> decompress -> ray hierarchy -> packet
+                     traversal + intersection (oracle ObjH.trace_keyed).
+    Times the secondary part only (the GPU metric's window: ray generation to the last intersection of
+    the last bounce). One result per pass; passes repeat the same bounces until there are `steps` of them
+    and they took `min_seconds` in all (at most `max_passes`)."""
     import oracle
 
     lib = oracle.lib()
@@ -200,12 +220,25 @@ def cpu_baseline(s, crop=None, threads=None, steps=1, min_seconds=0.0, max_passe
     crays = prays[sel]
     cpix = ((py[sel] - y0) * cw + (px[sel] - x0)).astype(np.uint32)
     scale = oracle.hash_scale(lo, hi, g)
-    keys = oracle.hash_rays(crays, lo, scale, g, b)
-    hits, _, _, _ = oh.trace_keyed(crays, keys, 3 * g + 2 * b, P, False, rl)
+    if algo == "box":
+        hits, _ = oh.trace_box(crays, False)
+    else:
+        keys = oracle.hash_rays(crays, lo, scale, g, b)
+        hits, _, _, _ = oh.trace_keyed(crays, keys, 3 * g + 2 * b, P, False, rl)
     spos0, snrm0 = oracle.resolve(s.positions, s.normals, s.material_ids, crays, hits, cpix, cw * chh)
     lp = np.array([l["position"] for l in s.lights], np.float32)
     L = len(lp)
     lbits = max(0, int(np.ceil(np.log2(L)))) if L > 1 else 0
+
+    def trace(rays, keys, key_bits, any_hit):
+        if algo == "box":
+            v = keys != oracle.KEY_NONE
+            out = np.zeros(len(rays), np.uint32) if any_hit else np.full(len(rays), oracle.HIT_NONE, np.uint64)
+            out[v], _ = oh.trace_box(rays[v], any_hit)
+            return out, int(v.sum())
+        res, R, _, _ = oh.trace_keyed(rays, keys, key_bits, P, any_hit, rl)
+        return res, R
+
     results = []
     while len(results) < max_passes and (len(results) < steps or sum(t for _, t in results) < min_seconds):
         spos, snrm, prev = spos0, snrm0, None
@@ -214,16 +247,22 @@ def cpu_baseline(s, crop=None, threads=None, steps=1, min_seconds=0.0, max_passe
         for bnc in range(s.depth):
             t1 = time.perf_counter()
             srays, skeys = oracle.raygen_shadow(spos, snrm, cw, chh, lp, 0.01, lo, scale, g, b)
-            flags, R1, _, _ = oh.trace_keyed(srays, skeys, lbits + 3 * g + 2 * b, P, True, rl)
+            flags, R1 = trace(srays, skeys, lbits + 3 * g + 2 * b, True)
             rrays, rkeys = oracle.raygen_reflect(spos, snrm, prev, cam[:3] if prev is None else None, cw, chh, 0.01,
                                                  s.jitter, s.seed, bnc, lo, scale, g, b)
-            rh, R2, _, _ = oh.trace_keyed(rrays, rkeys, 3 * g + 2 * b, P, False, rl)
+            rh, R2 = trace(rrays, rkeys, 3 * g + 2 * b, False)
             spos, snrm = oracle.resolve(s.positions, s.normals, s.material_ids, rrays, rh, None, cw * chh)
             t_sec += time.perf_counter() - t1
             rays_total += R1 + R2
             prev = rrays
         results.append((rays_total, t_sec))
-    return {"results": results, "threads": nthreads, "crop": (cw, chh), "objh_build_s": build_s}
+    return {"results": results, "threads": nthreads, "crop": (cw, chh), "objh_build_s": build_s, "algo": algo}
+
+
+CPU_ALGO = {"box": "the headline's algorithm restated in C++/OpenMP (every ray descends the single-ray box tree "
+                   "from the root, oracle ObjH.trace_box)",
+            "packet": "the reference's stage order restated in C++/OpenMP (compress, sort, decompress, ray "
+                      "hierarchy, packet traversal + intersection, oracle ObjH.trace_keyed)"}
 
 
 def cpu_sample_text(s, cb):
@@ -231,8 +270,8 @@ def cpu_sample_text(s, cb):
     where = f"the whole {cw}x{chh} frame" if (cw, chh) == (s.width, s.height) else f"a centred {cw}x{chh} crop of the frame"
     rays = sum(r for r, _ in cb["results"])
     secs = sum(t for _, t in cb["results"])
-    return (f"{where}, all bounces, {len(cb['results'])} pass(es): {rays} secondary rays in {secs:.2f} s "
-            f"(secondary part only, like the GPU metric)")
+    return (f"{CPU_ALGO[cb['algo']]}; {where}, all bounces, {len(cb['results'])} pass(es): {rays} secondary rays "
+            f"in {secs:.2f} s (secondary part only, like the GPU metric)")
 
 
 def gpu_arm(args, s, rank, world, td):
@@ -346,8 +385,8 @@ def gpu_arm(args, s, rank, world, td):
         chunks = last["chunks"]
         R = last["shadow_rays"] + last["reflection_rays"]
         slots = npix * (len(s.lights) + 1) * depth
-        key_bits = 3 * cfg.grid_bits + 2 * cfg.dir_log2 + 2
-        passes_sort = (key_bits + 7) // 8
+        # the batched form sorts both segments of a bounce together (the plain path: per batch, light tag)
+        key_bits, passes_sort = batch_sort_passes(3 * cfg.grid_bits + 2 * cfg.dir_log2, 2)
         bytes_stage = {
             "raygen": 64.0 * slots,
             "compress": 4.0 * slots + 12.0 * chunks + 4.0 * R,
@@ -624,13 +663,11 @@ def batching_bench(args):
     peaks = load_peaks()
     last = stage_runs[-1]
     n_rays, n_chunks = last["reflection_rays"], last["chunks"]
-    tag_bits = (len(sizes) - 1).bit_length()
     def eff(t, k):  # a scene's value, or the context's where the scene keeps it
         return getattr(best, k) if t[k] == rsh.TUNE_DEFAULT else t[k]
 
     hash_bits = max(3 * eff(t, "grid_bits") + 2 * eff(t, "dir_log2") for t in scene_tuning)
-    key_bits = min(31, hash_bits + tag_bits)
-    passes = (key_bits + 7) // 8
+    key_bits, passes = batch_sort_passes(hash_bits, len(sizes), bool(best.flags & rsh.FLAG_NO_COMPRESS))
     stage_bytes = {"hash": 32.0 * n_rays, "compress": 4.0 * n_rays + 12.0 * n_chunks,
                    "sort": n_chunks * (4.0 + 16.0 * passes), "decompress": 12.0 * n_chunks + 4.0 * n_rays,
                    "build": 32.0 * n_rays}
@@ -751,7 +788,8 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        cb = cpu_baseline(s, crop=crop, steps=args.warmup + args.steps, max_passes=args.warmup + args.steps)
+        cb = cpu_baseline(s, crop=crop, steps=args.warmup + args.steps, max_passes=args.warmup + args.steps,
+                          algo="box")
         res = cb["results"][args.warmup:]
         rays = sum(r for r, _ in res)
         secs = sum(t for _, t in res)
@@ -770,11 +808,17 @@ def main():
     out = gpu_arm(args, s, rank, world, td)
     if rank == 0:
         if not args.no_cpu_baseline:
-            cb = cpu_baseline(s, crop=crop, steps=1, min_seconds=args.cpu_seconds)
+            cb = cpu_baseline(s, crop=crop, steps=1, min_seconds=args.cpu_seconds, algo="box")
             rays = sum(r for r, _ in cb["results"])
             secs = sum(t for _, t in cb["results"])
             out["cpu_baseline"] = {"value": round(rays / secs / 1e6, 4), "unit": "Mrays/s", "cores": cb["threads"],
                                    "kind": "port", "sample": cpu_sample_text(s, cb)}
+            # second figure: the reference's stage order (packets over the ray-space hierarchy) on the host
+            cp = cpu_baseline(s, crop=crop, steps=1, min_seconds=0.0, algo="packet")
+            rp = sum(r for r, _ in cp["results"])
+            sp_ = sum(t for _, t in cp["results"])
+            out["cpu_baseline"]["packet"] = {"value": round(rp / sp_ / 1e6, 4), "unit": "Mrays/s",
+                                             "sample": cpu_sample_text(s, cp)}
         print(json.dumps(out))
     if td is not None:
         td.destroy_process_group()

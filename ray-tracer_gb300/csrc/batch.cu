@@ -198,6 +198,14 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         set_error("too many batch segments for a 31-bit key");
         return RSH_ERR_INVALID;
     }
+    {
+        // a last 8-bit digit pass for 1 or 2 leftover key bits would read and write every pair once more
+        // for almost no order: those lowest hash bits are dropped instead (a frame's two segments over a
+        // 24-bit hash sort in 3 passes, not 4)
+        const uint32_t empty_bit = (ctx->cfg.flags & RSH_FLAG_NO_COMPRESS) ? 1u : 0u;  // sorts one more bit
+        const uint32_t kb = hash_bits + tag_bits - pl.hash_drop + empty_bit, tail = kb % 8u;
+        if (kb > 8u && tail != 0u && tail <= 2u && hash_bits - pl.hash_drop > tail) pl.hash_drop += tail;
+    }
     pl.tag_shift = hash_bits - pl.hash_drop;
     pl.key_bits = pl.tag_shift + tag_bits;
     pl.P = ctx->cfg.packet_size;

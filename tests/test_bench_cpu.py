@@ -30,3 +30,15 @@ def test_reference_arm_json_line():
         assert k in line, k
     assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_batch_sort_passes_rule():
+    import bench
+
+    assert bench.batch_sort_passes(24, 2) == (24, 3)        # a frame: 1 tag bit over 24 dropped, 3 passes
+    assert bench.batch_sort_passes(24, 1) == (24, 3)
+    assert bench.batch_sort_passes(24, 2, True) == (24, 3)  # one more bit for empty slots, dropped too
+    assert bench.batch_sort_passes(20, 2) == (21, 3)
+    assert bench.batch_sort_passes(27, 300) == (31, 4)      # 9 tag bits: 36 -> 31 bits, 4 passes
+    assert bench.batch_sort_passes(24, 300) == (31, 4)
+    assert bench.batch_sort_passes(17, 300) == (24, 3)      # 26 bits: 2 leftover bits dropped
