@@ -358,7 +358,7 @@ rsh_status stage_tables(rsh_ctx* ctx, const BatchPlan& pl, char** out, cudaEvent
 // not allocate while capturing); otherwise a fenced ring slot of the context.
 // reset_stats: zero the node / triangle test counters first (a frame keeps counting over its batches).
 rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_staged = nullptr,
-                         bool reset_stats = true) {
+                         bool reset_stats = true, bool prekeyed = false) {
     if (pl.nseg == 0) return RSH_OK;
     char* tables = pre_staged;
     cudaEvent_t fence = nullptr;
@@ -374,13 +374,15 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     uint32_t* cnt = static_cast<uint32_t*>(pl.counts);
     uint32_t* totals = static_cast<uint32_t*>(pl.totals);
     int th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);  // gather + hash + per-segment counts
-    RSH_CUDA(cudaMemsetAsync(pl.seg_cnt, 0, 4ull * pl.nseg, s));
-    k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total,
-                                                       pl.tag_shift, pl.hash_drop, static_cast<rsh_ray*>(pl.rays_all),
-                                                       pl.gather,
-                                                       static_cast<uint32_t*>(pl.keys), static_cast<uint32_t*>(pl.seg_cnt));
-    note_launch();
-    RSH_CUDA(cudaGetLastError());
+    if (!prekeyed) {
+        RSH_CUDA(cudaMemsetAsync(pl.seg_cnt, 0, 4ull * pl.nseg, s));
+        k_batch_prep<<<(pl.total + 255) / 256, 256, 0, s>>>(
+            static_cast<PrepSeg*>(pl.prep), pl.nseg, pl.total, pl.tag_shift, pl.hash_drop,
+            static_cast<rsh_ray*>(pl.rays_all), pl.gather, static_cast<uint32_t*>(pl.keys),
+            static_cast<uint32_t*>(pl.seg_cnt));
+        note_launch();
+        RSH_CUDA(cudaGetLastError());
+    }
     k_batch_bounds<<<1, 1024, 0, s>>>(static_cast<uint32_t*>(pl.seg_cnt), pl.nseg, pl.unit_rays,
                                       static_cast<uint32_t*>(pl.seg_begin), static_cast<uint32_t*>(pl.pstart),
                                       static_cast<uint32_t*>(pl.seg_delta), static_cast<uint32_t*>(pl.sched),
@@ -507,12 +509,31 @@ rsh_status batch_trace_ordered(rsh_ctx* ctx, const rsh_batch_segment& seg, cudaS
 }
 
 // rsh_batch_trace without resetting the stage timers (a fused frame keeps its own).
+rsh_status batch_key_layout(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, BatchKeyLayout& out) {
+    if (count > 2) return RSH_ERR_INVALID;
+    BatchPlan pl;
+    RSH_TRY(batch_prepare(ctx, segments, count, pl));
+    if (pl.gather || (count && !pl.contiguous)) {
+        set_error("keys from ray generation need the segments' rays back to back in one array");
+        return RSH_ERR_INVALID;
+    }
+    out.keys = static_cast<uint32_t*>(pl.keys);
+    out.seg_cnt = static_cast<uint32_t*>(pl.seg_cnt);
+    out.tag_shift = pl.tag_shift;
+    out.hash_drop = pl.hash_drop;
+    for (uint32_t i = 0; i < count; ++i) {
+        out.start[i] = pl.h_prep[i].start;
+        out.hp[i] = pl.h_prep[i].hp;
+    }
+    return RSH_OK;
+}
+
 rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream,
-                       bool reset_stats) {
+                       bool reset_stats, bool prekeyed) {
     BatchPlan pl;
     RSH_TRY(batch_prepare(ctx, segments, count, pl));
     ctx->last_stream = stream;
-    RSH_TRY(batch_enqueue(ctx, pl, stream, nullptr, reset_stats));
+    RSH_TRY(batch_enqueue(ctx, pl, stream, nullptr, reset_stats, prekeyed));
     ctx->batch_counts_host.assign(1, pl.total);
     return RSH_OK;
 }

@@ -1190,17 +1190,33 @@ rsh_status rsh_render_frame(rsh_ctx* ctx, const rsh_scene* sc, uint32_t W, uint3
         rsh_ray* rrays = srays + (size_t)npix * LS;
         unsigned long long* rhits = static_cast<unsigned long long*>(bb.refl_hits.ptr);
         if (fused) {
-            // both batches of the bounce in one batched call: 2 segments, one persistent launch
-            th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);
-            // no keys: the batch hashes both segments itself
-            RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays, nullptr, s));
-            RSH_CUDA(launch_raygen_reflect(spos, snrm, incident, ctx->cam.eye, W, H, ctx->cfg.epsilon,
-                                           ctx->cfg.reflect_jitter, ctx->cfg.seed, b, hp_r, rrays, nullptr, s));
-            stage_end(ctx, th, s);
+            // both batches of the bounce in one batched call: 2 segments, one persistent launch; ray
+            // generation writes the batch's keys, segment counts and prefilled results itself
             rsh_batch_segment segs[2] = {
                 {sc, srays, npix * LS, 1, nullptr, sflags},
                 {sc, rrays, npix, 0, reinterpret_cast<uint64_t*>(rhits), nullptr}};
-            RSH_TRY(batch_trace(ctx, segs, 2, s, false));
+            BatchKeyLayout kl;
+            RSH_TRY(batch_key_layout(ctx, segs, 2, kl));
+            BatchKeyOut bs, br;
+            bs.keys = kl.keys + kl.start[0];
+            bs.tag = 0u;
+            bs.drop = kl.hash_drop;
+            bs.hp = kl.hp[0];
+            bs.count = kl.seg_cnt;
+            bs.flags = sflags;
+            br.keys = kl.keys + kl.start[1];
+            br.tag = 1u << kl.tag_shift;
+            br.drop = kl.hash_drop;
+            br.hp = kl.hp[1];
+            br.count = kl.seg_cnt + 1;
+            br.hits = rhits;
+            th = stage_begin(ctx, RSH_STAGE_RAYGEN, s);
+            RSH_CUDA(cudaMemsetAsync(kl.seg_cnt, 0, 8, s));
+            RSH_CUDA(launch_raygen_shadow(spos, snrm, W, H, lp, ctx->cfg.epsilon, hp_s, srays, nullptr, s, bs));
+            RSH_CUDA(launch_raygen_reflect(spos, snrm, incident, ctx->cam.eye, W, H, ctx->cfg.epsilon,
+                                           ctx->cfg.reflect_jitter, ctx->cfg.seed, b, hp_r, rrays, nullptr, s, br));
+            stage_end(ctx, th, s);
+            RSH_TRY(batch_trace(ctx, segs, 2, s, false, true));
             const uint32_t* seg_cnt = static_cast<const uint32_t*>(ctx->bufs["b_seg_cnt"].ptr);
             const uint32_t* bcnt = static_cast<const uint32_t*>(ctx->bufs["b_counts"].ptr);
             RSH_CUDA(cudaMemcpyAsync(fc + 4 * b, seg_cnt, 4, cudaMemcpyDeviceToDevice, s));

@@ -99,8 +99,21 @@ rsh_status make_hash_params(const rsh_scene* sc, const rsh_config& cfg, uint32_t
 void batch_release_ctx(const rsh_ctx* ctx);
 // rsh_batch_trace without resetting the stage timers (used inside a fused frame, which also keeps its
 // node / triangle test counters running: reset_stats false).
+// prekeyed: the segments' keys, ray counts and prefilled results were already written where
+// batch_key_layout says (by the frame's ray generation), so the batch does not read the rays to hash them.
 rsh_status batch_trace(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, cudaStream_t stream,
-                       bool reset_stats);
+                       bool reset_stats, bool prekeyed = false);
+// Where ray generation writes a batched call's keys itself: segment s's keys at keys + start[s], key =
+// s << tag_shift | (hash with hp[s] >> hash_drop) or RSH_KEY_NONE; its ray count into seg_cnt[s] (zeroed
+// by the caller first). For at most 2 segments whose rays lie back to back in one array.
+struct BatchKeyLayout {
+    uint32_t* keys = nullptr;
+    uint32_t* seg_cnt = nullptr;
+    uint32_t tag_shift = 0, hash_drop = 0;
+    uint32_t start[2] = {0, 0};
+    HashP hp[2]{};
+};
+rsh_status batch_key_layout(rsh_ctx* ctx, const rsh_batch_segment* segments, uint32_t count, BatchKeyLayout& out);
 // One segment of rays already in a coherent order, traced in that order (rays-only kernel); adds to the
 // test counters.
 rsh_status batch_trace_ordered(rsh_ctx* ctx, const rsh_batch_segment& seg, cudaStream_t stream);

@@ -48,13 +48,27 @@ struct CameraP {
 // ---- raygen + hash (raygen.cu)
 cudaError_t launch_raygen_primary(const CameraP& cam, uint32_t w, uint32_t h, rsh_ray* rays,
                                   uint32_t* pixel_of_ray, cudaStream_t s);
+// Keys of a batched call written by ray generation itself (the batched form of a frame): key = tag |
+// (ray hash >> drop) or RSH_KEY_NONE, the segment's ray count (one atomic per block into *count), and the
+// segment's results prefilled (flags 0 for an any-hit segment, hits RSH_HIT_NONE otherwise), so the batch
+// need not read the rays back to hash them.
+struct BatchKeyOut {
+    uint32_t* keys = nullptr;      // the batch's key array at the segment's first slot; null: not used
+    uint32_t tag = 0;
+    uint32_t drop = 0;
+    HashP hp{};                    // the segment scene's hash (tag 0)
+    uint32_t* count = nullptr;
+    uint32_t* flags = nullptr;
+    unsigned long long* hits = nullptr;
+};
 cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_t w, uint32_t h,
                                  const LightsP& lights, float eps, const HashP& hp, rsh_ray* rays,
-                                 uint32_t* keys, cudaStream_t s);
+                                 uint32_t* keys, cudaStream_t s, const BatchKeyOut& bk = BatchKeyOut());
 cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const rsh_ray* prev,
                                   const float eye[3], uint32_t w, uint32_t h, float eps,
                                   float jitter, uint32_t seed, uint32_t bounce, const HashP& hp,
-                                  rsh_ray* rays, uint32_t* keys, cudaStream_t s);
+                                  rsh_ray* rays, uint32_t* keys, cudaStream_t s,
+                                  const BatchKeyOut& bk = BatchKeyOut());
 cudaError_t launch_raygen_refract(const float4* spos, const float4* snrm, const rsh_ray* prev, const float eye[3],
                                   uint32_t w, uint32_t h, float eps, float eta, const HashP& hp, rsh_ray* rays,
                                   uint32_t* keys, cudaStream_t s);

@@ -65,59 +65,85 @@ RSH_DEV v3 soft_sample_pos(v3 lp, v3 d, uint32_t k) {
               (lp.z + (a0.z * ca) * 0.125f) + (a1.z * cb) * 0.125f};
 }
 
+// The batch keys of a block's slots (BatchKeyOut): each slot's key and prefilled result, and the block's
+// count of rays in one atomic. Every thread of the block calls it (it synchronises the block).
+RSH_DEV void batch_key_out(const BatchKeyOut& bk, uint32_t slot, bool in_range, bool valid, float4 o, float4 d) {
+    __shared__ uint32_t s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0u;
+    __syncthreads();
+    if (in_range) {
+        bk.keys[slot] = valid ? bk.tag | (ray_hash(o.x, o.y, o.z, d.x, d.y, d.z, bk.hp, 0u) >> bk.drop)
+                              : RSH_KEY_NONE;
+        if (bk.flags) bk.flags[slot] = 0u;
+        else bk.hits[slot] = RSH_HIT_NONE;
+    }
+    const uint32_t b = __ballot_sync(0xffffffffu, in_range && valid);
+    if (lane_id() == 0 && b) atomicAdd(&s_cnt, (uint32_t)__popc(b));
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cnt) atomicAdd(bk.count, s_cnt);
+}
+
 __global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* __restrict__ snrm,
                                 uint32_t w, uint32_t h, LightsP lights, float eps, HashP hp,
-                                rsh_ray* rays, uint32_t* keys) {
+                                rsh_ray* rays, uint32_t* keys, BatchKeyOut bk) {
     const uint32_t L = lights.count, S = lights.samples ? lights.samples : 1u, V = L * S;
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= w * h * V) return;
-    // slot = x + W*(v + L*S*y), v = l*S + s  (RayTracer.cu:700-702 with S samples per light)
-    const uint32_t x = slot % w;
-    const uint32_t v = (slot / w) % V;
-    const uint32_t y = slot / (w * V);
-    const uint32_t l = v / S, s = v % S;
-    const uint32_t pix = y * w + x;
-    const float4 p4 = __ldg(spos + pix);
-    uint32_t key = RSH_KEY_NONE;
-    if (p4.w != 0.0f) {
-        const v3 p = mk3(p4);
-        const v3 nn = norm3(mk3(__ldg(snrm + pix)));
-        const v3 lp = mk3(lights.pos[l][0], lights.pos[l][1], lights.pos[l][2]);
-        const v3 vl = p - lp;
-        const float len = len3(vl);
-        const v3 d = v3{vl.x / len, vl.y / len, vl.z / len};
-        const float diffuse = dot3(d, -nn);
-        const float tmax = len - 2.0f * eps;
-        if (diffuse > 0.0f && tmax > eps) {
-            v3 src = lp, dir = d;
-            float tm = tmax;
-            bool ok = true;
-            if (S > 1) {  // a sample of the 4x4 grid: its own origin, direction and interval
-                src = soft_sample_pos(lp, d, s);
-                const v3 vs = p - src;
-                const float ls = len3(vs);
-                dir = v3{vs.x / ls, vs.y / ls, vs.z / ls};
-                tm = ls - 2.0f * eps;
-                ok = tm > eps;
-            }
-            if (ok) {
-                const v3 o = src + dir * eps;
-                store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps), make_float4(dir.x, dir.y, dir.z, tm));
-                key = keys ? ray_hash(o.x, o.y, o.z, dir.x, dir.y, dir.z, hp, v) : 0u;
+    const bool in_range = slot < w * h * V;
+    bool valid = false;
+    float4 ro = make_float4(0.f, 0.f, 0.f, 0.f), rd = make_float4(0.f, 0.f, 0.f, -1.f);
+    if (in_range) {
+        // slot = x + W*(v + L*S*y), v = l*S + s  (RayTracer.cu:700-702 with S samples per light)
+        const uint32_t x = slot % w;
+        const uint32_t v = (slot / w) % V;
+        const uint32_t y = slot / (w * V);
+        const uint32_t l = v / S, s = v % S;
+        const uint32_t pix = y * w + x;
+        const float4 p4 = __ldg(spos + pix);
+        uint32_t key = RSH_KEY_NONE;
+        if (p4.w != 0.0f) {
+            const v3 p = mk3(p4);
+            const v3 nn = norm3(mk3(__ldg(snrm + pix)));
+            const v3 lp = mk3(lights.pos[l][0], lights.pos[l][1], lights.pos[l][2]);
+            const v3 vl = p - lp;
+            const float len = len3(vl);
+            const v3 d = v3{vl.x / len, vl.y / len, vl.z / len};
+            const float diffuse = dot3(d, -nn);
+            const float tmax = len - 2.0f * eps;
+            if (diffuse > 0.0f && tmax > eps) {
+                v3 src = lp, dir = d;
+                float tm = tmax;
+                bool ok = true;
+                if (S > 1) {  // a sample of the 4x4 grid: its own origin, direction and interval
+                    src = soft_sample_pos(lp, d, s);
+                    const v3 vs = p - src;
+                    const float ls = len3(vs);
+                    dir = v3{vs.x / ls, vs.y / ls, vs.z / ls};
+                    tm = ls - 2.0f * eps;
+                    ok = tm > eps;
+                }
+                if (ok) {
+                    const v3 o = src + dir * eps;
+                    ro = make_float4(o.x, o.y, o.z, eps);
+                    rd = make_float4(dir.x, dir.y, dir.z, tm);
+                    store_ray(rays, slot, ro, rd);
+                    key = keys ? ray_hash(o.x, o.y, o.z, dir.x, dir.y, dir.z, hp, v) : 0u;
+                    valid = true;
+                }
             }
         }
+        // empty slot: an explicit no-ray (tmax < tmin) for consumers without keys
+        if (!valid) store_ray(rays, slot, ro, rd);
+        if (keys) keys[slot] = key;
     }
-    if (key == RSH_KEY_NONE)  // empty slot: an explicit no-ray (tmax < tmin) for consumers without keys
-        store_ray(rays, slot, make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, -1.f));
-    if (keys) keys[slot] = key;  // no keys: the batched form hashes the rays itself
+    if (bk.keys) batch_key_out(bk, slot, in_range, valid, ro, rd);
 }
 
 cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_t w, uint32_t h,
                                  const LightsP& lights, float eps, const HashP& hp, rsh_ray* rays,
-                                 uint32_t* keys, cudaStream_t s) {
+                                 uint32_t* keys, cudaStream_t s, const BatchKeyOut& bk) {
     const uint32_t n = w * h * lights.count * (lights.samples ? lights.samples : 1u);
     if (n == 0) return cudaSuccess;
-    k_raygen_shadow<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, w, h, lights, eps, hp, rays, keys);
+    k_raygen_shadow<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, w, h, lights, eps, hp, rays, keys, bk);
     note_launch();
     return cudaGetLastError();
 }
@@ -148,51 +174,58 @@ RSH_DEV v3 sphere_sample(uint32_t seed, uint32_t slot, uint32_t bounce) {
 __global__ void k_raygen_reflect(const float4* __restrict__ spos, const float4* __restrict__ snrm,
                                  const rsh_ray* __restrict__ prev, v3 eye, uint32_t n, float eps,
                                  float jitter, uint32_t seed, uint32_t bounce, HashP hp,
-                                 rsh_ray* rays, uint32_t* keys) {
+                                 rsh_ray* rays, uint32_t* keys, BatchKeyOut bk) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= n) return;
-    const float4 p4 = __ldg(spos + slot);
-    uint32_t key = RSH_KEY_NONE;
-    if (p4.w != 0.0f) {
-        const v3 p = mk3(p4);
-        const v3 nn = norm3(mk3(__ldg(snrm + slot)));
-        v3 i;
-        if (prev) {
-            float4 po, pd;
-            load_ray(prev, slot, po, pd);
-            i = mk3(pd);
-        } else {
-            i = norm3(p - eye);
+    const bool in_range = slot < n;
+    bool valid = false;
+    float4 ro = make_float4(0.f, 0.f, 0.f, 0.f), rd = make_float4(0.f, 0.f, 0.f, -1.f);
+    if (in_range) {
+        const float4 p4 = __ldg(spos + slot);
+        uint32_t key = RSH_KEY_NONE;
+        if (p4.w != 0.0f) {
+            const v3 p = mk3(p4);
+            const v3 nn = norm3(mk3(__ldg(snrm + slot)));
+            v3 i;
+            if (prev) {
+                float4 po, pd;
+                load_ray(prev, slot, po, pd);
+                i = mk3(pd);
+            } else {
+                i = norm3(p - eye);
+            }
+            const float k2 = 2.0f * dot3(nn, i);
+            v3 r = i - nn * k2;  // reflect(i, n)
+            if (jitter > 0.0f) {
+                const v3 u = sphere_sample(seed, slot, bounce);
+                r = r + u * jitter;
+                const float rn = dot3(r, nn);
+                if (rn < 0.0f) r = r - nn * (2.0f * rn);
+            }
+            r = norm3(r);
+            if (r.x == r.x && r.y == r.y && r.z == r.z) {  // drop degenerate (NaN) directions
+                const v3 o = p + r * eps;
+                ro = make_float4(o.x, o.y, o.z, eps);
+                rd = make_float4(r.x, r.y, r.z, __int_as_float(0x7f800000));
+                store_ray(rays, slot, ro, rd);
+                key = keys ? ray_hash(o.x, o.y, o.z, r.x, r.y, r.z, hp, 0u) : 0u;
+                valid = true;
+            }
         }
-        const float k2 = 2.0f * dot3(nn, i);
-        v3 r = i - nn * k2;  // reflect(i, n)
-        if (jitter > 0.0f) {
-            const v3 u = sphere_sample(seed, slot, bounce);
-            r = r + u * jitter;
-            const float rn = dot3(r, nn);
-            if (rn < 0.0f) r = r - nn * (2.0f * rn);
-        }
-        r = norm3(r);
-        if (r.x == r.x && r.y == r.y && r.z == r.z) {  // drop degenerate (NaN) directions
-            const v3 o = p + r * eps;
-            store_ray(rays, slot, make_float4(o.x, o.y, o.z, eps),
-                      make_float4(r.x, r.y, r.z, __int_as_float(0x7f800000)));
-            key = keys ? ray_hash(o.x, o.y, o.z, r.x, r.y, r.z, hp, 0u) : 0u;
-        }
+        // no ray: stored as such, also for the next bounce, which reads this array as its incident rays
+        if (!valid) store_ray(rays, slot, ro, rd);
+        if (keys) keys[slot] = key;
     }
-    if (key == RSH_KEY_NONE)
-        store_ray(rays, slot, make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, -1.f));
-    if (keys) keys[slot] = key;
+    if (bk.keys) batch_key_out(bk, slot, in_range, valid, ro, rd);
 }
 
 cudaError_t launch_raygen_reflect(const float4* spos, const float4* snrm, const rsh_ray* prev,
                                   const float eye[3], uint32_t w, uint32_t h, float eps,
                                   float jitter, uint32_t seed, uint32_t bounce, const HashP& hp,
-                                  rsh_ray* rays, uint32_t* keys, cudaStream_t s) {
+                                  rsh_ray* rays, uint32_t* keys, cudaStream_t s, const BatchKeyOut& bk) {
     const uint32_t n = w * h;
     if (n == 0) return cudaSuccess;
     k_raygen_reflect<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, prev, v3{eye[0], eye[1], eye[2]}, n,
-                                                     eps, jitter, seed, bounce, hp, rays, keys);
+                                                     eps, jitter, seed, bounce, hp, rays, keys, bk);
     note_launch();
     return cudaGetLastError();
 }
