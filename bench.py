@@ -492,8 +492,12 @@ def fcfs_latency_ms(gaps, service) -> list:
 
 
 def serving_bench(args):
-    """Poisson request arrivals over resident scenes through rsh_server_*: p50/p99 latency and Mrays/s,
-    next to the same requests rendered one by one through rsh_render_frame (a serial per-frame loop)."""
+    """Poisson request arrivals over resident scenes through rsh_server_* at each rate of --serve-rates:
+    p50/p99 latency and Mrays/s (clocks sampled while the server runs), next to the same requests rendered
+    one at a time through rsh_render_frame, back to back: by the batched form (RSH_FLAG_FUSED) for every
+    request, and by the plain per-frame path for the first --serve-plain ones (it is ~50x slower). Each
+    serial loop's latency is that of a single renderer taking the same arrivals first come, first served,
+    with every request's own measured frame time."""
     import ctypes as C
 
     import rsh
@@ -510,7 +514,6 @@ def serving_bench(args):
     reqs = []
     for k in range(args.serve_requests):
         si = int(rng.integers(0, n_scenes))
-        s = sd[si]
         W, H = res_choices[int(rng.integers(0, len(res_choices)))]
         ang = rng.uniform(0, 2 * np.pi)
         eye = (60.0 * np.cos(ang), rng.uniform(-10, 30), 60.0 * np.sin(ang))
@@ -524,60 +527,90 @@ def serving_bench(args):
         for i in range(nl):
             r.lights[i] = arr[i]
         reqs.append(r)
-    gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
-    # serial per-frame loop (same requests, back to back, the plain path); each frame's own time gives the
-    # latency a single plain renderer would show under the same arrivals (first come, first served)
-    t0 = time.perf_counter()
-    serial_rays = 0
-    service = []
-    for r in reqs:
-        t1 = time.perf_counter()
-        ctx.set_camera(r.camera)
-        lib.rsh_lights_set(ctx.handle, r.lights, r.light_count)
-        rsh.check(lib.rsh_render_frame(ctx.handle, scs[r.scene_index].handle, r.width, r.height, r.depth, None, None),
-                  "render")
-        fs = rsh.FrameStats()
-        lib.rsh_frame_stats_get(ctx.handle, C.byref(fs))
-        serial_rays += fs.shadow_rays + fs.reflection_rays
-        service.append(time.perf_counter() - t1)
-    serial_s = time.perf_counter() - t0
-    serial_lat = fcfs_latency_ms(gaps, service)
-    # the server: submit with Poisson gaps, then wait for all
+
+    def serial(flags, subset):
+        """Renders the requests one at a time (synchronised each), returns (service times s, rays)."""
+        ctx.set_config(flags=flags)
+        for r in reqs[:2]:  # warm-up: buffers sized
+            ctx.set_camera(r.camera)
+            lib.rsh_lights_set(ctx.handle, r.lights, r.light_count)
+            rsh.check(lib.rsh_render_frame(ctx.handle, scs[r.scene_index].handle, r.width, r.height, r.depth, None,
+                                           None), "render")
+            ctx.stats()
+        service, rays = [], 0
+        for r in subset:
+            t1 = time.perf_counter()
+            ctx.set_camera(r.camera)
+            lib.rsh_lights_set(ctx.handle, r.lights, r.light_count)
+            rsh.check(lib.rsh_render_frame(ctx.handle, scs[r.scene_index].handle, r.width, r.height, r.depth, None,
+                                           None), "render")
+            fs = ctx.stats()  # synchronises
+            rays += fs["shadow_rays"] + fs["reflection_rays"]
+            service.append(time.perf_counter() - t1)
+        return service, rays
+
+    fused_service, fused_rays = serial(rsh.FLAG_FUSED, reqs)
+    plain_subset = reqs[: args.serve_plain]
+    plain_service, plain_rays = serial(0, plain_subset)
+    ctx.set_config(flags=0)
     arrs = (C.c_void_p * n_scenes)(*[s.handle for s in scs])
-    srv = C.c_void_p()
-    rsh.check(lib.rsh_server_create(ctx.handle, arrs, n_scenes, args.serve_budget_gb << 30, 64, C.byref(srv)), "srv")
-    ids = []
-    t0 = time.perf_counter()
-    for r, g in zip(reqs, gaps):
-        time.sleep(g)
-        i = C.c_uint64()
-        rsh.check(lib.rsh_server_submit(srv, C.byref(r), C.byref(i)), "submit")
-        ids.append(i.value)
-    lat, rays = [], 0
-    for i in ids:
-        rr = rsh.RequestResult()
-        st = lib.rsh_server_wait(srv, i, 600_000, C.byref(rr), None, None)
-        if st == rsh.RSH_OK:
-            lat.append(rr.finish_ms - rr.submit_ms)
-            rays += rr.rays
-    wall = time.perf_counter() - t0
-    stats = [C.c_uint64() for _ in range(4)]
-    lib.rsh_server_stats(srv, *[C.byref(x) for x in stats])
-    lib.rsh_server_destroy(srv)
+    out_rates = []
+    for rate in [float(x) for x in args.serve_rates.split(",")]:
+        gaps = np.random.default_rng([scenes.SEED_BASE + 4, int(rate)]).exponential(1.0 / rate, len(reqs))
+        srv = C.c_void_p()
+        rsh.check(lib.rsh_server_create(ctx.handle, arrs, n_scenes, args.serve_budget_gb << 30, 64, C.byref(srv)),
+                  "srv")
+        clocks = ClockSampler()
+        clocks.start()
+        ids = []
+        t0 = time.perf_counter()
+        due = t0
+        for r, g in zip(reqs, gaps):
+            due += g
+            delay = due - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            i = C.c_uint64()
+            rsh.check(lib.rsh_server_submit(srv, C.byref(r), C.byref(i)), "submit")
+            ids.append(i.value)
+        lat, rays = [], 0
+        for i in ids:
+            rr = rsh.RequestResult()
+            st = lib.rsh_server_wait(srv, i, 600_000, C.byref(rr), None, None)
+            if st == rsh.RSH_OK:
+                lat.append(rr.finish_ms - rr.submit_ms)
+                rays += rr.rays
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+        stats = [C.c_uint64() for _ in range(4)]
+        lib.rsh_server_stats(srv, *[C.byref(x) for x in stats])
+        lib.rsh_server_destroy(srv)
+        lat = np.array(lat)
+        fl = fcfs_latency_ms(gaps, fused_service)
+        pl_ = fcfs_latency_ms(gaps[: len(plain_service)], plain_service)
+        out_rates.append({
+            "arrival_rate_req_s": rate, "requests": len(reqs), "completed": int(len(lat)),
+            "arrival_window_s": round(float(np.sum(gaps)), 3),
+            "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
+            "server_wall_s": round(wall, 3), "server_mrays_s": round(rays / wall / 1e6, 3),
+            "serial_fused_p50_ms": round(float(np.percentile(fl, 50)), 2),
+            "serial_fused_p99_ms": round(float(np.percentile(fl, 99)), 2),
+            "serial_plain_p50_ms": round(float(np.percentile(pl_, 50)), 2),
+            "serial_plain_p99_ms": round(float(np.percentile(pl_, 99)), 2),
+            "steps": stats[1].value, "peak_inflight": stats[2].value, "peak_bytes": stats[3].value, "clocks": clk})
     for s in scs:
         s.destroy()
     ctx.destroy()
-    lat = np.array(lat)
-    return {"metric": "serving p50/p99 latency", "requests": len(reqs), "completed": int(len(lat)),
-            "arrival_rate_req_s": args.serve_rate, "p50_ms": round(float(np.percentile(lat, 50)), 2),
-            "p99_ms": round(float(np.percentile(lat, 99)), 2),
-            "serial_p50_ms": round(float(np.percentile(serial_lat, 50)), 2),
-            "serial_p99_ms": round(float(np.percentile(serial_lat, 99)), 2), "server_wall_s": round(wall, 3),
-            "server_mrays_s": round(rays / wall / 1e6, 3), "serial_wall_s": round(serial_s, 3),
-            "serial_mrays_s": round(serial_rays / serial_s / 1e6, 3),
-            "steps": stats[1].value, "peak_inflight": stats[2].value, "peak_bytes": stats[3].value,
-            "scenes_tris": [int(t) for t in tris]}
-
+    return {"metric": "serving p50/p99 latency and Mrays/s vs serial per-frame loops",
+            "scenes_tris": [int(t) for t in tris], "requests": len(reqs),
+            "resolutions": [f"{w}x{h}" for w, h in res_choices],
+            "serial_fused": {"mrays_s": round(fused_rays / sum(fused_service) / 1e6, 3),
+                             "wall_s": round(sum(fused_service), 3), "requests": len(reqs),
+                             "form": "rsh_render_frame, RSH_FLAG_FUSED, one request at a time"},
+            "serial_plain": {"mrays_s": round(plain_rays / sum(plain_service) / 1e6, 3),
+                             "wall_s": round(sum(plain_service), 3), "requests": len(plain_subset),
+                             "form": "rsh_render_frame, plain per-frame path, one request at a time"},
+            "rates": out_rates, "data": "synthetic (seeded random soups, seeded requests)"}
 
 
 def batching_bench(args):
@@ -763,8 +796,9 @@ def main():
     ap.add_argument("--sort", type=int, default=0, help="time rsh_sort_pairs alone on this many pairs")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-max-rays", type=int, default=2_000_000)
-    ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-requests", type=int, default=500)
+    ap.add_argument("--serve-rates", default="50,500,2000", help="arrival rates (req/s), comma separated")
+    ap.add_argument("--serve-plain", type=int, default=64, help="requests the plain serial loop renders")
     ap.add_argument("--serve-scenes", type=int, default=8)
     ap.add_argument("--serve-max-res", type=int, default=3)
     ap.add_argument("--serve-budget-gb", type=int, default=32)

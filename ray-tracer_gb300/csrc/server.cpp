@@ -105,6 +105,10 @@ struct rsh_server {
     uint64_t budget = 0;
     uint32_t max_inflight = 64;
     cudaStream_t stream = nullptr;
+    // request buffers come from the server's own stream-ordered pool, allocated and freed on its stream:
+    // a finished request's memory goes back without a device-wide synchronisation (cudaFree would stall
+    // every step in flight), and the pool keeps it for the next request instead of returning it
+    cudaMemPool_t pool = nullptr;
     std::thread th;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -129,17 +133,19 @@ struct rsh_server {
 
 namespace {
 
-rsh_status alloc_request(Req* q) {
-    char* p = nullptr;
-    RSH_CUDA(cudaMalloc(&p, q->bytes));  // q->bytes = request_bytes(q->r) >= request_layout(q->r)
+rsh_status alloc_request(rsh_server* s, Req* q) {
+    void* p = nullptr;
+    // q->bytes = request_bytes(q->r) >= request_layout(q->r)
+    RSH_CUDA(cudaMallocFromPoolAsync(&p, q->bytes, s->pool, s->stream));
     q->buf = p;
-    request_layout(q->r, q, p);
+    request_layout(q->r, q, static_cast<char*>(p));
     return RSH_OK;
 }
 
+// The request's steps have all retired (or never ran): its buffer goes back to the pool in stream order.
 void free_request(rsh_server* s, Req* q) {
     if (q->buf) {
-        cudaFree(q->buf);
+        cudaFreeAsync(q->buf, s->stream);
         q->buf = nullptr;
         s->bytes_in_use -= q->bytes;
     }
@@ -297,7 +303,7 @@ void server_main(rsh_server* s) {
             }
             s->queue.pop_front();
             s->bytes_in_use += q->bytes;
-            if (alloc_request(q) != RSH_OK) {
+            if (alloc_request(s, q) != RSH_OK) {
                 s->bytes_in_use -= q->bytes;
                 q->done = true;
                 q->status = RSH_ERR_OOM;
@@ -393,6 +399,21 @@ rsh_status rsh_server_create(rsh_ctx* ctx, const rsh_scene* const* scenes, uint3
     if (e != cudaSuccess) {
         delete s;
         return cuda_status(e, "rsh_server_create");
+    }
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    e = cudaMemPoolCreate(&s->pool, &props);
+    if (e == cudaSuccess) {
+        uint64_t keep = ~0ull;  // never trim the pool below what it holds: the budget bounds it
+        e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e != cudaSuccess) {
+        if (s->pool) cudaMemPoolDestroy(s->pool);
+        cudaStreamDestroy(s->stream);
+        delete s;
+        return cuda_status(e, "rsh_server_create: memory pool");
     }
     s->th = std::thread(server_main, s);
     *out = s;
@@ -507,6 +528,8 @@ rsh_status rsh_server_destroy(rsh_server* s) {
         if (rec.done) cudaEventDestroy(rec.done);
         if (rec.pinned) cudaFreeHost(rec.pinned);
     }
+    cudaStreamSynchronize(s->stream);
+    cudaMemPoolDestroy(s->pool);
     cudaStreamDestroy(s->stream);
     delete s;
     return RSH_OK;
