@@ -560,9 +560,28 @@ def serving_bench(args):
         srv = C.c_void_p()
         rsh.check(lib.rsh_server_create(ctx.handle, arrs, n_scenes, args.serve_budget_gb << 30, 64, C.byref(srv)),
                   "srv")
+        if args.serve_step_rays >= 0:
+            rsh.check(lib.rsh_server_set_step_rays(srv, args.serve_step_rays), "step rays")
         clocks = ClockSampler()
         clocks.start()
-        ids = []
+        # a client thread collects results in submission order while requests keep arriving (a finished
+        # request holds its device memory until it is collected)
+        import queue as _queue
+
+        pending, lat, tally = _queue.Queue(), [], {"rays": 0}
+
+        def collect():
+            while True:
+                i = pending.get()
+                if i is None:
+                    return
+                rr = rsh.RequestResult()
+                if lib.rsh_server_wait(srv, i, 600_000, C.byref(rr), None, None) == rsh.RSH_OK:
+                    lat.append(rr.finish_ms - rr.submit_ms)
+                    tally["rays"] += rr.rays
+
+        th = threading.Thread(target=collect)
+        th.start()
         t0 = time.perf_counter()
         due = t0
         for r, g in zip(reqs, gaps):
@@ -572,14 +591,10 @@ def serving_bench(args):
                 time.sleep(delay)
             i = C.c_uint64()
             rsh.check(lib.rsh_server_submit(srv, C.byref(r), C.byref(i)), "submit")
-            ids.append(i.value)
-        lat, rays = [], 0
-        for i in ids:
-            rr = rsh.RequestResult()
-            st = lib.rsh_server_wait(srv, i, 600_000, C.byref(rr), None, None)
-            if st == rsh.RSH_OK:
-                lat.append(rr.finish_ms - rr.submit_ms)
-                rays += rr.rays
+            pending.put(i.value)
+        pending.put(None)
+        th.join()
+        rays = tally["rays"]
         wall = time.perf_counter() - t0
         clk = clocks.stop()
         stats = [C.c_uint64() for _ in range(4)]
@@ -588,11 +603,14 @@ def serving_bench(args):
         lat = np.array(lat)
         fl = fcfs_latency_ms(gaps, fused_service)
         pl_ = fcfs_latency_ms(gaps[: len(plain_service)], plain_service)
+        # the serial batched loop under the same arrivals: rays over its makespan (first arrival to last finish)
+        fused_makespan = float(np.cumsum(gaps)[-1] + fl[-1] / 1e3)
         out_rates.append({
             "arrival_rate_req_s": rate, "requests": len(reqs), "completed": int(len(lat)),
             "arrival_window_s": round(float(np.sum(gaps)), 3),
             "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
             "server_wall_s": round(wall, 3), "server_mrays_s": round(rays / wall / 1e6, 3),
+            "serial_fused_mrays_s": round(fused_rays / fused_makespan / 1e6, 3),
             "serial_fused_p50_ms": round(float(np.percentile(fl, 50)), 2),
             "serial_fused_p99_ms": round(float(np.percentile(fl, 99)), 2),
             "serial_plain_p50_ms": round(float(np.percentile(pl_, 50)), 2),
@@ -799,6 +817,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-rates", default="50,500,2000", help="arrival rates (req/s), comma separated")
     ap.add_argument("--serve-plain", type=int, default=64, help="requests the plain serial loop renders")
+    ap.add_argument("--serve-step-rays", type=int, default=-1, help="server ray budget per step (-1: default)")
     ap.add_argument("--serve-scenes", type=int, default=8)
     ap.add_argument("--serve-max-res", type=int, default=3)
     ap.add_argument("--serve-budget-gb", type=int, default=32)

@@ -564,8 +564,10 @@ typedef struct rsh_request_result {
 } rsh_request_result;
 
 /* A continuous-batching request loop on its own host thread: requests are admitted while their
- * device memory fits the HBM budget; every step traces one bounce of every in-flight request in one
- * batched launch; requests leave as they finish and new ones join between steps. */
+ * device memory fits the HBM budget; every step traces the next stage (primary rays, or one bounce) of
+ * the oldest in-flight requests, up to a ray budget per step (rsh_server_set_step_rays), in one batched
+ * launch; requests leave as they finish and new ones join between steps. A finished request keeps its
+ * device memory (its results) until rsh_server_wait collects it. */
 rsh_status rsh_server_create(rsh_ctx* ctx, const rsh_scene* const* scenes, uint32_t scene_count,
                              uint64_t hbm_budget, uint32_t max_inflight, rsh_server** out);
 rsh_status rsh_server_submit(rsh_server* srv, const rsh_request* req, uint64_t* id_out);
@@ -580,6 +582,10 @@ rsh_status rsh_server_request_bytes(const rsh_request* req, uint64_t* bytes);
 rsh_status rsh_server_wait(rsh_server* srv, uint64_t id, uint32_t timeout_ms,
                            rsh_request_result* result, uint64_t* hits_host, uint32_t* flags_host);
 rsh_status rsh_server_cancel(rsh_server* srv, uint64_t id);
+/* Rays one step may generate (a stage of width*height primary rays or width*height*(lights + 1) bounce
+ * rays per request; at least one request per step); 0 = every in-flight request each step. Default
+ * 6,291,456: enough to fill the GPU, small enough that the oldest requests finish first. */
+rsh_status rsh_server_set_step_rays(rsh_server* srv, uint64_t rays);
 rsh_status rsh_server_stats(rsh_server* srv, uint64_t* completed, uint64_t* steps,
                             uint64_t* peak_inflight, uint64_t* peak_bytes);
 rsh_status rsh_server_destroy(rsh_server* srv);

@@ -104,6 +104,9 @@ struct rsh_server {
     std::vector<const rsh_scene*> scenes;
     uint64_t budget = 0;
     uint32_t max_inflight = 64;
+    // rays one step may generate (primary pixels, or pixels x (lights + 1) for a bounce); the oldest
+    // in-flight requests go first, so a request's stages do not wait behind every later arrival
+    uint64_t step_rays = 6ull << 20;
     cudaStream_t stream = nullptr;
     // request buffers come from the server's own stream-ordered pool, allocated and freed on its stream:
     // a finished request's memory goes back without a device-wide synchronisation (cudaFree would stall
@@ -330,10 +333,17 @@ void server_main(rsh_server* s) {
                 ++it;
             }
         }
-        // the requests with a stage left to enqueue
+        // the requests with a stage left to enqueue, oldest first, up to the step's ray budget (at least one)
         std::vector<Req*> act;
-        for (Req* q : s->inflight)
-            if (!q->cancelled && q->status == RSH_OK && q->stage <= q->r.depth) act.push_back(q);
+        uint64_t step_rays = 0;
+        for (Req* q : s->inflight) {
+            if (q->cancelled || q->status != RSH_OK || q->stage > q->r.depth) continue;
+            const uint64_t npix = (uint64_t)q->r.width * q->r.height;
+            const uint64_t rays = q->stage == 0 ? npix : npix * (q->r.light_count + 1u);
+            if (!act.empty() && s->step_rays && step_rays + rays > s->step_rays) break;
+            step_rays += rays;
+            act.push_back(q);
+        }
         if (act.empty() || s->steps_q.size() >= kDepth) {
             if (!s->steps_q.empty()) {  // the GPU is busy: wait for its oldest step
                 retire_oldest(s, lk, true);
@@ -490,6 +500,13 @@ rsh_status rsh_server_cancel(rsh_server* s, uint64_t id) {
     if (it == s->all.end()) return RSH_ERR_INVALID;
     it->second->cancelled = true;
     s->cv_work.notify_one();
+    return RSH_OK;
+}
+
+rsh_status rsh_server_set_step_rays(rsh_server* s, uint64_t rays) {
+    if (!s) return RSH_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->step_rays = rays;
     return RSH_OK;
 }
 

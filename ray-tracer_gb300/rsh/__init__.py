@@ -220,6 +220,7 @@ SIGNATURES = {
     "rsh_server_request_bytes": (C.c_int, [_P, _P]),
     "rsh_server_wait": (C.c_int, [_P, _U64, _U32, _P, _P, _P]),
     "rsh_server_cancel": (C.c_int, [_P, _U64]),
+    "rsh_server_set_step_rays": (C.c_int, [_P, _U64]),
     "rsh_server_stats": (C.c_int, [_P, _P, _P, _P, _P]),
     "rsh_server_destroy": (C.c_int, [_P]),
 }
