@@ -583,8 +583,8 @@ rsh_status rsh_server_wait(rsh_server* srv, uint64_t id, uint32_t timeout_ms,
                            rsh_request_result* result, uint64_t* hits_host, uint32_t* flags_host);
 rsh_status rsh_server_cancel(rsh_server* srv, uint64_t id);
 /* Rays one step may generate (a stage of width*height primary rays or width*height*(lights + 1) bounce
- * rays per request; at least one request per step); 0 = every in-flight request each step. Default
- * 6,291,456: enough to fill the GPU, small enough that the oldest requests finish first. */
+ * rays per request; at least one request per step), taken oldest first; 0 (the default) = every
+ * in-flight request each step. A budget bounds a step's length when requests are large. */
 rsh_status rsh_server_set_step_rays(rsh_server* srv, uint64_t rays);
 rsh_status rsh_server_stats(rsh_server* srv, uint64_t* completed, uint64_t* steps,
                             uint64_t* peak_inflight, uint64_t* peak_bytes);

@@ -104,9 +104,9 @@ struct rsh_server {
     std::vector<const rsh_scene*> scenes;
     uint64_t budget = 0;
     uint32_t max_inflight = 64;
-    // rays one step may generate (primary pixels, or pixels x (lights + 1) for a bounce); the oldest
-    // in-flight requests go first, so a request's stages do not wait behind every later arrival
-    uint64_t step_rays = 6ull << 20;
+    // rays one step may generate (primary pixels, or pixels x (lights + 1) for a bounce), the oldest
+    // in-flight requests first; 0: every in-flight request each step (measured best up to saturation)
+    uint64_t step_rays = 0;
     cudaStream_t stream = nullptr;
     // request buffers come from the server's own stream-ordered pool, allocated and freed on its stream:
     // a finished request's memory goes back without a device-wide synchronisation (cudaFree would stall
