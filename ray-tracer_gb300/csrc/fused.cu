@@ -614,9 +614,6 @@ RSH_DEV bool box_hit_fma(float4 b0, float4 b1, float ix, float iy, float iz, flo
 #ifndef RSH_RAYS_MIN_BLOCKS
 #define RSH_RAYS_MIN_BLOCKS 8
 #endif
-#ifndef RSH_RAYS_GROUP8
-#define RSH_RAYS_GROUP8 0
-#endif
 #ifndef RSH_TAIL_PER_WARP
 #define RSH_TAIL_PER_WARP 16
 #endif
@@ -820,222 +817,18 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     }
 }
 
-// The rays-only form with a group of 8 lanes per ray (4 rays per warp). A node step gives each lane one child:
-// the group's 8 child boxes are one coalesced 256-byte read, every lane tests its own box, and the hits
-// are ranked by shuffles within the group and written to the ray's stack in shared memory (any hit: in
-// child order; closest hit: farthest first, the lower child nearer among equal entry distances -- the order
-// of the lane-per-ray form). A cluster step tests the cluster's box once, then up to 8 of its triangles
-// at a time, one per lane; an any-hit ray ends at the first 8 that occlude it, a closest-hit ray takes the
-// group's smallest hit key. Rays are fetched from global memory by whole groups as they finish, from the
-// warp's current work unit, as in the lane-per-ray form. Each warp iteration runs one kind of step, the
-// kind more of its four groups want.
-constexpr uint32_t G_STACK = 96;  // entries of a ray's stack (shared memory)
-
-template <int U>
-__global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays_g8(FusedArgs a) {
-    __shared__ uint32_t s_stk[FW][4][G_STACK];
-    const uint32_t lane = lane_id(), c = lane & 7u, g = lane >> 3, gbase = lane & ~7u;
-    uint32_t* stk = s_stk[threadIdx.x >> 5][g];
-    const uint32_t units = dev_count(a.d_units, a.units_max);
-    const uint32_t tail = min(units, (uint32_t)RSH_TAIL_PER_WARP * gridDim.x * FW);
-    const uint32_t head = units - tail, tickets = head + RSH_TAIL_SPLIT * tail;
-    unsigned long long ntests = 0, ttests = 0;
-    uint32_t nk = 0, nend = 0, cs = 0;
-    bool drained = false;
-    // the group's ray (the same in its 8 lanes)
-    bool has = false, any = false;
-    uint32_t seg = 0, slot = 0, sp = 0;
-    const float4* __restrict__ boxes = nullptr;
-    const float4* __restrict__ tris = nullptr;
-    float tmin = 0.f, tcur = 0.f, ix = 0.f, iy = 0.f, iz = 0.f, oix = 0.f, oiy = 0.f, oiz = 0.f;
-    RayWT w;
-    unsigned long long best = RSH_HIT_NONE;
-    for (;;) {
-        // idle groups take the next rays of the warp's unit; units are fetched as they run out
-        for (;;) {
-            const uint32_t need = __ballot_sync(0xffffffffu, !has && c == 0u);
-            if (!need) break;
-            if (nk >= nend) {
-                if (drained) break;
-                uint32_t t = 0;
-                if (lane == 0) t = atomicAdd(&a.work[0], 1u);
-                t = __shfl_sync(0xffffffffu, t, 0);
-                if (t >= tickets) {
-                    drained = true;
-                    break;
-                }
-                uint32_t u = t, lo = 0, hi = U;
-                if (t >= head) {
-                    const uint32_t h = t - head;
-                    u = head + h / RSH_TAIL_SPLIT;
-                    lo = (h % RSH_TAIL_SPLIT) * (U / RSH_TAIL_SPLIT);
-                    hi = lo + U / RSH_TAIL_SPLIT;
-                }
-                nk = u * U + lo;
-                nend = u * U + hi;
-                cs = find_segment(a.segs, a.nseg, u);
-            }
-            const uint32_t k = nk + __popc(need & ((1u << gbase) - 1u));  // rank of this group among the needy
-            if (!has && k < nend) {
-                const uint32_t id = a.sorted_ids ? __ldg(a.sorted_ids + k) : (k < a.ordered_n ? k : INVALID_ID);
-                if (id != INVALID_ID) {
-                    const FusedSeg& sg = a.segs[cs];
-                    float4 o, d;
-                    load_ray(sg.rays, id - sg.slot_base, o, d);
-                    if (d.w > o.w) {
-                        if (sg.levels == 0u) {
-                            if (c == 0u) {  // a scene without triangles has no tree: the ray misses
-                                if (sg.any_hit) sg.flags[id - sg.slot_base] = 0u;
-                                else sg.hits[id - sg.slot_base] = RSH_HIT_NONE;
-                            }
-                        } else {
-                            seg = cs;
-                            slot = id - sg.slot_base;
-                            any = sg.any_hit != 0u;
-                            boxes = sg.wboxes;
-                            tris = sg.wtris;
-                            tmin = o.w;
-                            tcur = d.w;
-                            ix = safe_rcp(d.x);
-                            iy = safe_rcp(d.y);
-                            iz = safe_rcp(d.z);
-                            oix = o.x * ix;
-                            oiy = o.y * iy;
-                            oiz = o.z * iz;
-                            w = wt_setup(o, d);
-                            best = RSH_HIT_NONE;
-                            if (c == 0u) stk[0] = sg.wroot;
-                            sp = 1;
-                            has = true;
-                        }
-                    }
-                }
-            }
-            nk = min(nend, nk + __popc(need));
-            __syncwarp();
-        }
-        const uint32_t act = __ballot_sync(0xffffffffu, has && c == 0u);
-        if (!act) break;  // nothing in flight and nothing left to fetch
-        const uint32_t e = has ? stk[sp - 1] : 0u;
-        const bool node = has && (e >> E_LSHIFT) != 0u;
-        const uint32_t nn = __popc(__ballot_sync(0xffffffffu, node && c == 0u));
-        const uint32_t do_nodes = nn * 2u >= (uint32_t)__popc(act);
-        __syncwarp();
-        if (has && node == (do_nodes != 0u)) {
-            --sp;
-            const uint32_t idx = e & 0xFFFFFFu;
-            if (node) {
-                const uint32_t cnt = ((e >> 24) & 7u) + 1u;
-                if (c == 0u) ntests += cnt;
-                bool hit = false;
-                float tn = 0.0f;
-                uint32_t ent = 0;
-                if (c < cnt) {
-                    const float4 b0 = __ldg(boxes + 2ull * (idx + c)), b1 = __ldg(boxes + 2ull * (idx + c) + 1);
-                    hit = box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tn);
-                    ent = (__float_as_uint(b1.w) >> 31) ? idx + c : __float_as_uint(b0.w);
-                }
-                const uint32_t hm = (__ballot_sync(__activemask(), hit) >> gbase) & 0xFFu;
-                uint32_t rank;
-                if (any) {
-                    rank = __popc(hm & ((1u << c) - 1u));
-                } else {
-                    // hits farther than this one (equal distances: the higher child counts as farther)
-                    rank = 0;
-#pragma unroll
-                    for (uint32_t o = 1; o < 8; ++o) {
-                        const uint32_t j = (c + o) & 7u;
-                        const float tj = __shfl_sync(__activemask(), tn, gbase | j);
-                        if (((hm >> j) & 1u) && (tj > tn || (tj == tn && j > c))) ++rank;
-                    }
-                }
-                if (sp + cnt > G_STACK) {
-                    if (c == 0u) raise_device_error(a.err, RSH_DEVERR_OVERFLOW);
-                } else {
-                    if (hit) stk[sp + rank] = ent;
-                    sp += __popc(hm);
-                }
-            } else {
-                // the cluster's box against [tmin, current best]; a miss skips its triangles
-                const float4 b0 = __ldg(boxes + 2ull * idx), b1 = __ldg(boxes + 2ull * idx + 1);
-                const uint32_t t0 = __float_as_uint(b0.w), n = __float_as_uint(b1.w) & 0x7FFFFFFFu;
-                float tnb;
-                if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tnb)) {
-                    for (uint32_t base = 0; base < n; base += 8u) {
-                        const uint32_t m = min(8u, n - base);
-                        if (c == 0u) ttests += m;
-                        bool h = false;
-                        unsigned long long key = RSH_HIT_NONE;
-                        if (c < m) {
-                            const uint64_t tt = 3ull * (t0 + base + c);
-                            const float4 v0 = __ldg(tris + tt), v1 = __ldg(tris + tt + 1), v2 = __ldg(tris + tt + 2);
-                            float th;
-                            h = wt_hit(w, v0, v1, v2, th);
-                            if (h) key = hit_key(th, __float_as_uint(v0.w));
-                        }
-                        if (any) {
-                            if ((__ballot_sync(__activemask(), h) >> gbase) & 0xFFu) {
-                                best = 0ull;  // occluded
-                                sp = 0;
-                                break;
-                            }
-                        } else {
-#pragma unroll
-                            for (uint32_t o = 4; o > 0; o >>= 1) {
-                                const unsigned long long k2 = __shfl_xor_sync(__activemask(), key, o, 8);
-                                key = k2 < key ? k2 : key;
-                            }
-                            if (key < best) {
-                                best = key;
-                                tcur = fminf(tcur, __uint_as_float((uint32_t)(key >> 32)));
-                            }
-                        }
-                    }
-                }
-            }
-            if (sp == 0u) {
-                // the ray is done: its result, written by the group's first lane
-                if (c == 0u) {
-                    const FusedSeg& sg = a.segs[seg];
-                    if (any) sg.flags[slot] = best == 0ull ? RSH_OCCLUDED : 0u;
-                    else sg.hits[slot] = best;
-                }
-                has = false;
-            }
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        ntests += __shfl_xor_sync(0xffffffffu, ntests, d);
-        ttests += __shfl_xor_sync(0xffffffffu, ttests, d);
-    }
-    if (lane == 0) {
-        if (a.node_tests) atomicAdd(a.node_tests, ntests);
-        if (a.tri_tests) atomicAdd(a.tri_tests, ttests);
-    }
-}
-
 template <int U>
 static cudaError_t launch_fused_rays_u(const FusedArgs& a, cudaStream_t s) {
     int dev = 0, sms = 152, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-#if RSH_RAYS_GROUP8
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays_g8<U>, FW * 32, 0);
-#else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays<U>, FW * 32, 0);
-#endif
     if (per_sm < 1) per_sm = 1;
     if (a.blocks_per_sm && (int)a.blocks_per_sm < per_sm) per_sm = (int)a.blocks_per_sm;
     uint32_t grid = (uint32_t)(sms * per_sm);
     const uint32_t need = (a.units_max + FW - 1) / FW;
     if (need < grid) grid = need > 0 ? need : 1;
-#if RSH_RAYS_GROUP8
-    k_fused_rays_g8<U><<<grid, FW * 32, 0, s>>>(a);
-#else
     k_fused_rays<U><<<grid, FW * 32, 0, s>>>(a);
-#endif
     note_launch();
     return cudaGetLastError();
 }
