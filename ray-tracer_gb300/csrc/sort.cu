@@ -58,9 +58,28 @@ __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
             for (size_t i = tid; i < words / 4; i += nth) row[i] = make_uint4(0u, 0u, 0u, 0u);
         }
     }
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t k = __ldg(keys + i);
-        for (uint32_t p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8u * p)) & 255u], 1u);
+    // each thread counts a contiguous run of keys and adds equal consecutive digits up before one shared
+    // atomic: the keys arrive coherent (hash runs in ray order), so their upper digits repeat in long runs
+    // that would otherwise pile up on one shared counter
+    {
+        constexpr uint32_t RUN = 16;
+        const uint32_t nth = gridDim.x * blockDim.x;
+        for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * RUN; base < n; base += nth * RUN) {
+            const uint32_t end = min(n, base + RUN);
+            for (uint32_t p = 0; p < passes; ++p) {
+                uint32_t prev = (__ldg(keys + base) >> (8u * p)) & 255u, run = 0;
+                for (uint32_t i = base; i < end; ++i) {
+                    const uint32_t d = (__ldg(keys + i) >> (8u * p)) & 255u;
+                    if (d != prev) {
+                        atomicAdd(&sh[p][prev], run);
+                        prev = d;
+                        run = 0;
+                    }
+                    ++run;
+                }
+                atomicAdd(&sh[p][prev], run);
+            }
+        }
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < passes * 256u; i += blockDim.x) {
@@ -74,14 +93,32 @@ __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    if (threadIdx.x < passes) {
-        uint32_t* h = hist + 256u * threadIdx.x;
-        uint32_t acc = 0u;
-        for (uint32_t d = 0; d < 256u; ++d) {
-            const uint32_t v = __ldcg(h + d);
-            h[d] = acc;
-            acc += v;
+    // exclusive digit offsets of every pass: one block-wide scan of the 256 bins per pass
+    for (uint32_t p = 0; p < passes; ++p) {
+        uint32_t* h = hist + 256u * p;
+        const uint32_t t = threadIdx.x;  // blockDim.x == 256
+        const uint32_t v = __ldcg(h + t);
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((t & 31u) >= (uint32_t)o) x += y;
         }
+        if ((t & 31u) == 31u) sh[0][t >> 5] = x;  // the shared counters are free now
+        __syncthreads();
+        if (t < 32) {
+            uint32_t ws = t < 8u ? sh[0][t] : 0u;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, ws, o);
+                if (t >= (uint32_t)o) ws += y;
+            }
+            if (t < 8u) sh[1][t] = ws;
+        }
+        __syncthreads();
+        const uint32_t warp_off = (t >= 32u) ? sh[1][(t >> 5) - 1] : 0u;
+        h[t] = warp_off + x - v;
+        __syncthreads();
     }
 }
 
