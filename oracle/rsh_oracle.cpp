@@ -1186,8 +1186,10 @@ static void build_objh(const float* pos, uint32_t T, uint32_t cluster, const flo
 // triangles h.tris with search radius 8 -- each pass every cluster's nearest neighbour by merged-box area
 // (x y + y z) + x z (ties: the lower position), mutual pairs merge into a node at the lower position,
 // merged nodes numbered in position order -- then the triangles in depth-first order (left first), then the
-// breadth-first collapse to 8-wide nodes (open the largest-area child that is not a cluster of at most
-// `cluster` triangles, in place, while fewer than 8), children in consecutive slots from slot 1.
+// collapse to 8-wide nodes chosen by dynamic programming on the traversal cost (f(x, 1) = min(A (8 +
+// triangles) for a cluster of at most `cluster`, min over j of A (16 + j) + f(x, j)); f(x, k >= 2) = min
+// over i of f(left, i) + f(right, k - i); FP32, ties to the cluster, the smaller j, the smaller i), laid
+// out breadth first, every node's decomposition (left parts first) in consecutive slots from slot 1.
 namespace {
 struct PBox {
     float lo[3], hi[3];
@@ -1280,31 +1282,72 @@ static void build_box_tree(ObjH& h, float pad) {
     }
     h.wtris.resize(12ull * n);
     for (uint32_t k = 0; k < n; ++k) std::memcpy(&h.wtris[12ull * first[k]], &h.tris[12ull * k], 48);
-    // breadth-first collapse
+    // collapse costs (wide.cu): f(x, 1..8) and choices, children before parents (ids ascending)
     const uint32_t G = h.cluster;
-    auto is_cluster = [&](int32_t x) { return nodes[x].cnt <= G; };
+    const size_t N = nodes.size();
+    const float FINF = INF;
+    std::vector<float> fc(8 * N, FINF);
+    std::vector<uint32_t> choice(N, 0u);
+    const uint32_t CH_CLUSTER = 1u << 24;
+    for (size_t x = 0; x < N; ++x) {
+        float* f = &fc[8 * x];
+        uint32_t chw = 0;
+        if (x >= n) {
+            const float* fl = &fc[8ull * ch[x].first];
+            const float* fr = &fc[8ull * ch[x].second];
+            for (uint32_t k = 2; k <= 8; ++k) {
+                float best = FINF;
+                uint32_t bi = 1;
+                for (uint32_t i = 1; i < k; ++i) {
+                    const float c = fl[i - 1] + fr[k - i - 1];
+                    if (c < best) {
+                        best = c;
+                        bi = i;
+                    }
+                }
+                f[k - 1] = best;
+                chw |= bi << (3u * (k - 2u));
+            }
+        }
+        const float A = parea(nodes[x].lo, nodes[x].hi);
+        float best = FINF;
+        uint32_t bj = 0;
+        for (uint32_t j = 2; j <= 8; ++j) {
+            const float c = A * (16.0f + (float)j) + f[j - 1];
+            if (c < best) {
+                best = c;
+                bj = j;
+            }
+        }
+        const float ccl = nodes[x].cnt <= G ? A * (8.0f + (float)nodes[x].cnt) : FINF;
+        if (ccl <= best) {
+            f[0] = ccl;
+            chw |= CH_CLUSTER;
+        } else {
+            f[0] = best;
+            chw |= (bj - 2u) << 21;
+        }
+        choice[x] = chw;
+    }
+    // a node's children: the slots of its decomposition, left parts first; at the root a cluster is its
+    // own single child
     auto expand = [&](int32_t x, bool at_root, std::vector<int32_t>& c) {
         c.clear();
-        if (is_cluster(x)) {
+        if (choice[x] & CH_CLUSTER) {
             if (at_root) c.push_back(x);
             return;
         }
-        c.push_back(x);
-        for (;;) {
-            int best = -1;
-            float ba = -1.0f;
-            for (size_t q = 0; q < c.size(); ++q) {
-                if (is_cluster(c[q])) continue;
-                const float a = parea(nodes[c[q]].lo, nodes[c[q]].hi);
-                if (a > ba) {
-                    ba = a;
-                    best = (int)q;
-                }
+        std::vector<std::pair<int32_t, uint32_t>> st{{x, ((choice[x] >> 21) & 7u) + 2u}};
+        while (!st.empty()) {
+            const auto [y, k] = st.back();
+            st.pop_back();
+            if (k == 1u) {
+                c.push_back(y);
+                continue;
             }
-            if (best < 0 || c.size() + 1 > 8) break;
-            const int32_t y = c[best];
-            c[best] = ch[y].first;
-            c.insert(c.begin() + best + 1, ch[y].second);
+            const uint32_t si = (choice[y] >> (3u * (k - 2u))) & 7u;
+            st.push_back({ch[y].second, k - si});
+            st.push_back({ch[y].first, si});
         }
     };
     h.wbox.assign(8, 0.0f);  // slot 0: unused (the root has no slot)

@@ -11,10 +11,17 @@
 //     (x y + y z) + x z of its box extents, all in FP32, so the host restatement builds the same tree.
 //  2. Triangles laid out in the binary tree's depth-first order (left first), so every subtree's triangles
 //     are one contiguous range.
-//  3. Collapse to 8-wide nodes, breadth first: a node's children start as itself and, while there are
-//     fewer than 8, the child with the largest surface area that is not a cluster is replaced by its two
-//     children (in place, left then right); a subtree of at most `cluster` triangles is a cluster. Each
-//     node's children take consecutive slots, allocated level after level in queue order.
+//  3. Collapse to 8-wide nodes by the surface-area cost of the single-ray traversal, chosen by dynamic
+//     programming over the binary tree (children before parents, pass by pass): with A(x) the area
+//     measure of subtree x, f(x, k) = the least cost of covering x's subtree with exactly k child slots
+//     of its parent: f(x, 1) = min(A(x) (8 + triangles) if x has at most `cluster` triangles (a cluster),
+//     min over 2 <= j <= 8 of A(x) (16 + j) + f(x, j) (a node with j children)), ties to the cluster and
+//     to the smaller j; f(x, k >= 2) = min over 1 <= i < k of f(left, i) + f(right, k - i), ties to the
+//     smaller i; a single triangle has only f(., 1). The weights (16 + children per node step, 8 +
+//     triangles per cluster step) follow the traversal kernel, whose cost tracks its steps more than its
+//     box tests. Every f is an FP32 sum in a fixed order, so the host restatement makes the same choices.
+//     Then breadth first: a node's children are the slots of its decomposition (left parts first), in
+//     consecutive slots allocated level after level in queue order.
 // Slot layout (2 float4 per slot, padded box lo and hi): a cluster keeps its first triangle in lo.w and
 // 0x80000000 | its triangle count in hi.w; a node keeps its single-ray stack entry in lo.w,
 // 1 << 27 | (children - 1) << 24 | first child slot, and its child count in hi.w. Slot 0 is unused; the
@@ -136,47 +143,112 @@ __global__ void k_wide_tris(const float4* __restrict__ tris, uint32_t n, const u
     out[d + 2] = __ldg(tris + 3ull * k + 2);
 }
 
-RSH_DEV bool is_cluster(const WNode* nodes, int32_t x, uint32_t cluster) {
-    return __float_as_uint(nodes[x].lo.w) <= cluster;
+// per node of the binary tree: f(x, 1..8) and its choices packed in one word -- bits 3 (k - 2) .. for the
+// split i of f(x, k), k = 2..8; bits 21-23: j - 2 of the node choice; bit 24: x is a cluster
+constexpr float COST_NODE = 16.0f, COST_CLUSTER = 8.0f;
+constexpr uint32_t CH_CLUSTER = 1u << 24;
+
+RSH_DEV void collapse_costs(const WNode& w, uint32_t cluster, float* f, uint32_t& choice) {
+    const float A = box_area(w.lo, w.hi);
+    const uint32_t cnt = __float_as_uint(w.lo.w);
+    float best = __int_as_float(0x7f800000);
+    uint32_t bj = 0;
+    for (uint32_t j = 2; j <= 8; ++j) {
+        const float c = A * (COST_NODE + (float)j) + f[j - 1];
+        if (c < best) {
+            best = c;
+            bj = j;
+        }
+    }
+    const float ccl = cnt <= cluster ? A * (COST_CLUSTER + (float)cnt) : __int_as_float(0x7f800000);
+    if (ccl <= best) {
+        f[0] = ccl;
+        choice |= CH_CLUSTER;
+    } else {
+        f[0] = best;
+        choice |= (bj - 2u) << 21;
+    }
 }
 
-// one BFS level of the collapse: the children of every item (a node of the binary tree that is not a
-// cluster), at most 8 each, and their count. At the root (which has no slot of its own) a cluster is its
-// own single child.
-__global__ void k_wide_expand(const int32_t* __restrict__ items, uint32_t n, const WNode* __restrict__ nodes,
-                              const int2* __restrict__ chb, uint32_t cluster, bool root,
-                              int32_t* __restrict__ kids, uint32_t* __restrict__ nkids) {
+__global__ void k_collapse_leaves(const WNode* __restrict__ nodes, uint32_t n, uint32_t cluster, float* __restrict__ fc,
+                                  uint32_t* __restrict__ choice) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    float f[8];
+    for (int k = 0; k < 8; ++k) f[k] = __int_as_float(0x7f800000);
+    uint32_t ch = 0;
+    collapse_costs(nodes[x], cluster, f, ch);
+    for (int k = 0; k < 8; ++k) fc[8ull * x + k] = f[k];
+    choice[x] = ch;
+}
+
+// the nodes [b, e) of one PLOC pass (their children come from earlier passes)
+__global__ void k_collapse_pass(const WNode* __restrict__ nodes, const int2* __restrict__ chb, uint32_t b, uint32_t e,
+                                uint32_t cluster, float* __restrict__ fc, uint32_t* __restrict__ choice) {
+    const uint32_t x = b + blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= e) return;
+    const int2 lr = chb[x];
+    float fl[8], fr[8], f[8];
+    for (int k = 0; k < 8; ++k) {
+        fl[k] = fc[8ull * lr.x + k];
+        fr[k] = fc[8ull * lr.y + k];
+    }
+    uint32_t ch = 0;
+    f[0] = __int_as_float(0x7f800000);
+    for (uint32_t k = 2; k <= 8; ++k) {
+        float best = __int_as_float(0x7f800000);
+        uint32_t bi = 1;
+        for (uint32_t i = 1; i < k; ++i) {
+            const float c = fl[i - 1] + fr[k - i - 1];
+            if (c < best) {
+                best = c;
+                bi = i;
+            }
+        }
+        f[k - 1] = best;
+        ch |= bi << (3u * (k - 2u));
+    }
+    collapse_costs(nodes[x], cluster, f, ch);
+    for (int k = 0; k < 8; ++k) fc[8ull * x + k] = f[k];
+    choice[x] = ch;
+}
+
+// one BFS level of the collapse: the children of every item that is a node (its decomposition into the
+// j slots its choice says, left parts first), and their count; a cluster has none. At the root (which has
+// no slot of its own) a cluster is its own single child.
+__global__ void k_wide_expand(const int32_t* __restrict__ items, uint32_t n, const int2* __restrict__ chb,
+                              const uint32_t* __restrict__ choice, bool root, int32_t* __restrict__ kids,
+                              uint32_t* __restrict__ nkids) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int32_t x = items[i];
-    int32_t c[8];
+    const uint32_t cx = choice[x];
     uint32_t m = 0;
-    if (root && is_cluster(nodes, x, cluster)) {
-        c[0] = x;
-        m = 1;
-    } else if (!is_cluster(nodes, x, cluster)) {
-        c[0] = x;
-        m = 1;
-        for (;;) {
-            int32_t best = -1;
-            float ba = -1.0f;
-            for (uint32_t q = 0; q < m; ++q) {
-                if (is_cluster(nodes, c[q], cluster)) continue;
-                const float a = box_area(nodes[c[q]].lo, nodes[c[q]].hi);
-                if (a > ba) {
-                    ba = a;
-                    best = (int32_t)q;
-                }
+    if (cx & CH_CLUSTER) {
+        if (root) kids[8ull * i + m++] = x;
+    } else {
+        int32_t sy[8];
+        uint32_t sk[8], top = 0;
+        sy[0] = x;
+        sk[0] = ((cx >> 21) & 7u) + 2u;
+        top = 1;
+        while (top > 0) {
+            --top;
+            const int32_t y = sy[top];
+            const uint32_t k = sk[top];
+            if (k == 1u) {
+                kids[8ull * i + m++] = y;
+                continue;
             }
-            if (best < 0 || m + 1 > 8) break;
-            const int2 lr = chb[c[best]];
-            for (uint32_t q = m; q > (uint32_t)best + 1; --q) c[q] = c[q - 1];
-            c[best] = lr.x;
-            c[best + 1] = lr.y;
-            ++m;
+            const uint32_t si = (choice[y] >> (3u * (k - 2u))) & 7u;
+            const int2 lr = chb[y];
+            sy[top] = lr.y;  // the right part after the left one
+            sk[top] = k - si;
+            sy[top + 1] = lr.x;
+            sk[top + 1] = si;
+            top += 2;
         }
     }
-    for (uint32_t q = 0; q < m; ++q) kids[8ull * i + q] = c[q];
     nkids[i] = m;
 }
 
@@ -302,7 +374,8 @@ cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s) {
     int2* chb = nullptr;
     int32_t *cur = nullptr, *nxt = nullptr, *nn = nullptr, *kids = nullptr;
     uint32_t *keep = nullptr, *merge = nullptr, *kpos = nullptr, *mpos = nullptr, *sums = nullptr, *first = nullptr;
-    uint32_t *slots = nullptr, *nslots = nullptr, *nk = nullptr;
+    uint32_t *slots = nullptr, *nslots = nullptr, *nk = nullptr, *choice = nullptr;
+    float* fc = nullptr;
     cudaError_t e = cudaSuccess;
     const uint32_t nb = (n + SCAN_B - 1) / SCAN_B + 1;
     if ((e = alloc(nodes, cap_nodes)) || (e = alloc(chb, cap_nodes)) || (e = alloc(cur, n)) || (e = alloc(nxt, n)) ||
@@ -310,7 +383,9 @@ cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s) {
         (e = alloc(mpos, n + 1)) || (e = alloc(sums, nb)) || (e = alloc(first, cap_nodes)) ||
         (e = alloc(kids, 8ull * n)) || (e = alloc(nk, n)) || (e = alloc(slots, 2ull * n + 8)) ||
         (e = alloc(nslots, 2ull * n + 8)) || (e = alloc(h.wboxes, 2ull * (2ull * n + 8))) ||
-        (e = alloc(h.wtris, 3ull * n))) {
+        (e = alloc(h.wtris, 3ull * n)) || (e = alloc(fc, 8ull * cap_nodes)) || (e = alloc(choice, cap_nodes))) {
+        cudaFree(fc);
+        cudaFree(choice);
         cudaFree(nodes);
         cudaFree(chb);
         cudaFree(cur);
@@ -369,7 +444,19 @@ cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s) {
         note_launch();
         e = cudaGetLastError();
     }
-    // 3. collapse, breadth first: level items (binary node, slot); the root's slot is 0 (none)
+    // 3. collapse costs, children before parents (leaves, then the passes in order), then breadth first:
+    // level items (binary node, slot); the root's slot is 0 (none)
+    if (e == cudaSuccess) {
+        k_collapse_leaves<<<blocks(n), 256, 0, s>>>(nodes, n, cluster, fc, choice);
+        note_launch();
+        e = cudaGetLastError();
+    }
+    for (size_t p = 1; p < pass_begin.size() && e == cudaSuccess; ++p) {
+        const uint32_t b = pass_begin[p - 1], en = pass_begin[p];
+        k_collapse_pass<<<blocks(en - b), 256, 0, s>>>(nodes, chb, b, en, cluster, fc, choice);
+        note_launch();
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(h.wboxes, 0, 2 * sizeof(float4), s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(cur, &root, 4, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(slots, 0, 4, s);
@@ -377,7 +464,7 @@ cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s) {
     uint32_t items = 1, slot_base = 1, root_children = 0;
     bool at_root = true;
     while (items > 0 && e == cudaSuccess) {
-        k_wide_expand<<<blocks(items), 256, 0, s>>>(cur, items, nodes, chb, cluster, at_root, kids, nk);
+        k_wide_expand<<<blocks(items), 256, 0, s>>>(cur, items, chb, choice, at_root, kids, nk);
         note_launch();
         if ((e = scan_u32(nk, items, kpos, sums, s)) != cudaSuccess) break;
         k_wide_write<<<blocks(items), 256, 0, s>>>(cur, slots, items, nodes, first, kids, nk, kpos, slot_base, pad,
@@ -404,6 +491,8 @@ cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s) {
         }
     }
     cudaError_t e2 = cudaStreamSynchronize(s);
+    cudaFree(fc);
+    cudaFree(choice);
     cudaFree(nodes);
     cudaFree(chb);
     cudaFree(cur);
