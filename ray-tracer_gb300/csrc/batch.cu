@@ -277,7 +277,8 @@ rsh_status batch_prepare(rsh_ctx* ctx, const rsh_batch_segment* segs, uint32_t c
         f.boxes = sc->h.boxes;
         f.wboxes = sc->h.wboxes;
         f.wtris = sc->h.wtris;
-        f.wroot = sc->h.wroot;
+        f.wnodes = sc->h.wnodes;
+        f.wnroot = sc->h.wnroot;
         f.tri_count = sc->tri_count;
         f.cluster = sc->h.cluster;
         f.levels = sc->h.levels;

@@ -627,8 +627,9 @@ rsh_status rsh_scene_upload(rsh_ctx* ctx, const rsh_scene_desc* d, rsh_scene** o
     }
     uint32_t total = 0;
     for (uint32_t l = 0; l < sc->h.levels; ++l) total += sc->h.level_size[l];
-    // + the single-ray box tree: 2 float4 per slot (at most 2T + 8) and its own copy of the triangles
-    sc->bytes = tri_bytes * 3 + 8ull * T + 48ull * total + 32ull * (2ull * T + 8) + 48ull * T +
+    // + the single-ray box tree: 2 float4 per slot (at most 2T + 8), its traversal records (224 B per node,
+    // at most T + 4 nodes) and its own copy of the triangles
+    sc->bytes = tri_bytes * 3 + 8ull * T + 48ull * total + 32ull * (2ull * T + 8) + 224ull * (T + 4) + 48ull * T +
                 sizeof(rsh_material) * sc->material_count;
     ctx->allocated += sc->bytes;
     *out = sc;
@@ -652,6 +653,7 @@ rsh_status rsh_scene_destroy(rsh_ctx* ctx, rsh_scene* sc) {
     if (sc->h.boxes) cudaFree(sc->h.boxes);
     if (sc->h.wboxes) cudaFree(sc->h.wboxes);
     if (sc->h.wtris) cudaFree(sc->h.wtris);
+    if (sc->h.wnodes) cudaFree(sc->h.wnodes);
     if (ctx && ctx->allocated >= sc->bytes) ctx->allocated -= sc->bytes;
     delete sc;
     return RSH_OK;
@@ -681,7 +683,7 @@ rsh_status rsh_build_object_hierarchy(rsh_ctx* ctx, rsh_scene* sc, rsh_stream_t 
     }
     RSH_CUDA(cudaStreamSynchronize(s));
     for (void* p : {(void*)sc->h.spheres, (void*)sc->h.kids, (void*)sc->h.tris, (void*)sc->h.order,
-                    (void*)sc->h.boxes, (void*)sc->h.wboxes, (void*)sc->h.wtris})
+                    (void*)sc->h.boxes, (void*)sc->h.wboxes, (void*)sc->h.wtris, (void*)sc->h.wnodes})
         if (p) cudaFree(p);
     sc->h = ObjHierarchy();
     void* scr = nullptr;

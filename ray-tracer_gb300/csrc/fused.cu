@@ -573,8 +573,10 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
 // Rays-only form: every segment's switch level is at or above its tree's depth, so every ray is one job
 // from the root and no lane ever shares a ray. The rays descend the scene's single-ray box tree (wide.cu: an
 // 8-wide tree of mixed depth built by PLOC clustering, tighter than the object-sphere hierarchy's level
-// structure): a stack entry is a node's entry word from its box's lo.w, or a cluster's slot (a child is a
-// cluster when its hi.w has the top bit set; a cluster's hi.w holds its triangle count below that bit). The warp keeps no per-unit state: it takes work units
+// structure) in its traversal-record form: a stack entry is a node's REC_NODE | (children - 1) << 28 |
+// record index, or a cluster's slot (its box, first triangle and triangle count). A node step reads the
+// record's near planes and far planes for the ray's octant (12 float4 loads, no per-axis min / max) and
+// the entries of the children it pushes. The warp keeps no per-unit state: it takes work units
 // (RSH_RAYS_UNIT sorted rays, never straddling a segment) by atomic ticket, and every lane whose ray has
 // finished takes the next ray of the warp's current unit straight from global memory (its id from the
 // sorted order, the ray itself from the segment's array), fetching the next unit when the current one runs
@@ -611,8 +613,23 @@ RSH_DEV bool box_hit_fma(float4 b0, float4 b1, float ix, float iy, float iz, flo
     return tn <= tf;
 }
 
+// Entry (near) or exit (far) distances of four children of a traversal record from one plane of each axis:
+// near: max(tmin, tx, ty, tz); far: min(tmax, tx, ty, tz), each t = plane * (1 / d) - o * (1 / d). With the
+// plane chosen by the direction's sign (the lower plane is the near one for a positive component), tx equals
+// the min (near) or the max (far) of the two planes' distances that box_hit_fma takes, so both tests decide
+// every box alike.
+RSH_DEV void slab4(float4 px, float4 py, float4 pz, float ix, float iy, float iz, float oix, float oiy, float oiz,
+                   float lim, float* t, bool near) {
+    const float xs[4] = {px.x, px.y, px.z, px.w}, ys[4] = {py.x, py.y, py.z, py.w}, zs[4] = {pz.x, pz.y, pz.z, pz.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float tx = __fmaf_rn(xs[k], ix, -oix), ty = __fmaf_rn(ys[k], iy, -oiy), tz = __fmaf_rn(zs[k], iz, -oiz);
+        t[k] = near ? fmaxf(fmax3f(lim, tx, ty), tz) : fminf(fmin3f(lim, tx, ty), tz);
+    }
+}
+
 #ifndef RSH_RAYS_MIN_BLOCKS
-#define RSH_RAYS_MIN_BLOCKS 8
+#define RSH_RAYS_MIN_BLOCKS 7
 #endif
 #ifndef RSH_TAIL_PER_WARP
 #define RSH_TAIL_PER_WARP 16
@@ -627,7 +644,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     const uint32_t units = dev_count(a.d_units, a.units_max);
     const uint32_t tail = min(units, (uint32_t)RSH_TAIL_PER_WARP * gridDim.x * FW);
     const uint32_t head = units - tail, tickets = head + RSH_TAIL_SPLIT * tail;
-    unsigned long long ntests = 0, ttests = 0;
+    uint32_t ntests = 0, ttests = 0;  // the lane's counts, flushed to the launch's counters before 2^31
     // the warp's current unit: sorted rays [nk, nend) of segment cs
     uint32_t nk = 0, nend = 0, cs = 0;
     bool drained = false;
@@ -635,11 +652,13 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     bool has = false, any = false;
     uint32_t seg = 0, slot = 0;
     const float4* __restrict__ boxes = nullptr;
+    const float4* __restrict__ nodes = nullptr;
     const float4* __restrict__ tris = nullptr;
     int sp = 0;
     uint32_t stk[J_STACK];
     float ox = 0.f, oy = 0.f, oz = 0.f, tmin = 0.f, tcur = 0.f;
     float ix = 0.f, iy = 0.f, iz = 0.f, oix = 0.f, oiy = 0.f, oiz = 0.f;
+    uint32_t oct = 0;  // the direction's octant: bit a set when component a is negative
     RayWT w;
     unsigned long long best = RSH_HIT_NONE;
     for (;;) {
@@ -685,6 +704,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             slot = id - sg.slot_base;
                             any = sg.any_hit != 0u;
                             boxes = sg.wboxes;
+                            nodes = sg.wnodes;
                             tris = sg.wtris;
                             ox = o.x;
                             oy = o.y;
@@ -699,7 +719,8 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             oiz = oz * iz;
                             w = wt_setup(o, d);
                             best = RSH_HIT_NONE;
-                            stk[0] = sg.wroot;
+                            oct = (ix < 0.f ? 1u : 0u) | (iy < 0.f ? 2u : 0u) | (iz < 0.f ? 4u : 0u);
+                            stk[0] = sg.wnroot;
                             sp = 1;
                             has = true;
                         }
@@ -712,17 +733,16 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
         // one kind of step per iteration, the kind more lanes want
         bool do_nodes;
         {
-            const bool node = has && (stk[sp - 1] >> E_LSHIFT) != 0u;
+            const bool node = has && (stk[sp - 1] >> 31) != 0u;
             const uint32_t nn = __popc(__ballot_sync(0xffffffffu, node));
             const uint32_t nc = __popc(__ballot_sync(0xffffffffu, has && !node));
             do_nodes = nn >= nc;
         }
-        if (has && ((stk[sp - 1] >> E_LSHIFT) != 0u) == do_nodes) {
+        if (has && ((stk[sp - 1] >> 31) != 0u) == do_nodes) {
             const uint32_t e = stk[--sp];
-            const uint32_t L = e >> E_LSHIFT, idx = e & 0xFFFFFFu;
-            if (L == 0u) {
+            if (!(e >> 31)) {
                 // the cluster's box against [tmin, current best]; a miss skips its triangles
-                const float4 b0 = __ldg(boxes + 2ull * idx), b1 = __ldg(boxes + 2ull * idx + 1);
+                const float4 b0 = __ldg(boxes + 2ull * e), b1 = __ldg(boxes + 2ull * e + 1);
                 const uint32_t t0 = __float_as_uint(b0.w);  // the cluster's triangles: its box's link
                 uint32_t t1 = t0 + (__float_as_uint(b1.w) & 0x7FFFFFFFu);
                 float tnb;
@@ -746,54 +766,58 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                     }
                 }
             } else {
-                // the entry holds the children's link: up to 8 slots from `idx` on
-                const uint32_t cnt = ((e >> 24) & 7u) + 1u;
-                const float4* bb = boxes + 2ull * idx;
+                // a node record: the children's near planes and far planes, axis by axis, then their entries
+                const uint32_t cnt = ((e >> 28) & 7u) + 1u;
+                const float4* rec = nodes + REC_F4 * (size_t)(e & 0x0FFFFFFFu);
                 ntests += cnt;
                 if (sp + cnt > J_STACK) {
                     raise_device_error(a.err, RSH_DEVERR_OVERFLOW);
-                } else if (any) {
-                    // any hit: every child whose box the ray crosses is pushed as it is tested, in child
-                    // order (the last pops first): a cluster as its slot, a node as its entry word
-#pragma unroll
-                    for (uint32_t c = 0; c < 8; ++c) {
-                        if (c < cnt) {
-                            float tc;
-                            const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
-                            if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc))
-                                stk[sp++] = (__float_as_uint(b1.w) >> 31) ? idx + c : __float_as_uint(b0.w);
-                        }
-                    }
                 } else {
-                    // closest hit: the hits pushed farthest first, so that the nearest pops first (among
-                    // equal entry distances the lower child)
-                    float tcs[8];
-                    uint32_t hm = 0, cm = 0;
+                    const uint32_t nxo = (oct & 1u) << 1, nyo = 4u | (oct & 2u), nzo = 8u | ((oct >> 1) & 2u);
+                    float tn[8];
+                    uint32_t hm = 0;
 #pragma unroll
-                    for (uint32_t c = 0; c < 8; ++c) {
-                        tcs[c] = 0.0f;
-                        if (c < cnt) {
-                            float tc;
-                            const float4 b0 = __ldg(bb + 2 * c), b1 = __ldg(bb + 2 * c + 1);
-                            if (box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tc)) {
-                                hm |= 1u << c;
-                                cm |= (__float_as_uint(b1.w) >> 31) << c;
-                                tcs[c] = tc;
-                            }
+                    for (uint32_t h = 0; h < 2; ++h) {
+                        float n4[4], f4[4];
+                        slab4(__ldg(rec + nxo + h), __ldg(rec + nyo + h), __ldg(rec + nzo + h), ix, iy, iz, oix,
+                              oiy, oiz, tmin, n4, true);
+                        slab4(__ldg(rec + (nxo ^ 2u) + h), __ldg(rec + (nyo ^ 2u) + h), __ldg(rec + (nzo ^ 2u) + h),
+                              ix, iy, iz, oix, oiy, oiz, tcur, f4, false);
+#pragma unroll
+                        for (uint32_t k = 0; k < 4; ++k) {
+                            tn[4 * h + k] = n4[k];
+                            hm |= (n4[k] <= f4[k] ? 1u : 0u) << (4 * h + k);
                         }
                     }
-                    while (hm) {
-                        uint32_t bc = 0;
-                        float bt = -INFINITY;
+                    const uint32_t* ent = reinterpret_cast<const uint32_t*>(rec + 12);
+                    if (any) {
+                        // any hit: every child whose box the ray crosses is pushed in child order (the last
+                        // pops first)
 #pragma unroll
-                        for (uint32_t c = 0; c < 8; ++c)
-                            if (((hm >> c) & 1u) && tcs[c] >= bt) {
-                                bt = tcs[c];
-                                bc = c;
+                        for (uint32_t h = 0; h < 2; ++h) {
+                            if ((hm >> (4 * h)) & 15u) {
+                                const uint4 ee = __ldg(reinterpret_cast<const uint4*>(ent) + h);
+                                const uint32_t ce[4] = {ee.x, ee.y, ee.z, ee.w};
+#pragma unroll
+                                for (uint32_t k = 0; k < 4; ++k)
+                                    if ((hm >> (4 * h + k)) & 1u) stk[sp++] = ce[k];
                             }
-                        hm &= ~(1u << bc);
-                        // a child node's entry, from the box just tested (an L1 hit)
-                        stk[sp++] = ((cm >> bc) & 1u) ? idx + bc : __float_as_uint(__ldg(&bb[2 * bc].w));
+                        }
+                    } else {
+                        // closest hit: the hits pushed farthest first, so that the nearest pops first (among
+                        // equal entry distances the lower child)
+                        while (hm) {
+                            uint32_t bc = 0;
+                            float bt = -INFINITY;
+#pragma unroll
+                            for (uint32_t c = 0; c < 8; ++c)
+                                if (((hm >> c) & 1u) && tn[c] >= bt) {
+                                    bt = tn[c];
+                                    bc = c;
+                                }
+                            hm &= ~(1u << bc);
+                            stk[sp++] = __ldg(ent + bc);  // an L1 hit: the record was just read
+                        }
                     }
                 }
             }
@@ -803,17 +827,24 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                 if (any) sg.flags[slot] = best == 0ull ? RSH_OCCLUDED : 0u;
                 else sg.hits[slot] = best;
                 has = false;
+                // one ray adds fewer than 2^28 node tests (8 per slot) and 2^24 triangle tests
+                if ((ntests | ttests) >> 31) {
+                    if (a.node_tests) atomicAdd(a.node_tests, (unsigned long long)ntests);
+                    if (a.tri_tests) atomicAdd(a.tri_tests, (unsigned long long)ttests);
+                    ntests = ttests = 0;
+                }
             }
         }
     }
+    unsigned long long nt = ntests, tt = ttests;
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        ntests += __shfl_xor_sync(0xffffffffu, ntests, d);
-        ttests += __shfl_xor_sync(0xffffffffu, ttests, d);
+        nt += __shfl_xor_sync(0xffffffffu, nt, d);
+        tt += __shfl_xor_sync(0xffffffffu, tt, d);
     }
     if (lane == 0) {
-        if (a.node_tests) atomicAdd(a.node_tests, ntests);
-        if (a.tri_tests) atomicAdd(a.tri_tests, ttests);
+        if (a.node_tests) atomicAdd(a.node_tests, nt);
+        if (a.tri_tests) atomicAdd(a.tri_tests, tt);
     }
 }
 

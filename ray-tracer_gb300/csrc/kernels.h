@@ -136,7 +136,16 @@ struct ObjHierarchy {
     float4* wtris = nullptr;
     uint32_t wroot = 0;
     uint32_t wslots = 0;
+    // the same tree as traversal records (14 float4 per node: child boxes plane by plane, child entries)
+    float4* wnodes = nullptr;
+    uint32_t wnode_count = 0;
+    uint32_t wnroot = 0;           // the root's entry in record form
 };
+// A traversal record of the box tree: REC_F4 float4 (the eight children's box planes lo x, hi x, lo y, hi y,
+// lo z, hi z, 8 floats each, then their eight stack entries); a node's entry is REC_NODE | (children - 1)
+// << 28 | record index, a cluster's its slot index.
+constexpr uint32_t REC_F4 = 14;
+constexpr uint32_t REC_NODE = 0x80000000u;
 // Builds the single-ray box tree from h.tris (Morton order) and h.cluster; boxes widened by `pad`.
 cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s);
 cudaError_t build_object_hierarchy(const float4* positions_dev, uint32_t tri_count, uint32_t cluster,
@@ -198,9 +207,10 @@ struct FusedSeg {
     const uint32_t* kids;          // object-tree child ranges (level l at lvl_off[l] + l)
     const float4* tris;
     const float4* boxes;           // per node (like spheres): padded box lo, hi; lo.w / hi.w: child link
-    const float4* wboxes;          // the single-ray box tree (wide.cu), its triangles and its root's entry
-    const float4* wtris;
-    uint32_t wroot;
+    const float4* wboxes;          // the single-ray box tree (wide.cu): slots (cluster boxes), triangles,
+    const float4* wtris;           // traversal records and the root's record entry
+    const float4* wnodes;
+    uint32_t wnroot;
     uint32_t tri_count;
     uint32_t cluster;
     uint32_t levels;

@@ -283,6 +283,61 @@ __global__ void k_wide_write(const int32_t* __restrict__ items, const uint32_t* 
     boxes[2ull * s + 1] = make_float4(w.hi.x + pad, w.hi.y + pad, w.hi.z + pad, __uint_as_float(hw));
 }
 
+// Traversal records: the slot tree laid out again for the rays-only kernel, one record per node (per
+// block of consecutive child slots), REC_F4 float4 each: the eight children's padded boxes plane by plane
+// (lo x, hi x, lo y, hi y, lo z, hi z: 8 floats each) and their eight stack entries. A ray picks the near
+// and the far plane of each axis once per record from the sign of its direction, so a child's entry and
+// exit distances need no min / max per axis. An unused child has the empty box (lo = +inf, hi = -inf,
+// which every ray misses) and entry 0. A child's entry: a cluster's slot index (bit 31 clear), or a node's
+// REC_NODE | (children - 1) << 28 | record index (kernels.h).
+
+// start[f] = 1 and cnt[f] = children for the first child slot f of every node (the root's at slot 1)
+__global__ void k_rec_mark(const float4* __restrict__ boxes, uint32_t nslots, uint32_t root_children,
+                           uint32_t* __restrict__ start, uint32_t* __restrict__ cnt) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nslots) return;
+    if (t == 0u) {
+        start[1] = 1u;
+        cnt[1] = root_children;
+        return;
+    }
+    if (__float_as_uint(boxes[2ull * t + 1].w) & CLUSTER_BIT) return;
+    const uint32_t e = __float_as_uint(boxes[2ull * t].w);
+    const uint32_t f = e & 0xFFFFFFu;
+    start[f] = 1u;
+    cnt[f] = ((e >> 24) & 7u) + 1u;
+}
+
+__global__ void k_rec_write(const float4* __restrict__ boxes, uint32_t nslots, const uint32_t* __restrict__ start,
+                            const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ rid,
+                            float4* __restrict__ recs) {
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nslots || !start[f]) return;
+    const uint32_t n = cnt[f];
+    float* r = reinterpret_cast<float*>(recs + REC_F4 * (size_t)rid[f]);
+    uint32_t* re = reinterpret_cast<uint32_t*>(r + 48);
+    const float inf = __int_as_float(0x7f800000);
+    for (uint32_t c = 0; c < 8u; ++c) {
+        if (c < n) {
+            const uint32_t t = f + c;
+            const float4 b0 = boxes[2ull * t], b1 = boxes[2ull * t + 1];
+            r[c] = b0.x;
+            r[8 + c] = b1.x;
+            r[16 + c] = b0.y;
+            r[24 + c] = b1.y;
+            r[32 + c] = b0.z;
+            r[40 + c] = b1.z;
+            const uint32_t lw = __float_as_uint(b0.w);
+            re[c] = (__float_as_uint(b1.w) & CLUSTER_BIT) ? t
+                                                          : REC_NODE | (((lw >> 24) & 7u) << 28) | rid[lw & 0xFFFFFFu];
+        } else {
+            r[c] = r[16 + c] = r[32 + c] = inf;
+            r[8 + c] = r[24 + c] = r[40 + c] = -inf;
+            re[c] = 0u;
+        }
+    }
+}
+
 // exclusive scan of n u32 with the total at out[n]: per-block scans, a one-block scan of the block sums,
 // then the block offsets added (three launches; the build runs once per scene)
 constexpr uint32_t SCAN_B = 1024;
@@ -358,6 +413,35 @@ cudaError_t scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, uint32_t* su
 template <class T>
 cudaError_t alloc(T*& p, size_t count) {
     return cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * (count ? count : 1));
+}
+
+// The traversal records of a finished slot tree (slot 0 starts no block, so the root's children are
+// record 0).
+cudaError_t build_records(ObjHierarchy& h, uint32_t root_children, cudaStream_t s) {
+    const uint32_t ns = h.wslots;
+    uint32_t *start = nullptr, *cnt = nullptr, *rid = nullptr, *sums = nullptr;
+    uint32_t recs = 0;
+    cudaError_t e = cudaSuccess;
+    if (!(e = alloc(start, ns + 1)) && !(e = alloc(cnt, ns + 1)) && !(e = alloc(rid, ns + 1)) &&
+        !(e = alloc(sums, (ns + SCAN_B - 1) / SCAN_B + 1)) && !(e = cudaMemsetAsync(start, 0, 4ull * (ns + 1), s))) {
+        k_rec_mark<<<(ns + 255) / 256, 256, 0, s>>>(h.wboxes, ns, root_children, start, cnt);
+        note_launch();
+        if (!(e = scan_u32(start, ns, rid, sums, s)) &&
+            !(e = cudaMemcpyAsync(&recs, rid + ns, 4, cudaMemcpyDeviceToHost, s)) &&
+            !(e = cudaStreamSynchronize(s)) && !(e = alloc(h.wnodes, (size_t)REC_F4 * recs))) {
+            k_rec_write<<<(ns + 255) / 256, 256, 0, s>>>(h.wboxes, ns, start, cnt, rid, h.wnodes);
+            note_launch();
+            e = cudaGetLastError();
+            h.wnode_count = recs;
+            h.wnroot = REC_NODE | ((root_children - 1u) << 28);
+        }
+    }
+    const cudaError_t e2 = cudaStreamSynchronize(s);
+    cudaFree(start);
+    cudaFree(cnt);
+    cudaFree(rid);
+    cudaFree(sums);
+    return e != cudaSuccess ? e : e2;
 }
 
 }  // namespace
@@ -490,6 +574,8 @@ cudaError_t build_box_tree(ObjHierarchy& h, float pad, cudaStream_t s) {
             h.wslots = slot_base;
         }
     }
+    // 4. the traversal records
+    if (e == cudaSuccess) e = build_records(h, root_children, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
     cudaFree(fc);
     cudaFree(choice);
