@@ -488,11 +488,15 @@ inline bool box_hit(const float* b, const float inv[3], const float oi[3], float
 
 // One ray from the root of the single-ray box tree (wide.cu): the batched form's rays-only traversal
 // (fused.cu k_fused_rays). A stack entry is a node's entry word (its box's lo.w: 1 << 27 | (children - 1)
-// << 24 | first child slot) or a cluster's slot. A node step tests every child's box against [tmin, current
-// best] and pushes the hits: any hit in child order (the last child pops first), closest hit farthest first
-// (the nearest pops first; among equal entry distances the lower child). A cluster step tests the
-// cluster's box, then its triangles. Counts node tests (every child of a popped node) and triangle tests.
-// Returns false on a stack overflow (more than 96 entries).
+// << 24 | first child slot) or a cluster's slot, with the distance at which the ray enters its box (from
+// the parent's test; the root's is -inf). A closest-hit ray drops an entry whose entry distance lies beyond
+// its current best unread: no box inside it (children lie inside their parent's box) can be entered
+// earlier, and for a cluster this is exactly the outcome of testing its box again against the current
+// best. An any-hit ray's interval never shrinks, so it never drops one. A node step tests every child's box
+// against [tmin, current best] and pushes the hits: any hit in child order (the last child pops first),
+// closest hit farthest first (the nearest pops first; among equal entry distances the lower child). A
+// cluster step tests its triangles. Counts node tests (every child of a node that is stepped) and triangle
+// tests. Returns false on a stack overflow (more than 96 entries).
 bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint64_t& best, uint64_t& ntests,
                      uint64_t& ttests) {
     occluded = false;
@@ -503,15 +507,17 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
     const float oi[3] = {r.o[0] * inv[0], r.o[1] * inv[1], r.o[2] * inv[2]};
     float tcur = r.tmax;
     uint32_t stk[96];
+    float stt[96];
     int sp = 0;
-    stk[sp++] = h.wroot;
+    stk[sp] = h.wroot;
+    stt[sp++] = -INF;
     while (sp > 0) {
-        const uint32_t e = stk[--sp];
+        --sp;
+        const uint32_t e = stk[sp];
+        if (stt[sp] > tcur) continue;
         const uint32_t L = e >> 27, idx = e & 0xFFFFFFu;
         if (L == 0) {
             const float* b = &h.wbox[8ull * idx];
-            float tn;
-            if (!box_hit(b, inv, oi, r.tmin, tcur, tn)) continue;
             const uint32_t t0 = f2u(b[3]), t1 = t0 + (f2u(b[7]) & 0x7FFFFFFFu);
             for (uint32_t t = t0; t < t1; ++t) {
                 const float* v = &h.wtris[12ull * t];
@@ -558,7 +564,8 @@ bool ray_descend_box(const ObjH& h, const Ray& r, bool any, bool& occluded, uint
             }
             hm &= ~(1u << bc);
             const float* cb = &h.wbox[8ull * (idx + bc)];
-            stk[sp++] = (f2u(cb[7]) & 0x80000000u) ? idx + bc : f2u(cb[3]);
+            stk[sp] = (f2u(cb[7]) & 0x80000000u) ? idx + bc : f2u(cb[3]);
+            stt[sp++] = tcs[bc];
         }
     }
     return true;

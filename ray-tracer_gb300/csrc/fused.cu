@@ -651,16 +651,29 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     // the lane's ray
     bool has = false, any = false;
     uint32_t seg = 0, slot = 0;
-    const float4* __restrict__ boxes = nullptr;
     const float4* __restrict__ nodes = nullptr;
     const float4* __restrict__ tris = nullptr;
     int sp = 0;
     uint32_t stk[J_STACK];
+    float stt[J_STACK];  // closest hit: each entry's entry distance, from its parent's test
     float ox = 0.f, oy = 0.f, oz = 0.f, tmin = 0.f, tcur = 0.f;
     float ix = 0.f, iy = 0.f, iz = 0.f, oix = 0.f, oiy = 0.f, oiz = 0.f;
     uint32_t oct = 0;  // the direction's octant: bit a set when component a is negative
     RayWT w;
     unsigned long long best = RSH_HIT_NONE;
+    // the ray is done: its result, written by its own lane
+    auto finish = [&]() {
+        const FusedSeg& sg = a.segs[seg];
+        if (any) sg.flags[slot] = best == 0ull ? RSH_OCCLUDED : 0u;
+        else sg.hits[slot] = best;
+        has = false;
+        // one ray adds fewer than 2^28 node tests (8 per slot) and 2^24 triangle tests
+        if ((ntests | ttests) >> 31) {
+            if (a.node_tests) atomicAdd(a.node_tests, (unsigned long long)ntests);
+            if (a.tri_tests) atomicAdd(a.tri_tests, (unsigned long long)ttests);
+            ntests = ttests = 0;
+        }
+    };
     for (;;) {
         // idle lanes take the next rays of the warp's unit, units are fetched as they run out
         for (;;) {
@@ -703,7 +716,6 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             seg = cs;
                             slot = id - sg.slot_base;
                             any = sg.any_hit != 0u;
-                            boxes = sg.wboxes;
                             nodes = sg.wnodes;
                             tris = sg.wtris;
                             ox = o.x;
@@ -721,6 +733,7 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                             best = RSH_HIT_NONE;
                             oct = (ix < 0.f ? 1u : 0u) | (iy < 0.f ? 2u : 0u) | (iz < 0.f ? 4u : 0u);
                             stk[0] = sg.wnroot;
+                            stt[0] = -INFINITY;
                             sp = 1;
                             has = true;
                         }
@@ -730,6 +743,13 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
             nk = min(nend, nk + __popc(need));
         }
         if (!__any_sync(0xffffffffu, has)) break;  // nothing in flight and nothing left to fetch
+        // closest hit: entries that the ray enters beyond its current best are dropped unread (their
+        // subtrees cannot hold a nearer hit: a child's box lies inside its parent's, so no child is entered
+        // before its parent)
+        if (has && !any) {
+            while (sp > 0 && stt[sp - 1] > tcur) --sp;
+            if (sp == 0) finish();
+        }
         // one kind of step per iteration, the kind more lanes want
         bool do_nodes;
         {
@@ -741,12 +761,9 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
         if (has && ((stk[sp - 1] >> 31) != 0u) == do_nodes) {
             const uint32_t e = stk[--sp];
             if (!(e >> 31)) {
-                // the cluster's box against [tmin, current best]; a miss skips its triangles
-                const float4 b0 = __ldg(boxes + 2ull * e), b1 = __ldg(boxes + 2ull * e + 1);
-                const uint32_t t0 = __float_as_uint(b0.w);  // the cluster's triangles: its box's link
-                uint32_t t1 = t0 + (__float_as_uint(b1.w) & 0x7FFFFFFFu);
-                float tnb;
-                if (!box_hit_fma(b0, b1, ix, iy, iz, oix, oiy, oiz, tmin, tcur, tnb)) t1 = t0;
+                // a cluster: its triangles t0 .. t0 + count - 1 (its box was tested with the parent's
+                // children; a closest-hit ray re-checks only its entry distance, above)
+                const uint32_t t0 = e & 0x7FFFFFu, t1 = t0 + ((e >> 23) & 63u) + 1u;
                 for (uint32_t tt = t0; tt < t1; ++tt) {
                     const float4 v0 = __ldg(tris + 3ull * tt), v1 = __ldg(tris + 3ull * tt + 1),
                                  v2 = __ldg(tris + 3ull * tt + 2);
@@ -816,24 +833,13 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
                                     bc = c;
                                 }
                             hm &= ~(1u << bc);
-                            stk[sp++] = __ldg(ent + bc);  // an L1 hit: the record was just read
+                            stk[sp] = __ldg(ent + bc);  // an L1 hit: the record was just read
+                            stt[sp++] = bt;
                         }
                     }
                 }
             }
-            if (sp == 0) {
-                // the ray is done: its result, written by its own lane
-                const FusedSeg& sg = a.segs[seg];
-                if (any) sg.flags[slot] = best == 0ull ? RSH_OCCLUDED : 0u;
-                else sg.hits[slot] = best;
-                has = false;
-                // one ray adds fewer than 2^28 node tests (8 per slot) and 2^24 triangle tests
-                if ((ntests | ttests) >> 31) {
-                    if (a.node_tests) atomicAdd(a.node_tests, (unsigned long long)ntests);
-                    if (a.tri_tests) atomicAdd(a.tri_tests, (unsigned long long)ttests);
-                    ntests = ttests = 0;
-                }
-            }
+            if (sp == 0) finish();
         }
     }
     unsigned long long nt = ntests, tt = ttests;

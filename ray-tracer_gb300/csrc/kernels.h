@@ -143,7 +143,7 @@ struct ObjHierarchy {
 };
 // A traversal record of the box tree: REC_F4 float4 (the eight children's box planes lo x, hi x, lo y, hi y,
 // lo z, hi z, 8 floats each, then their eight stack entries); a node's entry is REC_NODE | (children - 1)
-// << 28 | record index, a cluster's its slot index.
+// << 28 | record index, a cluster's its first triangle | (triangles - 1) << 23.
 constexpr uint32_t REC_F4 = 14;
 constexpr uint32_t REC_NODE = 0x80000000u;
 // Builds the single-ray box tree from h.tris (Morton order) and h.cluster; boxes widened by `pad`.

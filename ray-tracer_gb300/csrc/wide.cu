@@ -288,8 +288,9 @@ __global__ void k_wide_write(const int32_t* __restrict__ items, const uint32_t* 
 // (lo x, hi x, lo y, hi y, lo z, hi z: 8 floats each) and their eight stack entries. A ray picks the near
 // and the far plane of each axis once per record from the sign of its direction, so a child's entry and
 // exit distances need no min / max per axis. An unused child has the empty box (lo = +inf, hi = -inf,
-// which every ray misses) and entry 0. A child's entry: a cluster's slot index (bit 31 clear), or a node's
-// REC_NODE | (children - 1) << 28 | record index (kernels.h).
+// which every ray misses) and entry 0. A child's entry: a cluster's first triangle | (triangles - 1) << 23
+// (bit 31 clear; fewer than 2^23 triangles, at most 64 per cluster), or a node's REC_NODE | (children - 1)
+// << 28 | record index (kernels.h).
 
 // start[f] = 1 and cnt[f] = children for the first child slot f of every node (the root's at slot 1)
 __global__ void k_rec_mark(const float4* __restrict__ boxes, uint32_t nslots, uint32_t root_children,
@@ -328,8 +329,9 @@ __global__ void k_rec_write(const float4* __restrict__ boxes, uint32_t nslots, c
             r[32 + c] = b0.z;
             r[40 + c] = b1.z;
             const uint32_t lw = __float_as_uint(b0.w);
-            re[c] = (__float_as_uint(b1.w) & CLUSTER_BIT) ? t
-                                                          : REC_NODE | (((lw >> 24) & 7u) << 28) | rid[lw & 0xFFFFFFu];
+            const uint32_t hw = __float_as_uint(b1.w);
+            re[c] = (hw & CLUSTER_BIT) ? lw | ((hw - CLUSTER_BIT - 1u) << 23)
+                                       : REC_NODE | (((lw >> 24) & 7u) << 28) | rid[lw & 0xFFFFFFu];
         } else {
             r[c] = r[16 + c] = r[32 + c] = inf;
             r[8 + c] = r[24 + c] = r[40 + c] = -inf;
