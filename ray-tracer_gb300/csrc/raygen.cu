@@ -83,67 +83,87 @@ RSH_DEV void batch_key_out(const BatchKeyOut& bk, uint32_t slot, bool in_range, 
     if (threadIdx.x == 0 && s_cnt) atomicAdd(bk.count, s_cnt);
 }
 
-__global__ void k_raygen_shadow(const float4* __restrict__ spos, const float4* __restrict__ snrm,
-                                uint32_t w, uint32_t h, LightsP lights, float eps, HashP hp,
-                                rsh_ray* rays, uint32_t* keys, BatchKeyOut bk) {
+// One thread per pixel: the pixel's surface point and normal are read and the normal normalised once,
+// then its V = L x S slots are written (slot = x + W (v + V y), RayTracer.cu:700-702 with S samples per
+// light), each with the same arithmetic as a thread per slot would use. The block's rays are counted once
+// (BatchKeyOut).
+__global__ void __launch_bounds__(128) k_raygen_shadow(const float4* __restrict__ spos,
+                                                       const float4* __restrict__ snrm, uint32_t w, uint32_t h,
+                                                       LightsP lights, float eps, HashP hp, rsh_ray* rays,
+                                                       uint32_t* keys, BatchKeyOut bk) {
+    __shared__ uint32_t s_cnt;
     const uint32_t L = lights.count, S = lights.samples ? lights.samples : 1u, V = L * S;
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in_range = slot < w * h * V;
-    bool valid = false;
-    float4 ro = make_float4(0.f, 0.f, 0.f, 0.f), rd = make_float4(0.f, 0.f, 0.f, -1.f);
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in_range = pix < w * h;
+    uint32_t nvalid = 0;
+    if (threadIdx.x == 0) s_cnt = 0u;
     if (in_range) {
-        // slot = x + W*(v + L*S*y), v = l*S + s  (RayTracer.cu:700-702 with S samples per light)
-        const uint32_t x = slot % w;
-        const uint32_t v = (slot / w) % V;
-        const uint32_t y = slot / (w * V);
-        const uint32_t l = v / S, s = v % S;
-        const uint32_t pix = y * w + x;
+        const uint32_t y = pix / w, x = pix - y * w;
         const float4 p4 = __ldg(spos + pix);
-        uint32_t key = RSH_KEY_NONE;
-        if (p4.w != 0.0f) {
-            const v3 p = mk3(p4);
-            const v3 nn = norm3(mk3(__ldg(snrm + pix)));
-            const v3 lp = mk3(lights.pos[l][0], lights.pos[l][1], lights.pos[l][2]);
-            const v3 vl = p - lp;
-            const float len = len3(vl);
-            const v3 d = v3{vl.x / len, vl.y / len, vl.z / len};
-            const float diffuse = dot3(d, -nn);
-            const float tmax = len - 2.0f * eps;
-            if (diffuse > 0.0f && tmax > eps) {
-                v3 src = lp, dir = d;
-                float tm = tmax;
-                bool ok = true;
-                if (S > 1) {  // a sample of the 4x4 grid: its own origin, direction and interval
-                    src = soft_sample_pos(lp, d, s);
-                    const v3 vs = p - src;
-                    const float ls = len3(vs);
-                    dir = v3{vs.x / ls, vs.y / ls, vs.z / ls};
-                    tm = ls - 2.0f * eps;
-                    ok = tm > eps;
-                }
-                if (ok) {
-                    const v3 o = src + dir * eps;
-                    ro = make_float4(o.x, o.y, o.z, eps);
-                    rd = make_float4(dir.x, dir.y, dir.z, tm);
-                    store_ray(rays, slot, ro, rd);
-                    key = keys ? ray_hash(o.x, o.y, o.z, dir.x, dir.y, dir.z, hp, v) : 0u;
-                    valid = true;
+        const bool surface = p4.w != 0.0f;
+        const v3 p = mk3(p4);
+        const v3 nn = surface ? norm3(mk3(__ldg(snrm + pix))) : v3{0.f, 0.f, 0.f};
+        for (uint32_t v = 0; v < V; ++v) {
+            const uint32_t slot = x + w * (v + V * y);
+            const uint32_t l = S == 1u ? v : v / S, sm = S == 1u ? 0u : v % S;
+            bool valid = false;
+            float4 ro = make_float4(0.f, 0.f, 0.f, 0.f), rd = make_float4(0.f, 0.f, 0.f, -1.f);
+            uint32_t key = RSH_KEY_NONE;
+            if (surface) {
+                const v3 lp = mk3(lights.pos[l][0], lights.pos[l][1], lights.pos[l][2]);
+                const v3 vl = p - lp;
+                const float len = len3(vl);
+                const v3 d = v3{vl.x / len, vl.y / len, vl.z / len};
+                const float diffuse = dot3(d, -nn);
+                const float tmax = len - 2.0f * eps;
+                if (diffuse > 0.0f && tmax > eps) {
+                    v3 src = lp, dir = d;
+                    float tm = tmax;
+                    bool ok = true;
+                    if (S > 1) {  // a sample of the 4x4 grid: its own origin, direction and interval
+                        src = soft_sample_pos(lp, d, sm);
+                        const v3 vs = p - src;
+                        const float ls = len3(vs);
+                        dir = v3{vs.x / ls, vs.y / ls, vs.z / ls};
+                        tm = ls - 2.0f * eps;
+                        ok = tm > eps;
+                    }
+                    if (ok) {
+                        const v3 o = src + dir * eps;
+                        ro = make_float4(o.x, o.y, o.z, eps);
+                        rd = make_float4(dir.x, dir.y, dir.z, tm);
+                        key = keys ? ray_hash(o.x, o.y, o.z, dir.x, dir.y, dir.z, hp, v) : 0u;
+                        valid = true;
+                    }
                 }
             }
+            // an empty slot holds an explicit no-ray (tmax < tmin) for consumers without keys
+            store_ray(rays, slot, ro, rd);
+            if (keys) keys[slot] = key;
+            if (bk.keys) {
+                bk.keys[slot] = valid ? bk.tag | (ray_hash(ro.x, ro.y, ro.z, rd.x, rd.y, rd.z, bk.hp, 0u) >> bk.drop)
+                                      : RSH_KEY_NONE;
+                if (bk.flags) bk.flags[slot] = 0u;
+                else bk.hits[slot] = RSH_HIT_NONE;
+            }
+            nvalid += valid ? 1u : 0u;
         }
-        // empty slot: an explicit no-ray (tmax < tmin) for consumers without keys
-        if (!valid) store_ray(rays, slot, ro, rd);
-        if (keys) keys[slot] = key;
     }
-    if (bk.keys) batch_key_out(bk, slot, in_range, valid, ro, rd);
+    if (bk.keys) {
+        __syncthreads();
+        const uint32_t c = __reduce_add_sync(0xffffffffu, nvalid);
+        if (lane_id() == 0 && c) atomicAdd(&s_cnt, c);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_cnt) atomicAdd(bk.count, s_cnt);
+    }
 }
 
 cudaError_t launch_raygen_shadow(const float4* spos, const float4* snrm, uint32_t w, uint32_t h,
                                  const LightsP& lights, float eps, const HashP& hp, rsh_ray* rays,
                                  uint32_t* keys, cudaStream_t s, const BatchKeyOut& bk) {
-    const uint32_t n = w * h * lights.count * (lights.samples ? lights.samples : 1u);
-    if (n == 0) return cudaSuccess;
-    k_raygen_shadow<<<(n + 255u) / 256u, 256, 0, s>>>(spos, snrm, w, h, lights, eps, hp, rays, keys, bk);
+    const uint32_t n = w * h;
+    if (n == 0 || lights.count == 0) return cudaSuccess;
+    k_raygen_shadow<<<(n + 127u) / 128u, 128, 0, s>>>(spos, snrm, w, h, lights, eps, hp, rays, keys, bk);
     note_launch();
     return cudaGetLastError();
 }
