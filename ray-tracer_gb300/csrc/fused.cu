@@ -613,6 +613,17 @@ RSH_DEV bool box_hit_fma(float4 b0, float4 b1, float ix, float iy, float iz, flo
     return tn <= tf;
 }
 
+// Two plane distances at once: the packed FP32 fused multiply-add (fma.rn.f32x2, sm_100 and later), each
+// half rounded exactly like a scalar fma.rn.
+RSH_DEV void fma2(float a0, float a1, float b, float c, float& r0, float& r1) {
+    unsigned long long ra, rb, rc, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a0), "f"(a1));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(rb) : "f"(b));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(rc) : "f"(c));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r0), "=f"(r1) : "l"(rd));
+}
+
 // Entry (near) or exit (far) distances of four children of a traversal record from one plane of each axis:
 // near: max(tmin, tx, ty, tz); far: min(tmax, tx, ty, tz), each t = plane * (1 / d) - o * (1 / d). With the
 // plane chosen by the direction's sign (the lower plane is the near one for a positive component), tx equals
@@ -620,12 +631,16 @@ RSH_DEV bool box_hit_fma(float4 b0, float4 b1, float ix, float iy, float iz, flo
 // every box alike.
 RSH_DEV void slab4(float4 px, float4 py, float4 pz, float ix, float iy, float iz, float oix, float oiy, float oiz,
                    float lim, float* t, bool near) {
-    const float xs[4] = {px.x, px.y, px.z, px.w}, ys[4] = {py.x, py.y, py.z, py.w}, zs[4] = {pz.x, pz.y, pz.z, pz.w};
+    float tx[4], ty[4], tz[4];
+    fma2(px.x, px.y, ix, -oix, tx[0], tx[1]);
+    fma2(px.z, px.w, ix, -oix, tx[2], tx[3]);
+    fma2(py.x, py.y, iy, -oiy, ty[0], ty[1]);
+    fma2(py.z, py.w, iy, -oiy, ty[2], ty[3]);
+    fma2(pz.x, pz.y, iz, -oiz, tz[0], tz[1]);
+    fma2(pz.z, pz.w, iz, -oiz, tz[2], tz[3]);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float tx = __fmaf_rn(xs[k], ix, -oix), ty = __fmaf_rn(ys[k], iy, -oiy), tz = __fmaf_rn(zs[k], iz, -oiz);
-        t[k] = near ? fmaxf(fmax3f(lim, tx, ty), tz) : fminf(fmin3f(lim, tx, ty), tz);
-    }
+    for (int k = 0; k < 4; ++k)
+        t[k] = near ? fmaxf(fmax3f(lim, tx[k], ty[k]), tz[k]) : fminf(fmin3f(lim, tx[k], ty[k]), tz[k]);
 }
 
 #ifndef RSH_RAYS_MIN_BLOCKS
