@@ -331,7 +331,9 @@ rsh_status rsh_write_png(const char* path, const uint32_t* rgba, uint32_t width,
 rsh_status rsh_hash_params_make(const float lo[3], const float hi[3], uint32_t grid_bits,
                                 uint32_t dir_log2, uint32_t tag_bits, rsh_hash_params* out);
 
-/* Primary (camera) rays in 8x8 pixel-tile order: ray k belongs to pixel rsh_tile_pixel(k).
+/* Primary (camera) rays in 8x8 pixel-tile order, tile rows from the image's middle outwards (rows m, m-1,
+ * m+1, m-2, ... with m = tile rows / 2; the longest primary rays, usually in the view's centre band, are
+ * traced first): ray k belongs to pixel pixel_of_ray[k] (0xFFFFFFFF: padding of a partial tile, no ray).
  * Replaces the GL rasteriser of the G-buffer (FrameBuffer.cpp:55-140). */
 rsh_status rsh_raygen_primary(const rsh_camera* cam, uint32_t width, uint32_t height,
                               rsh_ray* rays, uint32_t* pixel_of_ray, rsh_stream_t stream);

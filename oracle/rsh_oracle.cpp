@@ -637,7 +637,9 @@ void orc_raygen_primary(const float* cam /*eye,dir,right,up*/, uint32_t W, uint3
     for (int64_t kk = 0; kk < (int64_t)n; ++kk) {
         const uint32_t k = (uint32_t)kk;
         const uint32_t tile = k >> 6, within = k & 63u;
-        const uint32_t x = (tile % tx) * 8 + (within & 7u), y = (tile / tx) * 8 + (within >> 3);
+        // tile rows from the image's middle outwards (raygen.cu tile_row)
+        const uint32_t tr = tile / tx, m = ty >> 1, row = (tr & 1u) ? m - ((tr + 1u) >> 1) : m + (tr >> 1);
+        const uint32_t x = (tile % tx) * 8 + (within & 7u), y = row * 8 + (within >> 3);
         Ray r{};
         r.o[0] = cam[0];
         r.o[1] = cam[1];

@@ -13,13 +13,21 @@
 namespace rsh {
 
 // ------------------------------------------------------------------ primary rays (tile order)
-__global__ void k_raygen_primary(CameraP cam, uint32_t w, uint32_t h, uint32_t tiles_x, uint32_t n,
+// Tile row r of the ray order is image tile row tile_row(r): from the middle outwards (m, m - 1, m + 1,
+// m - 2, ... with m = rows / 2). Primary rays run longest in the view's centre band (on typical views the
+// horizon, where rays travel far), so a persistent traversal starts them first instead of ending on them.
+RSH_DEV uint32_t tile_row(uint32_t r, uint32_t rows) {
+    const uint32_t m = rows >> 1;
+    return (r & 1u) ? m - ((r + 1u) >> 1) : m + (r >> 1);
+}
+
+__global__ void k_raygen_primary(CameraP cam, uint32_t w, uint32_t h, uint32_t tiles_x, uint32_t tiles_y, uint32_t n,
                                  rsh_ray* rays, uint32_t* pixel_of_ray) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t tile = k >> 6, within = k & 63u;
     const uint32_t x = (tile % tiles_x) * 8u + (within & 7u);
-    const uint32_t y = (tile / tiles_x) * 8u + (within >> 3);
+    const uint32_t y = tile_row(tile / tiles_x, tiles_y) * 8u + (within >> 3);
     float4 o = make_float4(cam.eye[0], cam.eye[1], cam.eye[2], 0.0f);
     float4 d;
     if (x < w && y < h) {
@@ -43,7 +51,7 @@ cudaError_t launch_raygen_primary(const CameraP& cam, uint32_t w, uint32_t h, rs
     const uint32_t tx = (w + 7u) / 8u, ty = (h + 7u) / 8u;
     const uint32_t n = tx * ty * 64u;
     if (n == 0) return cudaSuccess;
-    k_raygen_primary<<<(n + 255u) / 256u, 256, 0, s>>>(cam, w, h, tx, n, rays, pixel_of_ray);
+    k_raygen_primary<<<(n + 255u) / 256u, 256, 0, s>>>(cam, w, h, tx, ty, n, rays, pixel_of_ray);
     note_launch();
     return cudaGetLastError();
 }
