@@ -189,7 +189,8 @@ def cpu_baseline(s, crop=None, threads=None, steps=1, min_seconds=0.0, max_passe
     own rays) or a centred crop of it: primary hits, then `depth` bounces of shadow + reflection rays.
       algo "box":    the headline's own algorithm, the batched form's rays-only traversal restated: every
                      ray descends the scene's single-ray box tree (PLOC, 8-wide) from the root, one ray per
-                     host thread at a time (oracle ObjH.trace_box; the GPU's counters equal its counts);
+                     host thread at a time (oracle ObjH.trace_box; with RSH_FLAG_SEQUENTIAL_RAYS the GPU's counters
+                     equal its counts);
       algo "packet": the reference's stage order, compress -> sort -> decompress -> ray hierarchy -> packet
                      traversal + intersection (oracle ObjH.trace_keyed).
     Times the secondary part only (the GPU metric's window: ray generation to the last intersection of

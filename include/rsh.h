@@ -161,6 +161,14 @@ typedef struct rsh_config {
 /* Batched form: sort the hashed slots directly instead of their runs of equal keys (no compression or
  * decompression), for incoherent batches whose keys hardly repeat; rsh_autotune_scenes tries both. */
 #define RSH_FLAG_NO_COMPRESS 16u
+/* Batched form: every ray is traced by one lane from its first step to its last. By default, once a warp
+ * of the rays-only kernel has no ray left to take and at most 16 of its lanes still trace one, its idle
+ * lanes take subtrees (stack entries) of those rays, which shortens launches that would end on a few long
+ * rays (scenes with long sight lines); results are the same either way. The default costs the steps about
+ * 4% (the kernel runs at its register limit) and changes the node and triangle test counts through the
+ * order the hits are met in; with this flag the counts equal a sequential traversal's, ray by ray, and
+ * scenes whose launches end evenly run faster. */
+#define RSH_FLAG_SEQUENTIAL_RAYS 32u
 #define RSH_FLAG_RAH 4u            /* plain path: ray-hierarchy ablation without hashing/sorting: packets
                                       of consecutive trimmed rays (the reference's algorithm 1 "RAH",
                                       main.cpp:1016-1037) */

@@ -449,6 +449,7 @@ rsh_status batch_enqueue(rsh_ctx* ctx, BatchPlan& pl, cudaStream_t s, char* pre_
     fa.work = static_cast<uint32_t*>(pl.work);
     fa.rays_only = pl.rays_only;
     fa.blocks_per_sm = ctx->cfg.fused_blocks;
+    fa.share_tail = (ctx->cfg.flags & RSH_FLAG_SEQUENTIAL_RAYS) ? 0u : 1u;
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;
@@ -500,6 +501,7 @@ rsh_status batch_trace_ordered(rsh_ctx* ctx, const rsh_batch_segment& seg, cudaS
     fa.work = static_cast<uint32_t*>(pl.work);
     fa.rays_only = 1;
     fa.blocks_per_sm = ctx->cfg.fused_blocks;
+    fa.share_tail = (ctx->cfg.flags & RSH_FLAG_SEQUENTIAL_RAYS) ? 0u : 1u;
     fa.node_tests = ctx->d_stats;
     fa.tri_tests = ctx->d_stats + 1;
     fa.err = ctx->d_err;

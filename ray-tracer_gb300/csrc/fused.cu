@@ -646,6 +646,9 @@ RSH_DEV void slab4(float4 px, float4 py, float4 pz, float ix, float iy, float iz
 #ifndef RSH_RAYS_MIN_BLOCKS
 #define RSH_RAYS_MIN_BLOCKS 7
 #endif
+#ifndef RSH_SHARE_BUSY
+#define RSH_SHARE_BUSY 16  // busy lanes at or below which a drained warp shares its rays (SHARE)
+#endif
 #ifndef RSH_TAIL_PER_WARP
 #define RSH_TAIL_PER_WARP 16
 #endif
@@ -653,8 +656,12 @@ RSH_DEV void slab4(float4 px, float4 py, float4 pz, float ix, float iy, float iz
 #define RSH_TAIL_SPLIT 2
 #endif
 
-template <int U>
+template <int U, bool SHARE>
 __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(FusedArgs a) {
+    // SHARE: a drained warp's rays shared among its idle lanes; the records of the rays being shared, one per
+    // lane: the owner's best hit key (closest hit), occluded (any hit), helpers still on a subtree of it
+    __shared__ unsigned long long sh_best[SHARE ? FW : 1][32];
+    __shared__ uint32_t sh_occ[SHARE ? FW : 1][32], sh_pend[SHARE ? FW : 1][32];
     const uint32_t lane = lane_id();
     const uint32_t units = dev_count(a.d_units, a.units_max);
     const uint32_t tail = min(units, (uint32_t)RSH_TAIL_PER_WARP * gridDim.x * FW);
@@ -676,8 +683,16 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     uint32_t oct = 0;  // the direction's octant: bit a set when component a is negative
     RayWT w;
     unsigned long long best = RSH_HIT_NONE;
-    // the ray is done: its result, written by its own lane
+    bool sharing = false;  // warp-uniform (SHARE): the warp shares its last rays
+    bool done = false;     // sharing: the lane's subtree is done, its result not yet merged
+    uint32_t own = lane;   // sharing: the lane whose ray this lane works on
+    // the ray is done: its result, written by its own lane (while sharing: merged at the loop's top)
     auto finish = [&]() {
+        if (SHARE && sharing) {
+            done = true;
+            has = false;
+            return;
+        }
         const FusedSeg& sg = a.segs[seg];
         if (any) sg.flags[slot] = best == 0ull ? RSH_OCCLUDED : 0u;
         else sg.hits[slot] = best;
@@ -757,7 +772,109 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
             }
             nk = min(nend, nk + __popc(need));
         }
-        if (!__any_sync(0xffffffffu, has)) break;  // nothing in flight and nothing left to fetch
+        if (!__any_sync(0xffffffffu, has || (SHARE && done))) break;  // nothing in flight, nothing to fetch
+        // SHARE: once no ray is left to take and at most RSH_SHARE_BUSY lanes still trace one, idle lanes take
+        // stack entries (subtrees) of the warp's rays in flight, so that a long ray near the launch's end
+        // runs on many lanes instead of one. A ray's lane (its owner) keeps its result; a helper merges its
+        // own into the owner's record when its subtree is done (atomicMin of the hit key, or the occluded
+        // flag), and the owner writes the result once its stack is empty and no helper is left. Everything
+        // happens here, between steps: the steps themselves are the sequential ones.
+        if (SHARE && drained && (sharing || __popc(__ballot_sync(0xffffffffu, has)) <= RSH_SHARE_BUSY)) {
+            const uint32_t wp = threadIdx.x >> 5;
+            if (!sharing) {
+                sh_best[wp][lane] = has ? best : RSH_HIT_NONE;
+                sh_occ[wp][lane] = 0u;
+                sh_pend[wp][lane] = 0u;
+                own = lane;
+                sharing = true;
+            }
+            __syncwarp();
+            if (has) {
+                if (any) {
+                    if (sh_occ[wp][own]) {
+                        sp = 0;
+                        done = true;
+                        has = false;
+                    }
+                } else {
+                    tcur = fminf(tcur, __uint_as_float((uint32_t)(sh_best[wp][own] >> 32)));
+                }
+            }
+            if (done && own == lane && sh_pend[wp][lane] == 0u) {
+                // the owner, with no helper left: the ray's merged result
+                if (any) best = (best == 0ull || sh_occ[wp][lane]) ? 0ull : best;
+                else best = min(best, sh_best[wp][lane]);
+                const FusedSeg& sg = a.segs[seg];
+                if (any) sg.flags[slot] = best == 0ull ? RSH_OCCLUDED : 0u;
+                else sg.hits[slot] = best;
+                done = false;
+            } else if (done && own != lane) {
+                // a helper's subtree is done: its result into the owner's record
+                if (any) {
+                    if (best == 0ull) sh_occ[wp][own] = 1u;
+                } else {
+                    atomicMin(&sh_best[wp][own], best);
+                }
+                atomicSub(&sh_pend[wp][own], 1u);
+                done = false;
+            }
+            __syncwarp();
+            const uint32_t idle = __ballot_sync(0xffffffffu, !has && !done);
+            const uint32_t donors = __ballot_sync(0xffffffffu, has && sp >= 2);
+            if (idle && donors) {
+                const uint32_t r = __popc(idle & lanemask_lt());
+                const bool recv = !has && !done && r < (uint32_t)__popc(donors);
+                const uint32_t src = recv ? __fns(donors, 0u, (int)r + 1) : lane;
+                const bool give = has && sp >= 2 && (uint32_t)__popc(donors & lanemask_lt()) < (uint32_t)__popc(idle);
+                uint32_t ge = 0u;
+                float gt = 0.0f;
+                if (give) {
+                    --sp;
+                    ge = stk[sp];
+                    gt = stt[sp];
+                }
+                ge = __shfl_sync(0xffffffffu, ge, src);
+                gt = __shfl_sync(0xffffffffu, gt, src);
+                const uint32_t go = __shfl_sync(0xffffffffu, own, src);
+                any = __shfl_sync(0xffffffffu, any, src);
+                seg = __shfl_sync(0xffffffffu, seg, src);
+                slot = __shfl_sync(0xffffffffu, slot, src);
+                nodes = reinterpret_cast<const float4*>(
+                    __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(nodes), src));
+                tris = reinterpret_cast<const float4*>(
+                    __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(tris), src));
+                tmin = __shfl_sync(0xffffffffu, tmin, src);
+                tcur = __shfl_sync(0xffffffffu, tcur, src);
+                ix = __shfl_sync(0xffffffffu, ix, src);
+                iy = __shfl_sync(0xffffffffu, iy, src);
+                iz = __shfl_sync(0xffffffffu, iz, src);
+                oix = __shfl_sync(0xffffffffu, oix, src);
+                oiy = __shfl_sync(0xffffffffu, oiy, src);
+                oiz = __shfl_sync(0xffffffffu, oiz, src);
+                oct = __shfl_sync(0xffffffffu, oct, src);
+                w.ox = __shfl_sync(0xffffffffu, w.ox, src);
+                w.oy = __shfl_sync(0xffffffffu, w.oy, src);
+                w.oz = __shfl_sync(0xffffffffu, w.oz, src);
+                w.sx = __shfl_sync(0xffffffffu, w.sx, src);
+                w.sy = __shfl_sync(0xffffffffu, w.sy, src);
+                w.sz = __shfl_sync(0xffffffffu, w.sz, src);
+                w.kx = __shfl_sync(0xffffffffu, w.kx, src);
+                w.ky = __shfl_sync(0xffffffffu, w.ky, src);
+                w.kz = __shfl_sync(0xffffffffu, w.kz, src);
+                w.tmin = __shfl_sync(0xffffffffu, w.tmin, src);
+                w.tmax = __shfl_sync(0xffffffffu, w.tmax, src);
+                if (recv) {
+                    own = go;
+                    stk[0] = ge;
+                    stt[0] = gt;
+                    sp = 1;
+                    best = RSH_HIT_NONE;
+                    has = true;
+                    atomicAdd(&sh_pend[wp][own], 1u);
+                }
+            }
+            __syncwarp();
+        }
         // closest hit: entries that the ray enters beyond its current best are dropped unread (their
         // subtrees cannot hold a nearer hit: a child's box lies inside its parent's, so no child is entered
         // before its parent)
@@ -869,20 +986,24 @@ __global__ void __launch_bounds__(FW * 32, RSH_RAYS_MIN_BLOCKS) k_fused_rays(Fus
     }
 }
 
-template <int U>
-static cudaError_t launch_fused_rays_u(const FusedArgs& a, cudaStream_t s) {
+template <int U, bool SHARE>
+static cudaError_t launch_fused_rays_s(const FusedArgs& a, cudaStream_t s) {
     int dev = 0, sms = 152, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays<U>, FW * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_rays<U, SHARE>, FW * 32, 0);
     if (per_sm < 1) per_sm = 1;
     if (a.blocks_per_sm && (int)a.blocks_per_sm < per_sm) per_sm = (int)a.blocks_per_sm;
     uint32_t grid = (uint32_t)(sms * per_sm);
     const uint32_t need = (a.units_max + FW - 1) / FW;
     if (need < grid) grid = need > 0 ? need : 1;
-    k_fused_rays<U><<<grid, FW * 32, 0, s>>>(a);
+    k_fused_rays<U, SHARE><<<grid, FW * 32, 0, s>>>(a);
     note_launch();
     return cudaGetLastError();
+}
+template <int U>
+static cudaError_t launch_fused_rays_u(const FusedArgs& a, cudaStream_t s) {
+    return a.share_tail ? launch_fused_rays_s<U, true>(a, s) : launch_fused_rays_s<U, false>(a, s);
 }
 
 template <int P>

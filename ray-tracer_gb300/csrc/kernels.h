@@ -240,6 +240,7 @@ struct FusedArgs {
     uint32_t* work;
     uint32_t rays_only;            // every segment's switch level >= its tree depth: no packet phase
     uint32_t blocks_per_sm;        // CTAs per SM of the launch (0: as many as fit)
+    uint32_t share_tail;           // rays-only kernel: a drained warp shares its last rays among its lanes
     unsigned long long* node_tests;
     unsigned long long* tri_tests;
     uint32_t* err;

@@ -28,6 +28,7 @@ FLAG_FUSED = 2
 FLAG_RAH = 4
 FLAG_SOFT_SHADOWS = 8
 FLAG_NO_COMPRESS = 16
+FLAG_SEQUENTIAL_RAYS = 32
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
 NODE_DTYPE = np.dtype([("c", "<f4", 3), ("radius", "<f4"), ("axis", "<f4", 3), ("cos_spread", "<f4"),

@@ -37,8 +37,14 @@ def _both_forms(name, sample):
         st, checked = frame_check.check_frame(ctx, s, sc, s.width, s.height, s.depth, float(s.jitter),
                                               sample=sample, seed=0x5EED0000, cache=cache)
         out[form] = (st, checked)
-    # the batched form's work counters (the roofline's numerator) equal the oracle's restatement of its
-    # traversal (per-ray box descent from the root) over the frame's own secondary rays, test for test
+    # the batched form's work counters (the roofline's numerator): with RSH_FLAG_SEQUENTIAL_RAYS (every ray
+    # on one lane from its first step to its last) they equal the oracle's restatement of its traversal
+    # (per-ray box descent from the root) over the frame's own secondary rays, test for test; by default a
+    # drained warp shares its last rays' subtrees among its idle lanes, which changes the counts only through
+    # the order the hits are met in (a far subtree is no longer culled by its ray's nearer hits)
+    ctx.set_config(flags=rsh.FLAG_FUSED | rsh.FLAG_SEQUENTIAL_RAYS)
+    ctx.render(sc, s.width, s.height, s.depth)
+    seq = ctx.stats()
     lo, hi = sc.bounds()
     oh = oracle.ObjH(s.positions, ctx.config.cluster_size, lo, hi)
     npix, L = s.width * s.height, len(s.lights)
@@ -47,8 +53,9 @@ def _both_forms(name, sample):
         for rays, any_hit in ((ctx.frame_rays(b, True, npix * L), True), (ctx.frame_rays(b, False, npix), False)):
             _, (n, t) = oh.trace_box(rays[rays["tmax"] > rays["tmin"]], any_hit)
             nodes, tris = nodes + n, tris + t
+    assert (seq["node_tests"], seq["tri_tests"]) == (nodes, tris)
     st = out["batched"][0]
-    assert (st["node_tests"], st["tri_tests"]) == (nodes, tris)
+    assert abs(st["node_tests"] / nodes - 1.0) < 0.10 and abs(st["tri_tests"] / tris - 1.0) < 0.10
     sc.destroy()
     ctx.destroy()
     # both forms trace the same rays
