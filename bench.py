@@ -738,6 +738,7 @@ def batching_bench(args):
            "scenes_tris": [int(s.tri_count) for s in sd],
            "autotuned": {"packet_size": best.packet_size, "fused_blocks_per_sm": best.fused_blocks,
                          "run_compression": not (best.flags & rsh.FLAG_NO_COMPRESS),
+                         "shared_launch_ends": not (best.flags & rsh.FLAG_SEQUENTIAL_RAYS),
                          "per_scene": scene_tuning, "tuning_s": round(tune_s, 2),
                          "batch_ms_untuned": round(untuned_ms, 3), "batch_ms_tuned": round(tuned_ms, 3),
                          "context_defaults": {"grid_bits": best.grid_bits, "dir_log2": best.dir_log2,

@@ -538,8 +538,9 @@ typedef struct rsh_tune_space {
  * switch level are chosen on that scene's segments alone, one parameter at a time, and stored in the
  * scene (rsh_scene_set_tuning); then every scene at switch level 15 at once is tried against that (the
  * rays-only kernel, which skips the ray hierarchy, runs only when no segment uses packets below the root);
- * last, the packet size, the traversal launch's CTAs per SM and run compression on or off
- * (RSH_FLAG_NO_COMPRESS) are chosen with the scenes tuned. The search keeps the untuned configuration
+ * last, the packet size, the traversal launch's CTAs per SM, run compression on or off
+ * (RSH_FLAG_NO_COMPRESS) and the shared launch ends on or off (RSH_FLAG_SEQUENTIAL_RAYS) are chosen with
+ * the scenes tuned. The search keeps the untuned configuration
  * when its result is not faster on the whole batch. Points whose hash does not fit beside the batch's
  * segment tag in 31 bits are skipped. *best_ms (optional) is the whole batch's time with the final
  * choice, *untuned_ms (optional) its time with the context's configuration and no scene tuning. */

@@ -869,10 +869,12 @@ extern "C" rsh_status rsh_autotune_scenes(rsh_ctx* ctx, const rsh_batch_segment*
     }
     ms = tune_packet(ctx, segs, count, *space, reps, stream, ms);
     ms = tune_blocks(ctx, segs, count, *space, reps, stream, ms);
-    {  // run compression on or off, on the whole batch
+    // run compression on or off, then the launch's end shared among a drained warp's lanes or not, each on
+    // the whole batch
+    for (const uint32_t flag : {RSH_FLAG_NO_COMPRESS, RSH_FLAG_SEQUENTIAL_RAYS}) {
         rsh_config c = ctx->cfg;
         const rsh_config keep = c;
-        c.flags ^= RSH_FLAG_NO_COMPRESS;
+        c.flags ^= flag;
         float m2;
         if (rsh_set_config(ctx, &c) == RSH_OK && time_batch(ctx, segs, count, reps, stream, &m2) == RSH_OK &&
             m2 < ms)
