@@ -274,3 +274,33 @@ def test_empty_scene_segments_miss(ray_level):
     full.destroy()
     empty.destroy()
     ctx.destroy()
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_shared_launch_ends_change_no_result(any_hit):
+    """At the end of a rays-only launch a drained warp's idle lanes take subtrees of its rays still in flight
+    (the default); RSH_FLAG_SEQUENTIAL_RAYS keeps every ray on one lane. Both give the brute-force records and
+    flags, and the sequential counts equal the oracle's box descent of the same rays, test for test."""
+    c = rsh.Context(grid_bits=5, dir_log2=4, packet_size=8, cluster_size=8)
+    s = scenes.random_soup(60_000, np.random.default_rng(31))
+    sc = c.scene(s.positions, s.normals, s.material_ids, s.materials)
+    rng = np.random.default_rng(32)
+    rays = scenes.surface_rays(s, 90_001, rng)
+    if any_hit:
+        rays["tmax"] = rng.uniform(0.05, 40.0, len(rays)).astype(np.float32)
+    rays["tmax"][::101] = -1.0
+    bf = oracle.brute(s.positions, rays, any_hit)
+    shared = c.trace(sc, rays, any_hit, fused=True)
+    n_shared = c.test_counters(reset=True)
+    c.set_config(flags=rsh.FLAG_SEQUENTIAL_RAYS)
+    seq = c.trace(sc, rays, any_hit, fused=True)
+    n_seq = c.test_counters(reset=True)
+    c.check_device_errors()
+    assert np.array_equal(shared, bf) and np.array_equal(seq, bf)
+    lo, hi = sc.bounds()
+    oh = oracle.ObjH(s.positions, c.config.cluster_size, lo, hi)
+    _, n_orc = oh.trace_box(rays[rays["tmax"] > rays["tmin"]], any_hit)
+    assert tuple(n_seq) == tuple(int(x) for x in n_orc)
+    assert abs(n_shared[0] / n_seq[0] - 1.0) < 0.10
+    sc.destroy()
+    c.destroy()
