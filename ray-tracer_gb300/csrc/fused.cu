@@ -1,7 +1,8 @@
 // Fused persistent traversal + intersection (the batched form's single launch). Two kernels:
-//   k_fused_rays (switch level at or above every segment's tree depth, the default): each warp takes
-//     64 sorted rays at a time and runs one job per ray from the root (the per-ray job queue below);
-//     no packet phase and no ray hierarchy; the launch's last units go out as half units;
+//   k_fused_rays (switch level at or above every segment's tree depth, the default): each lane traces one
+//     ray at a time from the root, refilled from the warp's current unit of 64 sorted rays; no packet
+//     phase and no ray hierarchy; the launch's last units go out as half units, and (instance SHARE) a
+//     drained warp's last rays are shared among its idle lanes;
 //   k_fused (a lower switch level): packets of the ray hierarchy walk the upper object tree, rays leave
 //     them at the switch level, as described next.
 //
@@ -571,10 +572,10 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
 }
 
 // Rays-only form: every segment's switch level is at or above its tree's depth, so every ray is one job
-// from the root and no lane ever shares a ray. The rays descend the scene's single-ray box tree (wide.cu: an
+// from the root, traced by one lane (until, in the SHARE instance, the launch's end). The rays descend the scene's single-ray box tree (wide.cu: an
 // 8-wide tree of mixed depth built by PLOC clustering, tighter than the object-sphere hierarchy's level
 // structure) in its traversal-record form: a stack entry is a node's REC_NODE | (children - 1) << 28 |
-// record index, or a cluster's slot (its box, first triangle and triangle count). A node step reads the
+// record index, or a cluster's first triangle | (triangles - 1) << 23. A node step reads the
 // record's near planes and far planes for the ray's octant (12 float4 loads, no per-axis min / max) and
 // the entries of the children it pushes. The warp keeps no per-unit state: it takes work units
 // (RSH_RAYS_UNIT sorted rays, never straddling a segment) by atomic ticket, and every lane whose ray has
@@ -582,7 +583,10 @@ __global__ void __launch_bounds__(FW * 32, RSH_FUSED_MIN_BLOCKS) k_fused(FusedAr
 // sorted order, the ray itself from the segment's array), fetching the next unit when the current one runs
 // out. So lanes are refilled continuously and no lane waits for the slowest ray of a unit; a lane writes its
 // ray's result (shadow flag or hit record) itself when the ray ends. The launch's last units go out as
-// pieces of RSH_RAYS_UNIT / RSH_TAIL_SPLIT rays.
+// pieces of RSH_RAYS_UNIT / RSH_TAIL_SPLIT rays. Single long rays (up to 20x the median ray's tests) still
+// hold an SM after the others have finished; the SHARE instance (the default) lets a drained warp's idle
+// lanes take their subtrees (described at its loop's top), at the price of about 4% on every step, which
+// the instance without it (RSH_FLAG_SEQUENTIAL_RAYS) does not pay.
 //
 // Box test (box_hit_fma): t = b * (1 / d) - o * (1 / d) as one fused multiply-add per plane, with direction
 // components below 1e-20 in magnitude replaced by +-1e-20 (finite reciprocals, no inf - inf), and the
