@@ -94,17 +94,22 @@ RSH_DEV void batch_key_out(const BatchKeyOut& bk, uint32_t slot, bool in_range, 
 // One thread per pixel: the pixel's surface point and normal are read and the normal normalised once,
 // then its V = L x S slots are written (slot = x + W (v + V y), RayTracer.cu:700-702 with S samples per
 // light), each with the same arithmetic as a thread per slot would use. The block's rays are counted once
-// (BatchKeyOut).
+// (BatchKeyOut). The light positions are copied to shared memory first: indexing the parameter bank with
+// the light number is a constant load with a register index, which the SM issues through its narrow
+// address-divergence pipe, and three of those per slot made that pipe the kernel's bound.
 __global__ void __launch_bounds__(128) k_raygen_shadow(const float4* __restrict__ spos,
                                                        const float4* __restrict__ snrm, uint32_t w, uint32_t h,
                                                        LightsP lights, float eps, HashP hp, rsh_ray* rays,
                                                        uint32_t* keys, BatchKeyOut bk) {
     __shared__ uint32_t s_cnt;
+    __shared__ float s_lp[8 * 3];
     const uint32_t L = lights.count, S = lights.samples ? lights.samples : 1u, V = L * S;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in_range = pix < w * h;
     uint32_t nvalid = 0;
     if (threadIdx.x == 0) s_cnt = 0u;
+    if (threadIdx.x < 3u * L) s_lp[threadIdx.x] = (&lights.pos[0][0])[threadIdx.x];
+    __syncthreads();
     if (in_range) {
         const uint32_t y = pix / w, x = pix - y * w;
         const float4 p4 = __ldg(spos + pix);
@@ -118,7 +123,7 @@ __global__ void __launch_bounds__(128) k_raygen_shadow(const float4* __restrict_
             float4 ro = make_float4(0.f, 0.f, 0.f, 0.f), rd = make_float4(0.f, 0.f, 0.f, -1.f);
             uint32_t key = RSH_KEY_NONE;
             if (surface) {
-                const v3 lp = mk3(lights.pos[l][0], lights.pos[l][1], lights.pos[l][2]);
+                const v3 lp = mk3(s_lp[3u * l], s_lp[3u * l + 1u], s_lp[3u * l + 2u]);
                 const v3 vl = p - lp;
                 const float len = len3(vl);
                 const v3 d = v3{vl.x / len, vl.y / len, vl.z / len};
@@ -158,7 +163,6 @@ __global__ void __launch_bounds__(128) k_raygen_shadow(const float4* __restrict_
         }
     }
     if (bk.keys) {
-        __syncthreads();
         const uint32_t c = __reduce_add_sync(0xffffffffu, nvalid);
         if (lane_id() == 0 && c) atomicAdd(&s_cnt, c);
         __syncthreads();

@@ -65,7 +65,15 @@ RSH_DEV float soft_weight(uint32_t k) {
     return 0.525f / 16.0f;
 }
 
+// The lights are copied to shared memory first: indexing the parameter bank with the light number would
+// be a constant load with a register index per field, issued through the SM's narrow address-divergence
+// pipe.
 __global__ void k_shade(ShadeArgs a) {
+    __shared__ rsh_light s_light[8];
+    static_assert(sizeof(rsh_light) == 8 * sizeof(float), "rsh_light is 8 floats");
+    if (threadIdx.x < 8u * a.lights)
+        reinterpret_cast<float*>(s_light)[threadIdx.x] = reinterpret_cast<const float*>(a.light)[threadIdx.x];
+    __syncthreads();
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= a.w * a.h) return;
     float4 acc = a.bounce == 0 ? make_float4(0.f, 0.f, 0.f, 1.f) : a.accum[pix];
@@ -100,7 +108,7 @@ __global__ void k_shade(ShadeArgs a) {
                     if (a.shadow[x + a.w * ((l * S + k) + a.lights * S * y)] != RSH_OCCLUDED) sf += soft_weight(k);
                 factor = log2f(1.0f + sf * 2.0f);
             }
-            const rsh_light& L = a.light[l];
+            const rsh_light& L = s_light[l];
             v3 ld = v3{L.position[0], L.position[1], L.position[2]} - p;
             const float dist = len3(ld);
             ld = v3{ld.x / dist, ld.y / dist, ld.z / dist};
