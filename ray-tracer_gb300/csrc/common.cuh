@@ -47,6 +47,19 @@ RSH_DEV void store_ray(rsh_ray* rays, uint32_t i, float4 o, float4 d) {
     p[0] = o;
     p[1] = d;
 }
+// The same ray as one 256-bit store (st.global.v8.f32, sm_100 and later): each lane writes its whole
+// 32-byte sector in one instruction. Only for an array whose base is 32-byte aligned (a32, checked by the
+// caller once per thread); otherwise the two 16-byte stores above.
+RSH_DEV void store_ray32(rsh_ray* rays, uint32_t i, float4 o, float4 d, bool a32) {
+    if (a32) {
+        float* p = reinterpret_cast<float*>(rays) + 8ull * i;
+        asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(o.x), "f"(o.y),
+                     "f"(o.z), "f"(o.w), "f"(d.x), "f"(d.y), "f"(d.z), "f"(d.w)
+                     : "memory");
+    } else {
+        store_ray(rays, i, o, d);
+    }
+}
 
 // ------------------------------------------------------------------ device error word
 // Bounded device waits and overflow checks report here (never __trap()); the host reads it back with

@@ -96,16 +96,18 @@ RSH_DEV void batch_key_out(const BatchKeyOut& bk, uint32_t slot, bool in_range, 
 // light), each with the same arithmetic as a thread per slot would use. The block's rays are counted once
 // (BatchKeyOut). The light positions are copied to shared memory first: indexing the parameter bank with
 // the light number is a constant load with a register index, which the SM issues through its narrow
-// address-divergence pipe, and three of those per slot made that pipe the kernel's bound.
-__global__ void __launch_bounds__(128) k_raygen_shadow(const float4* __restrict__ spos,
-                                                       const float4* __restrict__ snrm, uint32_t w, uint32_t h,
-                                                       LightsP lights, float eps, HashP hp, rsh_ray* rays,
-                                                       uint32_t* keys, BatchKeyOut bk) {
+// address-divergence pipe, and three of those per slot made that pipe the kernel's bound. 12 blocks per SM
+// (at most 40 registers, no spills) keep enough warps in flight to cover the surface reads.
+__global__ void __launch_bounds__(128, 12) k_raygen_shadow(const float4* __restrict__ spos,
+                                                           const float4* __restrict__ snrm, uint32_t w, uint32_t h,
+                                                           LightsP lights, float eps, HashP hp, rsh_ray* rays,
+                                                           uint32_t* keys, BatchKeyOut bk) {
     __shared__ uint32_t s_cnt;
     __shared__ float s_lp[8 * 3];
     const uint32_t L = lights.count, S = lights.samples ? lights.samples : 1u, V = L * S;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in_range = pix < w * h;
+    const bool a32 = (reinterpret_cast<uintptr_t>(rays) & 31u) == 0u;
     uint32_t nvalid = 0;
     if (threadIdx.x == 0) s_cnt = 0u;
     if (threadIdx.x < 3u * L) s_lp[threadIdx.x] = (&lights.pos[0][0])[threadIdx.x];
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(128) k_raygen_shadow(const float4* __restrict_
                 }
             }
             // an empty slot holds an explicit no-ray (tmax < tmin) for consumers without keys
-            store_ray(rays, slot, ro, rd);
+            store_ray32(rays, slot, ro, rd, a32);
             if (keys) keys[slot] = key;
             if (bk.keys) {
                 bk.keys[slot] = valid ? bk.tag | (ray_hash(ro.x, ro.y, ro.z, rd.x, rd.y, rd.z, bk.hp, 0u) >> bk.drop)
@@ -209,6 +211,7 @@ __global__ void k_raygen_reflect(const float4* __restrict__ spos, const float4* 
                                  rsh_ray* rays, uint32_t* keys, BatchKeyOut bk) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in_range = slot < n;
+    const bool a32 = (reinterpret_cast<uintptr_t>(rays) & 31u) == 0u;
     bool valid = false;
     float4 ro = make_float4(0.f, 0.f, 0.f, 0.f), rd = make_float4(0.f, 0.f, 0.f, -1.f);
     if (in_range) {
@@ -238,13 +241,13 @@ __global__ void k_raygen_reflect(const float4* __restrict__ spos, const float4* 
                 const v3 o = p + r * eps;
                 ro = make_float4(o.x, o.y, o.z, eps);
                 rd = make_float4(r.x, r.y, r.z, __int_as_float(0x7f800000));
-                store_ray(rays, slot, ro, rd);
+                store_ray32(rays, slot, ro, rd, a32);
                 key = keys ? ray_hash(o.x, o.y, o.z, r.x, r.y, r.z, hp, 0u) : 0u;
                 valid = true;
             }
         }
         // no ray: stored as such, also for the next bounce, which reads this array as its incident rays
-        if (!valid) store_ray(rays, slot, ro, rd);
+        if (!valid) store_ray32(rays, slot, ro, rd, a32);
         if (keys) keys[slot] = key;
     }
     if (bk.keys) batch_key_out(bk, slot, in_range, valid, ro, rd);

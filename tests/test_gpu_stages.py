@@ -215,6 +215,44 @@ def test_raygen_secondary_bitexact(cornell, jitter):
     assert d_r2.numpy()[v].tobytes() == o_r2[v].tobytes()
 
 
+def test_raygen_rays_at_16_byte_offset(cornell):
+    """Ray arrays are written with one 32-byte store per ray when their base is 32-byte aligned; a base that
+    is only 16-byte aligned takes the two 16-byte stores and must give the same bytes."""
+    s = cornell
+    W, H = 40, 32
+    cam, spos, snrm = _primary_surface(s, W, H)
+    lo, hi = _lohi(s)
+    lp = np.array([l["position"] for l in s.lights], np.float32)
+    hp = rsh.hash_params(lo, hi, 5, 4, 2)
+    d_spos, d_snrm = rsh.DeviceArray.from_numpy(spos), rsh.DeviceArray.from_numpy(snrm)
+    larr = rsh.make_lights(s.lights)
+    eye = (C.c_float * 3)(*cam.eye)
+    hp0 = rsh.hash_params(lo, hi, 5, 4, 0)
+    for off in (0, 16):
+        n = W * H * len(s.lights)
+        buf = rsh.DeviceArray(32 * n + 32, np.uint8, zero=True)
+        d_keys = rsh.DeviceArray(n, np.uint32)
+        rsh.check(rsh.lib().rsh_raygen_shadow(d_spos.ptr, d_snrm.ptr, W, H, larr, len(s.lights), 0.01, C.byref(hp),
+                                              buf.ptr + off, d_keys.ptr, None), "shadow")
+        orays, okeys = oracle.raygen_shadow(spos, snrm, W, H, lp, 0.01, lo, np.array(hp.scale[:]), 5, 4)
+        got = buf.numpy()[off:off + 32 * n].view(rsh.RAY_DTYPE)
+        v = okeys != rsh.KEY_NONE
+        assert v.sum() > 100
+        assert np.array_equal(d_keys.numpy(), okeys)
+        assert got[v].tobytes() == orays[v].tobytes()
+        m = W * H
+        rbuf = rsh.DeviceArray(32 * m + 32, np.uint8, zero=True)
+        d_k = rsh.DeviceArray(m, np.uint32)
+        rsh.check(rsh.lib().rsh_raygen_reflect(d_spos.ptr, d_snrm.ptr, None, eye, W, H, 0.01, 0.0, 77, 0,
+                                               C.byref(hp0), rbuf.ptr + off, d_k.ptr, None), "reflect")
+        o_r, o_k = oracle.raygen_reflect(spos, snrm, None, cam.as_array()[:3], W, H, 0.01, 0.0, 77, 0, lo,
+                                         np.array(hp0.scale[:]), 5, 4)
+        assert np.array_equal(d_k.numpy(), o_k)
+        v = o_k != rsh.KEY_NONE
+        assert v.sum() > 100
+        assert rbuf.numpy()[off:off + 32 * m].view(rsh.RAY_DTYPE)[v].tobytes() == o_r[v].tobytes()
+
+
 # ---------------------------------------------------------------- compress / sort / decompress
 def _keys_cases():
     rng = np.random.default_rng(5)
