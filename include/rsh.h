@@ -400,8 +400,9 @@ rsh_status rsh_compress(rsh_ctx* ctx, const uint32_t* keys, uint32_t n_slots, ui
 /* rsh_compress without allocating: same outputs and semantics, no context, no cudaMalloc/cudaFree.
  * For callers that may not allocate device memory themselves or let a library do it: hosts that own and
  * pre-partition all device memory, and loops that allocate once at start-up and must not allocate while
- * they run. No counterpart in the reference. The scratch (per-tile summaries and prefixes) is a static device array of 196,684 bytes that every GPU loading the
- * library keeps until the process exits; n_slots above 16,777,216 is rejected with RSH_ERR_INVALID. The
+ * they run. No counterpart in the reference. The scratch (per-tile summaries and prefixes) is a static
+ * device array of 196,684 bytes that every GPU loading the library keeps until the process exits;
+ * n_slots above 16,777,216 is rejected with RSH_ERR_INVALID. The
  * first call on a device looks up the array's device address (call it once before any stream capture);
  * that address is kept for the process, so a cudaDeviceReset of that device invalidates it.
  * All calls share the array: calls that overlap on the GPU race, so serialise them on one stream. */
