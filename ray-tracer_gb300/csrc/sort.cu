@@ -60,22 +60,44 @@ __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n_max,
     }
     // each thread counts a contiguous run of keys and adds equal consecutive digits up before one shared
     // atomic: the keys arrive coherent (hash runs in ray order), so their upper digits repeat in long runs
-    // that would otherwise pile up on one shared counter
+    // that would otherwise pile up on one shared counter. The run is loaded once into registers (four
+    // 16-byte loads when the keys are 16-byte aligned) and every pass counts from there: one 4-byte load
+    // per key and pass, with the lanes' runs 64 bytes apart, kept the L1 busy a line per lane.
     {
         constexpr uint32_t RUN = 16;
         const uint32_t nth = gridDim.x * blockDim.x;
+        const bool a16 = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0u;
         for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * RUN; base < n; base += nth * RUN) {
-            const uint32_t end = min(n, base + RUN);
+            const uint32_t cnt = min(n - base, RUN);
+            uint32_t k[RUN];
+            if (a16 && cnt == RUN) {
+                const uint4* q = reinterpret_cast<const uint4*>(keys + base);
+#pragma unroll
+                for (uint32_t j = 0; j < RUN / 4u; ++j) {
+                    const uint4 v = __ldg(q + j);
+                    k[4u * j] = v.x;
+                    k[4u * j + 1u] = v.y;
+                    k[4u * j + 2u] = v.z;
+                    k[4u * j + 3u] = v.w;
+                }
+            } else {
+#pragma unroll
+                for (uint32_t i = 0; i < RUN; ++i) k[i] = i < cnt ? __ldg(keys + base + i) : 0u;
+            }
             for (uint32_t p = 0; p < passes; ++p) {
-                uint32_t prev = (__ldg(keys + base) >> (8u * p)) & 255u, run = 0;
-                for (uint32_t i = base; i < end; ++i) {
-                    const uint32_t d = (__ldg(keys + i) >> (8u * p)) & 255u;
-                    if (d != prev) {
-                        atomicAdd(&sh[p][prev], run);
-                        prev = d;
-                        run = 0;
+                const uint32_t sh_p = 8u * p;
+                uint32_t prev = (k[0] >> sh_p) & 255u, run = 0;
+#pragma unroll
+                for (uint32_t i = 0; i < RUN; ++i) {
+                    if (i < cnt) {
+                        const uint32_t d = (k[i] >> sh_p) & 255u;
+                        if (d != prev) {
+                            atomicAdd(&sh[p][prev], run);
+                            prev = d;
+                            run = 0;
+                        }
+                        ++run;
                     }
-                    ++run;
                 }
                 atomicAdd(&sh[p][prev], run);
             }

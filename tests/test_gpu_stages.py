@@ -323,6 +323,23 @@ def test_sort_pairs_stable_bitexact(ctx, n, bits):
         assert np.array_equal(d_vo.numpy(m), vo)
 
 
+@pytest.mark.parametrize("n", [5, 100_003])
+def test_sort_pairs_keys_at_4_byte_offset(ctx, n):
+    """The histogram pass loads 16 keys with four 16-byte loads when the key array is 16-byte aligned;
+    a key array that starts 4 bytes into an allocation takes the 4-byte loads and sorts the same."""
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 1 << 20, n + 1, dtype=np.uint64).astype(np.uint32)
+    keys[1: n // 2] = keys[n // 2]
+    d_k = rsh.DeviceArray.from_numpy(keys)
+    d_ko = rsh.DeviceArray(n, np.uint32)
+    d_vo = rsh.DeviceArray(n, np.uint32)
+    rsh.check(rsh.lib().rsh_sort_pairs(ctx.handle, d_k.ptr + 4, None, d_ko.ptr, d_vo.ptr, n, None, 20, None), "sort")
+    ctx.check_device_errors()
+    ko, vo = oracle.sort_pairs(keys[1:], None, 20)
+    assert np.array_equal(d_ko.numpy(n), ko)
+    assert np.array_equal(d_vo.numpy(n), vo)
+
+
 @pytest.mark.parametrize("name", ["runs", "big", "all_equal", "one", "tile_edges"])
 def test_decompress_bitexact(ctx, name):
     keys = _keys_cases()[name]
